@@ -1,0 +1,84 @@
+"""ctypes binding to libdd_gb300.so (the C ABI declared in include/dd_gb300.h).
+
+Status codes are mapped to the exception classes the reference raises for the
+same conditions (ValueError for bad arguments, NotImplementedError for
+unsupported shapes/options, RuntimeError for CUDA failures).  There is no CPU
+fallback: if the library is missing, every entry point raises.
+"""
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libdd_gb300.so")
+
+DD_OK, DD_ERR_INVALID, DD_ERR_UNSUPPORTED, DD_ERR_CUDA, DD_ERR_TIMEOUT, DD_ERR_WORKSPACE = range(6)
+DD_FP64, DD_FP32 = 0, 1
+
+_EXC = {
+    DD_ERR_INVALID: ValueError,
+    DD_ERR_UNSUPPORTED: NotImplementedError,
+    DD_ERR_CUDA: RuntimeError,
+    DD_ERR_TIMEOUT: TimeoutError,
+    DD_ERR_WORKSPACE: ValueError,
+}
+
+P = ctypes.c_void_p
+PP = ctypes.POINTER(ctypes.c_void_p)
+I = ctypes.c_int
+I64 = ctypes.c_int64
+D = ctypes.c_double
+SZ = ctypes.c_size_t
+
+# name -> argtypes; every function returns int status unless listed in _RESTYPE
+SIGNATURES = {
+    "dd_version": [],
+    "dd_last_error": [],
+    "dd_plan_create": [I, ctypes.POINTER(I64), P, P, P, I, I, I, ctypes.POINTER(P)],
+    "dd_plan_destroy": [P],
+    "dd_plan_workspace_size": [P, I, I, ctypes.POINTER(SZ)],
+    "dd_fft_r2c": [P, I, PP, PP, I, P, SZ, P],
+    "dd_fft_c2r": [P, I, PP, PP, I, P, SZ, P],
+    "dd_dealias": [P, P, P],
+    "dd_euler": [P, P, P, D, I64, P],
+    "dd_etd1": [I, P, P, P, P, D, I64, P],
+    "dd_etd2rk1": [I, P, P, P, P, P, D, I64, P],
+    "dd_etd2rk2": [I, P, P, P, P, P, D, I64, P],
+    "dd_phi_table": [I, D, I, D, I, P, P],
+}
+_RESTYPE = {"dd_last_error": ctypes.c_char_p}
+
+_lib = None
+
+
+class LibraryMissing(ImportError):
+    pass
+
+
+def lib():
+    """Load the CUDA library (raises LibraryMissing if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.isfile(LIB_PATH):
+            raise LibraryMissing("%s is not built; run __graft_entry__.build() (nvcc) first" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        for name, args in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = _RESTYPE.get(name, ctypes.c_int)
+        _lib = L
+    return _lib
+
+
+def check(rc, what=""):
+    if rc != DD_OK:
+        msg = lib().dd_last_error().decode(errors="replace")
+        raise _EXC.get(rc, RuntimeError)("%s%s" % (what + ": " if what else "", msg))
+
+
+def call(name, *args):
+    check(getattr(lib(), name)(*args), name)
+
+
+def ptr_array(ptrs):
+    arr = (ctypes.c_void_p * len(ptrs))(*[ctypes.c_void_p(int(p)) for p in ptrs])
+    return ctypes.cast(arr, PP), arr

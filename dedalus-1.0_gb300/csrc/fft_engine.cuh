@@ -1,0 +1,197 @@
+// Batched shared-memory FFT engine.
+//
+// A thread block holds P pencils of length L in a shared-memory tile laid out
+// [element][pencil] (pencil fastest, row stride PS >= P, PS odd so that both
+// pencil-contiguous and element-contiguous accesses are bank-conflict free
+// for 8- and 16-byte complex entries).  The transform is a mixed-radix
+// Stockham autosort (decimation in time): each pass reads R inputs at stride
+// L/R, twiddles by W_{Ns R}^{r k}, does an in-register radix-R DFT and writes
+// the outputs at ((j-k) R + k) + r Ns.  Radices are 2, 4, 8 and 16; in-register
+// twiddles are exact constants (multiples of pi/8), the inter-pass twiddles
+// come from a per-length table W_L^m = exp(-2 pi i m / L) staged in shared
+// memory (conjugated for the inverse transform).
+//
+// Forward transforms use exp(-i...), inverse exp(+i...); neither is scaled.
+#pragma once
+#include "dd_common.cuh"
+
+namespace dd {
+
+// --------------------------------------------------- in-register DFTs
+// cos/sin of pi/8 and pi/4, correctly rounded decimal expansions.
+#define DD_C8 0.92387953251128675613
+#define DD_S8 0.38268343236508977173
+#define DD_R2 0.70710678118654752440
+
+// v * W_R^m (forward) or v * conj(W_R^m) (inverse), m a compile-time constant
+// with R in {8, 16}; trivial multiples are exact.
+template <int M, int R, bool INV, typename T>
+__device__ __forceinline__ C<T> tw_const(C<T> v) {
+    constexpr int m16 = ((M % R) * (16 / R)) % 16;  // angle in units of 2 pi / 16
+    if constexpr (m16 == 0) {
+        return v;
+    } else if constexpr (m16 == 4) {
+        return mul_mi<INV>(v);
+    } else if constexpr (m16 == 8) {
+        return mk<T>(-v.x, -v.y);
+    } else if constexpr (m16 == 12) {
+        return mul_mi<!INV>(v);
+    } else {
+        // forward twiddle exp(-2 pi i m16/16) = (c, -s)
+        constexpr double ang_c[16] = {1, DD_C8, DD_R2, DD_S8, 0, -DD_S8, -DD_R2, -DD_C8,
+                                      -1, -DD_C8, -DD_R2, -DD_S8, 0, DD_S8, DD_R2, DD_C8};
+        constexpr double ang_s[16] = {0, DD_S8, DD_R2, DD_C8, 1, DD_C8, DD_R2, DD_S8,
+                                      0, -DD_S8, -DD_R2, -DD_C8, -1, -DD_C8, -DD_R2, -DD_S8};
+        const T c = T(ang_c[m16]);
+        const T s = INV ? T(ang_s[m16]) : T(-ang_s[m16]);
+        return mk<T>(v.x * c - v.y * s, v.x * s + v.y * c);
+    }
+}
+
+template <bool INV, typename T>
+__device__ __forceinline__ void dft2(C<T>& a, C<T>& b) {
+    C<T> t = a;
+    a = t + b;
+    b = t - b;
+}
+
+template <bool INV, typename T>
+__device__ __forceinline__ void dft4(C<T>& a0, C<T>& a1, C<T>& a2, C<T>& a3) {
+    C<T> t0 = a0 + a2, t1 = a0 - a2, t2 = a1 + a3, t3 = mul_mi<INV>(a1 - a3);
+    a0 = t0 + t2;
+    a2 = t0 - t2;
+    a1 = t1 + t3;
+    a3 = t1 - t3;
+}
+
+// In-place DFT of R values v[0..R-1], natural order in and out.
+template <int R, bool INV, typename T>
+__device__ __forceinline__ void dft(C<T>* v) {
+    if constexpr (R == 2) {
+        dft2<INV>(v[0], v[1]);
+    } else if constexpr (R == 4) {
+        dft4<INV>(v[0], v[1], v[2], v[3]);
+    } else if constexpr (R == 8) {
+        // even/odd split: E = DFT4(v0,v2,v4,v6), O = DFT4(v1,v3,v5,v7)
+        C<T> e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
+        C<T> o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
+        dft4<INV>(e0, e1, e2, e3);
+        dft4<INV>(o0, o1, o2, o3);
+        o1 = tw_const<1, 8, INV>(o1);
+        o2 = tw_const<2, 8, INV>(o2);
+        o3 = tw_const<3, 8, INV>(o3);
+        v[0] = e0 + o0; v[4] = e0 - o0;
+        v[1] = e1 + o1; v[5] = e1 - o1;
+        v[2] = e2 + o2; v[6] = e2 - o2;
+        v[3] = e3 + o3; v[7] = e3 - o3;
+    } else if constexpr (R == 16) {
+        // 4 x 4: n = 4 n1 + n2; Y[n2][k1] = DFT4_n1 v[4 n1 + n2]; twiddle
+        // W16^(n2 k1); X[k1 + 4 k2] = DFT4_n2 Y[n2][k1].
+        C<T> y[4][4];
+#pragma unroll
+        for (int n2 = 0; n2 < 4; n2++) {
+            y[n2][0] = v[n2]; y[n2][1] = v[4 + n2]; y[n2][2] = v[8 + n2]; y[n2][3] = v[12 + n2];
+            dft4<INV>(y[n2][0], y[n2][1], y[n2][2], y[n2][3]);
+        }
+        y[1][1] = tw_const<1, 16, INV>(y[1][1]);
+        y[1][2] = tw_const<2, 16, INV>(y[1][2]);
+        y[1][3] = tw_const<3, 16, INV>(y[1][3]);
+        y[2][1] = tw_const<2, 16, INV>(y[2][1]);
+        y[2][2] = tw_const<4, 16, INV>(y[2][2]);
+        y[2][3] = tw_const<6, 16, INV>(y[2][3]);
+        y[3][1] = tw_const<3, 16, INV>(y[3][1]);
+        y[3][2] = tw_const<6, 16, INV>(y[3][2]);
+        y[3][3] = tw_const<9, 16, INV>(y[3][3]);
+#pragma unroll
+        for (int k1 = 0; k1 < 4; k1++) {
+            C<T> a0 = y[0][k1], a1 = y[1][k1], a2 = y[2][k1], a3 = y[3][k1];
+            dft4<INV>(a0, a1, a2, a3);
+            v[k1] = a0; v[k1 + 4] = a1; v[k1 + 8] = a2; v[k1 + 12] = a3;
+        }
+    } else {
+        static_assert(R == 2 || R == 4 || R == 8 || R == 16, "unsupported radix");
+    }
+}
+
+// --------------------------------------------------- pencil configuration
+// Per length: pencils per block (P), threads per block (NT) and radix
+// schedule (R1, R2, R3; 1 = unused).  Threads per pencil TPP = NT / P and every
+// pass has (L / R) / TPP butterflies per thread, an integer >= 1.
+template <int L> struct FFTCfg;
+template <> struct FFTCfg<8>    { static constexpr int P = 64, NT = 64,  R1 = 8,  R2 = 1,  R3 = 1; };
+template <> struct FFTCfg<16>   { static constexpr int P = 64, NT = 256, R1 = 4,  R2 = 4,  R3 = 1; };
+template <> struct FFTCfg<32>   { static constexpr int P = 64, NT = 256, R1 = 8,  R2 = 4,  R3 = 1; };
+template <> struct FFTCfg<64>   { static constexpr int P = 32, NT = 256, R1 = 8,  R2 = 8,  R3 = 1; };
+template <> struct FFTCfg<128>  { static constexpr int P = 32, NT = 256, R1 = 16, R2 = 8,  R3 = 1; };
+template <> struct FFTCfg<256>  { static constexpr int P = 16, NT = 256, R1 = 16, R2 = 16, R3 = 1; };
+template <> struct FFTCfg<512>  { static constexpr int P = 8,  NT = 256, R1 = 8,  R2 = 8,  R3 = 8; };
+template <> struct FFTCfg<1024> { static constexpr int P = 4,  NT = 256, R1 = 16, R2 = 16, R3 = 4; };
+
+template <int L>
+struct Pencil {
+    static constexpr int P = FFTCfg<L>::P;
+    static constexpr int NT = FFTCfg<L>::NT;
+    static constexpr int PS = P + 1;  // odd row stride (complex entries)
+    static constexpr int TPP = NT / P;
+    template <typename T>
+    static constexpr size_t smem_bytes() { return sizeof(C<T>) * ((size_t)L * PS + L); }
+};
+
+// One Stockham pass of radix R with current sub-transform length NS.
+template <typename T, int L, int R, int NS, bool INV>
+__device__ __forceinline__ void stockham_pass(C<T>* tile, const C<T>* tw, int p, int jt) {
+    constexpr int PS = Pencil<L>::PS;
+    constexpr int TPP = Pencil<L>::TPP;
+    constexpr int NB = L / R;          // butterflies per pencil
+    constexpr int BPT = NB / TPP;      // butterflies per thread
+    static_assert(BPT >= 1 && NB % TPP == 0, "bad radix schedule");
+    C<T> v[BPT][R];
+#pragma unroll
+    for (int b = 0; b < BPT; b++) {
+        const int j = jt + TPP * b;
+#pragma unroll
+        for (int r = 0; r < R; r++) v[b][r] = tile[(j + r * NB) * PS + p];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int b = 0; b < BPT; b++) {
+        const int j = jt + TPP * b;
+        const int k = j & (NS - 1);
+        if constexpr (NS > 1) {
+            constexpr int STEP = L / (NS * R);
+#pragma unroll
+            for (int r = 1; r < R; r++) {
+                const C<T> w = tw[(r * k) * STEP];
+                v[b][r] = INV ? cmulc(v[b][r], w) : cmul(v[b][r], w);
+            }
+        }
+        dft<R, INV>(v[b]);
+        const int d = (j - k) * R + k;
+#pragma unroll
+        for (int r = 0; r < R; r++) tile[(d + r * NS) * PS + p] = v[b][r];
+    }
+    __syncthreads();
+}
+
+// Transform every pencil of the tile in place.  Must be called by all NT
+// threads of the block; the caller synchronises before (tile filled) and this
+// returns synchronised (tile holds the result in natural order).
+template <typename T, int L, bool INV>
+__device__ __forceinline__ void pencil_fft(C<T>* tile, const C<T>* tw) {
+    using Cfg = FFTCfg<L>;
+    constexpr int P = Pencil<L>::P;
+    const int p = threadIdx.x % P;
+    const int jt = threadIdx.x / P;
+    stockham_pass<T, L, Cfg::R1, 1, INV>(tile, tw, p, jt);
+    if constexpr (Cfg::R2 > 1) stockham_pass<T, L, Cfg::R2, Cfg::R1, INV>(tile, tw, p, jt);
+    if constexpr (Cfg::R3 > 1) stockham_pass<T, L, Cfg::R3, Cfg::R1 * Cfg::R2, INV>(tile, tw, p, jt);
+    static_assert(Cfg::R1 * Cfg::R2 * Cfg::R3 == L, "radix schedule does not multiply to L");
+}
+
+// Stage the length-L twiddle table (global, L entries) into shared memory.
+template <typename T, int L>
+__device__ __forceinline__ void load_twiddles(C<T>* s_tw, const typename Vec2<T>::type* g_tw) {
+    for (int i = threadIdx.x; i < L; i += blockDim.x) s_tw[i] = ldc<T>(g_tw + i);
+}
+
+}  // namespace dd

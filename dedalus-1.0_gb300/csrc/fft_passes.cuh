@@ -1,0 +1,252 @@
+// Transform passes: one kernel template moves a tile of pencils between
+// global memory and shared memory around the pencil FFT engine.  The source
+// and destination layouts (pruned/dealiased loads, compact intermediates,
+// Hermitian packing of real rows, scaling) live in small "Op" structs whose
+// load/store members are inlined into the kernel, so every pass is a single
+// read and a single write of its data.
+//
+// Grid: x = (pencil tile) * nfield + field, y = slow index (up to 65535), z =
+// slow index / 65535.  The field index varies fastest so that the blocks
+// working on the same tile for different fields run together and re-reads of
+// a shared input hit L2.
+// LD_E / ST_E select whether consecutive threads walk elements (the pencil is
+// contiguous in memory) or pencils (pencils are adjacent in memory) when
+// moving data to and from the tile, so global accesses stay coalesced.
+#pragma once
+#include "fft_engine.cuh"
+#include "geometry.cuh"
+
+namespace dd {
+
+template <typename T, int L, bool INV, bool LD_E, bool ST_E, class Op>
+__global__ void __launch_bounds__(FFTCfg<L>::NT) k_pass(const Op op, int nfield) {
+    extern __shared__ __align__(16) unsigned char dd_smem[];
+    constexpr int P = Pencil<L>::P, PS = Pencil<L>::PS, NT = Pencil<L>::NT;
+    C<T>* tile = reinterpret_cast<C<T>*>(dd_smem);
+    C<T>* tw = tile + L * PS;
+    load_twiddles<T, L>(tw, op.tw);
+    const int fld = blockIdx.x % nfield;
+    const int f0 = (blockIdx.x / nfield) * P;
+    const int s = blockIdx.y + 65535 * blockIdx.z;
+    const int npen = op.npencil();
+    for (int idx = threadIdx.x; idx < L * P; idx += NT) {
+        const int e = LD_E ? idx % L : idx / P;
+        const int p = LD_E ? idx / L : idx % P;
+        const int f = f0 + p;
+        tile[e * PS + p] = (f < npen) ? op.load(fld, s, e, f) : zero<T>();
+    }
+    __syncthreads();
+    pencil_fft<T, L, INV>(tile, tw);
+    const int nst = op.nstore();
+    for (int idx = threadIdx.x; idx < nst * P; idx += NT) {
+        const int e = ST_E ? idx % nst : idx / P;
+        const int p = ST_E ? idx / nst : idx % P;
+        const int f = f0 + p;
+        if (f < npen) op.store(fld, s, e, f, tile + p, PS);
+    }
+}
+
+template <typename T, int L, bool INV, bool LD_E, bool ST_E, class Op>
+int launch_pass(const Op& op, int npencil, int nslow, int nfield, cudaStream_t st) {
+    constexpr int P = Pencil<L>::P, NT = Pencil<L>::NT;
+    const size_t smem = Pencil<L>::template smem_bytes<T>();
+    auto kern = k_pass<T, L, INV, LD_E, ST_E, Op>;
+    static bool configured = false;  // per instantiation
+    if (!configured) {
+        DD_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        configured = true;
+    }
+    if (npencil <= 0 || nslow <= 0 || nfield <= 0) return DD_OK;
+    if (nslow > 65535 && nslow % 65535 != 0) {
+        set_error("pass: slow extent %d must be <= 65535 or a multiple of it", nslow);
+        return DD_ERR_UNSUPPORTED;
+    }
+    dim3 grid(cdiv(npencil, P) * nfield, nslow > 65535 ? 65535 : nslow, nslow > 65535 ? nslow / 65535 : 1);
+    kern<<<grid, NT, smem, st>>>(op, nfield);
+    DD_LAUNCH_CHECK();
+    return DD_OK;
+}
+
+// ============================================================ 3D operators
+// Inverse along kz: K[ky][kz][kx] (kept entries) -> W1[kyc][z][kxc].
+template <typename T, typename KT>
+struct OpZInv3 {
+    using V = typename Vec2<T>::type;
+    using KV = typename Vec2<KT>::type;
+    Geo3 g; CPtrs in; Ptrs out; const V* tw;
+    __device__ int npencil() const { return g.Kx; }
+    __device__ int nstore() const { return g.Nz; }
+    __device__ C<T> load(int fld, int kyc, int e, int kx) const {
+        if (!kept_full(e, g.Nz, g.Mz)) return zero<T>();
+        const int ky = compact_to_full(kyc, g.Ny, g.Ky);
+        const KV v = ((const KV*)in.p[fld])[((int64_t)ky * g.Nz + e) * g.Nh + kx];
+        return mk<T>((T)v.x, (T)v.y);
+    }
+    __device__ void store(int fld, int kyc, int e, int kx, const C<T>* col, int PS) const {
+        stc<T>((V*)out.p[fld] + ((int64_t)kyc * g.Nz + e) * g.Kx + kx, col[e * PS]);
+    }
+};
+
+// Inverse along ky: W1[kyc][z][kxc] -> W2[z][y][kxc].
+template <typename T>
+struct OpYInv3 {
+    using V = typename Vec2<T>::type;
+    Geo3 g; CPtrs in; Ptrs out; const V* tw;
+    __device__ int npencil() const { return g.Kx; }
+    __device__ int nstore() const { return g.Ny; }
+    __device__ C<T> load(int fld, int z, int e, int kx) const {
+        if (!kept_full(e, g.Ny, g.My)) return zero<T>();
+        const int kyc = full_to_compact(e, g.Ny, g.Ky);
+        return ldc<T>((const V*)in.p[fld] + ((int64_t)kyc * g.Nz + z) * g.Kx + kx);
+    }
+    __device__ void store(int fld, int z, int e, int kx, const C<T>* col, int PS) const {
+        stc<T>((V*)out.p[fld] + ((int64_t)z * g.Ny + e) * g.Kx + kx, col[e * PS]);
+    }
+};
+
+// Hermitian packing of two half-spectrum rows A, B (kx < Kx) into one full
+// complex sequence Z = A + iB whose inverse DFT is a + ib.  The imaginary
+// parts at kx = 0 and kx = N/2 are dropped, as a c2r transform does.
+template <typename T, typename V>
+__device__ __forceinline__ C<T> pack_rows(const V* ra, const V* rb, int e, int N, int K) {
+    const int kx = e <= N / 2 ? e : N - e;
+    if (kx >= K) return zero<T>();
+    C<T> A = ldc<T>(ra + kx), B = ldc<T>(rb + kx);
+    if (kx == 0 || 2 * kx == N) { A.y = T(0); B.y = T(0); }
+    if (e > N / 2) { A.y = -A.y; B.y = -B.y; }
+    return mk<T>(A.x - B.y, A.y + B.x);
+}
+
+// Separation of the forward DFT Z of a + ib into the half spectra A (a), B (b)
+// at bin k, times s.
+template <typename T>
+__device__ __forceinline__ void unpack_rows(const C<T>* col, int PS, int k, int N, T s, C<T>& A, C<T>& B) {
+    const C<T> z = col[k * PS];
+    const C<T> zn = col[((N - k) & (N - 1)) * PS];
+    const T h = T(0.5) * s;
+    A = mk<T>((z.x + zn.x) * h, (z.y - zn.y) * h);
+    B = mk<T>((z.y + zn.y) * h, (zn.x - z.x) * h);
+}
+
+// c2r along x: W2 rows [r][kxc] (r = z*Ny + y) -> x rows; pencil f = row pair.
+template <typename T, typename XT>
+struct OpXc2r3 {
+    using V = typename Vec2<T>::type;
+    int nrows, Nx, Kx; CPtrs in; Ptrs out; const V* tw;
+    __device__ int npencil() const { return (nrows + 1) / 2; }
+    __device__ int nstore() const { return Nx; }
+    __device__ C<T> load(int fld, int, int e, int f) const {
+        const V* W = (const V*)in.p[fld];
+        const int ra = 2 * f, rb = min(2 * f + 1, nrows - 1);
+        C<T> z = pack_rows<T>(W + (int64_t)ra * Kx, W + (int64_t)rb * Kx, e, Nx, Kx);
+        if (rb == ra) z.y = T(0);
+        return z;
+    }
+    __device__ void store(int fld, int, int e, int f, const C<T>* col, int PS) const {
+        XT* x = (XT*)out.p[fld];
+        const C<T> v = col[e * PS];
+        x[(int64_t)(2 * f) * Nx + e] = (XT)v.x;
+        if (2 * f + 1 < nrows) x[(int64_t)(2 * f + 1) * Nx + e] = (XT)v.y;
+    }
+};
+
+// r2c along x: x rows -> W2 rows [r][kxc], scaled by s (the 1/N of the
+// reference's forward transform).
+template <typename T, typename XT>
+struct OpXr2c3 {
+    using V = typename Vec2<T>::type;
+    int nrows, Nx, Kx; T s; CPtrs in; Ptrs out; const V* tw;
+    __device__ int npencil() const { return (nrows + 1) / 2; }
+    __device__ int nstore() const { return Kx; }
+    __device__ C<T> load(int fld, int, int e, int f) const {
+        const XT* x = (const XT*)in.p[fld];
+        const T a = (T)x[(int64_t)(2 * f) * Nx + e];
+        const T b = (2 * f + 1 < nrows) ? (T)x[(int64_t)(2 * f + 1) * Nx + e] : T(0);
+        return mk<T>(a, b);
+    }
+    __device__ void store(int fld, int, int k, int f, const C<T>* col, int PS) const {
+        C<T> A, B;
+        unpack_rows<T>(col, PS, k, Nx, s, A, B);
+        V* W = (V*)out.p[fld];
+        stc<T>(W + (int64_t)(2 * f) * Kx + k, A);
+        if (2 * f + 1 < nrows) stc<T>(W + (int64_t)(2 * f + 1) * Kx + k, B);
+    }
+};
+
+// Forward along y: W2[z][y][kxc] -> W1[kyc][z][kxc] (kept ky only).
+template <typename T>
+struct OpYFwd3 {
+    using V = typename Vec2<T>::type;
+    Geo3 g; CPtrs in; Ptrs out; const V* tw;
+    __device__ int npencil() const { return g.Kx; }
+    __device__ int nstore() const { return g.Ny; }
+    __device__ C<T> load(int fld, int z, int e, int kx) const {
+        return ldc<T>((const V*)in.p[fld] + ((int64_t)z * g.Ny + e) * g.Kx + kx);
+    }
+    __device__ void store(int fld, int z, int e, int kx, const C<T>* col, int PS) const {
+        if (!kept_full(e, g.Ny, g.My)) return;
+        const int kyc = full_to_compact(e, g.Ny, g.Ky);
+        stc<T>((V*)out.p[fld] + ((int64_t)kyc * g.Nz + z) * g.Kx + kx, col[e * PS]);
+    }
+};
+
+// Forward along z: W1[kyc][z][kxc] -> K[ky][kz][kx] (kept ky, kx < Kx); the
+// non-kept kz entries of those columns are written as zeros.
+template <typename T, typename KT>
+struct OpZFwd3 {
+    using V = typename Vec2<T>::type;
+    using KV = typename Vec2<KT>::type;
+    Geo3 g; CPtrs in; Ptrs out; const V* tw;
+    __device__ int npencil() const { return g.Kx; }
+    __device__ int nstore() const { return g.Nz; }
+    __device__ C<T> load(int fld, int kyc, int e, int kx) const {
+        return ldc<T>((const V*)in.p[fld] + ((int64_t)kyc * g.Nz + e) * g.Kx + kx);
+    }
+    __device__ void store(int fld, int kyc, int e, int kx, const C<T>* col, int PS) const {
+        const int ky = compact_to_full(kyc, g.Ny, g.Ky);
+        KV v;
+        if (kept_full(e, g.Nz, g.Mz)) { const C<T> c = col[e * PS]; v.x = (KT)c.x; v.y = (KT)c.y; }
+        else { v.x = KT(0); v.y = KT(0); }
+        ((KV*)out.p[fld])[((int64_t)ky * g.Nz + e) * g.Nh + kx] = v;
+    }
+};
+
+// ============================================================ 2D operators
+// Inverse along ky: K[kx][ky] (kept) -> W[y][kxc]; pencil = kx row.
+template <typename T, typename KT>
+struct OpYInv2 {
+    using V = typename Vec2<T>::type;
+    using KV = typename Vec2<KT>::type;
+    Geo2 g; CPtrs in; Ptrs out; const V* tw;
+    __device__ int npencil() const { return g.Kx; }
+    __device__ int nstore() const { return g.Ny; }
+    __device__ C<T> load(int fld, int, int e, int kx) const {
+        if (!kept_full(e, g.Ny, g.My)) return zero<T>();
+        const KV v = ((const KV*)in.p[fld])[(int64_t)kx * g.Ny + e];
+        return mk<T>((T)v.x, (T)v.y);
+    }
+    __device__ void store(int fld, int, int e, int kx, const C<T>* col, int PS) const {
+        stc<T>((V*)out.p[fld] + (int64_t)e * g.Kx + kx, col[e * PS]);
+    }
+};
+
+// Forward along y: W[y][kxc] -> K[kx][ky] (all ky; zeros where not kept).
+template <typename T, typename KT>
+struct OpYFwd2 {
+    using V = typename Vec2<T>::type;
+    using KV = typename Vec2<KT>::type;
+    Geo2 g; CPtrs in; Ptrs out; const V* tw;
+    __device__ int npencil() const { return g.Kx; }
+    __device__ int nstore() const { return g.Ny; }
+    __device__ C<T> load(int fld, int, int e, int kx) const {
+        return ldc<T>((const V*)in.p[fld] + (int64_t)e * g.Kx + kx);
+    }
+    __device__ void store(int fld, int, int e, int kx, const C<T>* col, int PS) const {
+        KV v;
+        if (kept_full(e, g.Ny, g.My)) { const C<T> c = col[e * PS]; v.x = (KT)c.x; v.y = (KT)c.y; }
+        else { v.x = KT(0); v.y = KT(0); }
+        ((KV*)out.p[fld])[(int64_t)kx * g.Ny + e] = v;
+    }
+};
+
+}  // namespace dd

@@ -1,0 +1,41 @@
+// Host-side plan: one grid geometry with its wavenumber tables and twiddles.
+#pragma once
+#include "geometry.cuh"
+#include "fft_engine.cuh"
+
+struct dd_plan {
+    int ndim;
+    int device;
+    dd::Geo3 g3;          // valid when ndim == 3
+    dd::Geo2 g2;          // valid when ndim == 2
+    // wavenumber tables in the reference's k-layout order (device, float64):
+    //   3D: kx[Nh], ky[Ny], kz[Nz];  2D: kx[Nh], ky[Ny]
+    double* kx;
+    double* ky;
+    double* kz;
+    // twiddle tables W_L^m, m < L, per axis length (device), fp64 and fp32
+    double2* tw64_x; double2* tw64_y; double2* tw64_z;
+    float2* tw32_x;  float2* tw32_y;  float2* tw32_z;
+    // rounded-down 1/N_total used by the forward transform
+    double inv_n;
+};
+
+namespace dd {
+
+template <typename T> struct TwSel;
+template <> struct TwSel<double> {
+    static const double2* x(const dd_plan* p) { return p->tw64_x; }
+    static const double2* y(const dd_plan* p) { return p->tw64_y; }
+    static const double2* z(const dd_plan* p) { return p->tw64_z; }
+};
+template <> struct TwSel<float> {
+    static const float2* x(const dd_plan* p) { return p->tw32_x; }
+    static const float2* y(const dd_plan* p) { return p->tw32_y; }
+    static const float2* z(const dd_plan* p) { return p->tw32_z; }
+};
+
+// Dispatch a pass on a runtime length.
+template <typename T, bool INV, bool LD_E, bool ST_E, class Op>
+int launch_pass_len(int L, const Op& op, int npen, int nslow, int nfield, cudaStream_t st);
+
+}  // namespace dd

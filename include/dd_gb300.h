@@ -1,0 +1,106 @@
+/*
+ * dd_gb300.h -- C ABI of the GB300-native pseudospectral RHS / timestepping
+ * library (libdd_gb300.so).
+ *
+ * Conventions
+ *  - Every entry point returns an int status (DD_OK = 0); dd_last_error()
+ *    gives a message for the calling host thread's last failure.
+ *  - All array arguments are DEVICE pointers owned by the caller; the library
+ *    never allocates caller-visible memory.  Plans own only their small
+ *    wavenumber and twiddle tables; scratch space is passed in by the caller
+ *    (size from dd_plan_workspace_size).
+ *  - `stream` is a cudaStream_t (NULL = legacy default stream).  Calls are
+ *    asynchronous with respect to the host.
+ *  - Layouts are the reference's (dedalus/data_objects/representations.py:86-93):
+ *      3D x-space float64 [z][y][x],  k-space complex128 [ky][kz][kx], kx < Nx/2+1
+ *      2D x-space float64 [y][x],     k-space complex128 [kx][ky]
+ *    complex128 is interleaved (re, im) doubles.
+ *  - Transform sizes: powers of two, 8 <= N <= 512 per axis.
+ */
+#ifndef DD_GB300_H
+#define DD_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes (mapped to Python exceptions by the host binding) */
+#define DD_OK              0
+#define DD_ERR_INVALID     1  /* bad argument (null pointer, bad size)      -> ValueError */
+#define DD_ERR_UNSUPPORTED 2  /* shape / option not supported               -> NotImplementedError */
+#define DD_ERR_CUDA        3  /* CUDA runtime error                         -> RuntimeError */
+#define DD_ERR_TIMEOUT     4  /* a bounded device wait expired              -> TimeoutError */
+#define DD_ERR_WORKSPACE   5  /* workspace too small                        -> ValueError */
+
+#define DD_FP64 0
+#define DD_FP32 1
+
+typedef struct dd_plan dd_plan;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int dd_version(void);
+/* Message describing this host thread's most recent failure ("" if none). */
+const char* dd_last_error(void);
+
+/* ------------------------------------------------------------------ plans
+ * One plan per grid geometry, the analogue of the reference's FFTW plan pair
+ * (dedalus/utils/fftw/_fftw.pyx:246-309 rPlan, created in
+ * representations.py:312-316).  xshape is (Nz, Ny, Nx) or (Ny, Nx).  k tables
+ * are the reference's wavenumbers (representations.py:204-233) in k-layout
+ * order: kx[Nx/2+1], ky[Ny], kz[Nz] (3D) or kx[Nx/2+1], ky[Ny] (2D), on the
+ * host.  mx, my, mz give the largest kept |mode index| per axis after
+ * dealiasing (representations.py:359-408): kept modes are 0..m and N-m..N-1.
+ * Fails with DD_ERR_UNSUPPORTED for non power-of-two sizes.
+ */
+int dd_plan_create(int ndim, const int64_t* xshape, const double* kx, const double* ky,
+                   const double* kz, int mx, int my, int mz, dd_plan** out);
+int dd_plan_destroy(dd_plan* plan);
+
+/* Scratch bytes needed by dd_fft_* for `nfield` fields at `precision`. */
+int dd_plan_workspace_size(const dd_plan* plan, int nfield, int precision, size_t* bytes);
+
+/* Forward transform x -> k of nfield fields: r2c, scaled by 1/N_total, then
+ * 2/3 dealiasing (non-kept modes written as zeros).  Replaces
+ * FourierRepresentation.forward = fwd_fftw + dealias (representations.py:318-345). */
+int dd_fft_r2c(const dd_plan* plan, int nfield, const double* const* x, void* const* k,
+               int precision, void* work, size_t work_bytes, void* stream);
+
+/* Backward transform k -> x of nfield fields: c2r of the kept (dealiased)
+ * modes, unnormalised.  The k arrays are read only; the reference's in-place
+ * dealias before the transform is dd_dealias.  Replaces
+ * FourierRepresentation.backward = dealias + rev_fftw (representations.py:323-357). */
+int dd_fft_c2r(const dd_plan* plan, int nfield, const void* const* k, double* const* x,
+               int precision, void* work, size_t work_bytes, void* stream);
+
+/* In-place 2/3 dealiasing of one k array.  Replaces dealias_cy_{2d,3d}.dealias_23
+ * (dedalus/data_objects/dealias_cy_3d.pyx:13-37, dealias_cy_2d.pyx:59-78). */
+int dd_dealias(const dd_plan* plan, void* k, void* stream);
+
+/* ------------------------------------------------------------ stage kernels
+ * Same arguments and arithmetic as the reference's Cython kernels
+ * (dedalus/time_stepping/forward_step_cy_3d.pyx:17-124 and
+ * forward_step_cy_2d.pyx:21-120): contiguous complex128 arrays of n entries,
+ * intfactor float64 (the reference passes -IF), output may alias start.
+ * ndim selects the 2D or 3D Taylor branch.
+ */
+int dd_euler(const void* start, void* output, const void* deriv, double dt, int64_t n, void* stream);
+int dd_etd1(int ndim, const void* start, void* output, const void* deriv, const double* intfactor,
+            double dt, int64_t n, void* stream);
+int dd_etd2rk1(int ndim, const void* start, void* output, const void* deriv1, const void* deriv2,
+               const double* intfactor, double dt, int64_t n, void* stream);
+int dd_etd2rk2(int ndim, const void* start, void* output, const void* deriv1, const void* deriv2,
+               const double* intfactor, double dt, int64_t n, void* stream);
+
+/* phi-function table for integer squared wavenumbers q = 0..qmax:
+ * table[q] = {Z, f0(Z), f1(Z), f2(Z)} (4 doubles) with Z = -(nu q^vo) h, the
+ * reference's intfactor*dt for k2 == q (physics.py:504-522), evaluated with
+ * the stage kernels' arithmetic.  Used by the fused timesteppers. */
+int dd_phi_table(int ndim, double nu, int viscosity_order, double h, int qmax, void* table, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DD_GB300_H */
