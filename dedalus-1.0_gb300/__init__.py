@@ -9,6 +9,19 @@ ABI in ``include/dd_gb300.h``; PyTorch provides device buffers and streams.
 """
 from . import _lib
 from . import kgrid
-from . import engine
+from . import config
+from . import init_cond
 
-__all__ = ["_lib", "kgrid", "engine"]
+try:  # the device layers need torch; host helpers (kgrid, init_cond) do not
+    from . import engine
+    from . import representations
+    from . import fields
+    from . import physics
+    from . import time_step
+    from . import mods
+except ImportError as e:  # pragma: no cover
+    if "torch" not in str(e):
+        raise
+
+__all__ = ["_lib", "kgrid", "config", "init_cond", "engine", "representations", "fields", "physics",
+           "time_step", "mods"]

@@ -39,11 +39,17 @@ SIGNATURES = {
     "dd_fft_r2c": [P, I, PP, PP, I, P, SZ, P],
     "dd_fft_c2r": [P, I, PP, PP, I, P, SZ, P],
     "dd_dealias": [P, P, P],
+    "dd_deriv": [P, I, P, P, P],
+    "dd_scale_add": [P, P, D, I, I64, P],
     "dd_euler": [P, P, P, D, I64, P],
     "dd_etd1": [I, P, P, P, P, D, I64, P],
     "dd_etd2rk1": [I, P, P, P, P, P, D, I64, P],
     "dd_etd2rk2": [I, P, P, P, P, P, D, I64, P],
     "dd_phi_table": [I, D, I, D, I, P, P],
+    "dd_hydro3d_workspace_size": [P, I, ctypes.POINTER(SZ)],
+    "dd_hydro3d_rhs": [P, PP, PP, P, I, I, P, SZ, P],
+    "dd_hydro3d_rk4_step": [P, PP, P, P, P, D, I, D, I, ctypes.POINTER(I), P, SZ, P],
+    "dd_any_nonkept": [P, I, PP, P, P],
 }
 _RESTYPE = {"dd_last_error": ctypes.c_char_p}
 

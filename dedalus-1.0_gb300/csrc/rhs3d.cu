@@ -348,6 +348,18 @@ __global__ void k_any_nonkept3(Geo3 g, CPtrs y, int ncomp, int* flag) {
     if (__syncthreads_or(found) && threadIdx.x == 0) atomicOr(flag, 1);
 }
 
+// Zero every non-kept entry of ncomp full-layout arrays (grid.y = component).
+__global__ void k_dealias3_all(Geo3 g, Ptrs k) {
+    double2* K = (double2*)k.p[blockIdx.y];
+    const int64_t n = g.kcount();
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int ix = (int)(i % g.Nh);
+        const int64_t r = i / g.Nh;
+        const int kz_i = (int)(r % g.Nz), ky_i = (int)(r / g.Nz);
+        if (ix > g.Mx || !kept_full(ky_i, g.Ny, g.My) || !kept_full(kz_i, g.Nz, g.Mz)) K[i] = make_double2(0., 0.);
+    }
+}
+
 static unsigned ew_grid(int64_t n) {
     int64_t b = (n + 255) / 256;
     if (b > 152 * 16) b = 152 * 16;

@@ -1,0 +1,280 @@
+"""GPU physics classes: drop-ins for the reference's ``IncompressibleHydro``,
+``BoussinesqHydro`` and ``IncompressibleMHD`` (dedalus/physics/physics.py).
+
+Same constructor ``Cls(shape, representation, length=None)``, the same
+``parameters`` dictionary and defaults, ``create_fields(t)``,
+``RHS(data, deriv)`` (fills ``deriv[f][c]['kspace']`` and sets each
+component's ``integrating_factor`` on the first call, physics.py:504-522),
+``compute_dt`` and the forcing setters.  The right-hand sides are computed by
+fused CUDA kernels (one C-ABI call per RHS).  The branches the fused kernels
+do not implement (shear, rotation, tracer, forcing functions) raise
+NotImplementedError instead of running anywhere else.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from .config import decfg, precision_code
+from .engine import current_stream, dptr
+from .fields import create_field_classes, StateData
+
+
+def _ptrs(tensors):
+    return _lib.ptr_array([t.data_ptr() for t in tensors])
+
+
+class Physics:
+    """physics.py:42-158 (base): fields, parameters, aux equations, dt."""
+
+    def __init__(self, shape, representation, length=None):
+        self.shape = shape
+        self._representation = representation
+        self.length = length if length else (2 * np.pi,) * len(self.shape)
+        self.ndim = len(self.shape)
+        self.dims = range(self.ndim)
+        self._field_list = []
+        self._aux_field_list = []
+        self.parameters = {}
+        self.aux_eqns = {}
+        self.forcing_functions = {}
+        self._forcing_function_names = {}
+        self._field_classes = create_field_classes(self._representation, self.shape, self.length)
+        self._is_finalized = False
+        self._tracer = decfg.getboolean('physics', 'use_tracer')
+        self.k2 = None
+        self._ws = None
+        self._tables = {}
+
+    def __getitem__(self, item):
+        value = self.parameters.get(item, None)
+        if value is None:
+            raise KeyError
+        return value
+
+    def create_fields(self, time, field_list=None):
+        if field_list is None:
+            field_list = self._field_list
+        return StateData(time, self.shape, self.length, self._field_classes, field_list=field_list,
+                         params=self.parameters)
+
+    def _finalize(self):
+        self._is_finalized = True
+
+    def compute_dt(self, data):
+        self.dtlist = []
+        self.set_dtlist(data)
+        return min(self.dtlist)
+
+    # --------------------------------------------------------- device data
+    def plan(self, data):
+        return next(iter(data.fields.values()))[0].plan
+
+    def workspace(self, nbytes):
+        if self._ws is None or self._ws.numel() < nbytes:
+            self._ws = None
+            self._ws = torch.empty(int(nbytes), dtype=torch.uint8, device=torch.device('cuda', torch.cuda.current_device()))
+        return self._ws
+
+    def inv_k2_table(self, plan):
+        """1/q for integer squared wavenumbers q (q = 0 -> 1), or None."""
+        if not plan.integer_k:
+            return None
+        key = ('inv_k2', id(plan))
+        t = self._tables.get(key)
+        if t is None:
+            qmax = int(sum((n // 2) ** 2 for n in plan.xshape))
+            q = np.arange(qmax + 1, dtype=np.float64)
+            q[0] = 1.
+            t = torch.from_numpy(1.0 / q).to(plan.device)
+            self._tables[key] = t
+        return t
+
+    def phi_table(self, plan, nu, vo, h):
+        """dd_phi_table for (nu, vo, h) on this grid (3D or 2D variant)."""
+        key = ('phi', id(plan), float(nu), int(vo), float(h))
+        t = self._tables.get(key)
+        if t is None:
+            qmax = int(sum((n // 2) ** 2 for n in plan.xshape))
+            t = torch.empty((qmax + 1, 4), dtype=torch.float64, device=plan.device)
+            _lib.call("dd_phi_table", plan.ndim, float(nu), int(vo), float(h), qmax, dptr(t), current_stream())
+            if len(self._tables) > 64:
+                self._tables = {k: v for k, v in self._tables.items() if k[0] == 'inv_k2'}
+            self._tables[key] = t
+        return t
+
+
+class IncompressibleHydro(Physics):
+    """physics.py:419-610."""
+
+    def __init__(self, *args, **kwargs):
+        Physics.__init__(self, *args, **kwargs)
+        self._field_list.append(('u', 'VectorField'))
+        self._aux_field_list.append(('mathscalar', 'ScalarField'))
+        self._aux_field_list.append(('mathvector', 'VectorField'))
+        self.parameters['viscosity_order'] = 1
+        self.parameters['nu'] = 0.
+        self.parameters['shear_rate'] = 0.
+        self.parameters['Omega'] = None
+        if self._tracer:
+            self._field_list.append(('c', 'ScalarField'))
+            self.parameters['c_diff'] = 0.
+        self._trans = {0: 'x', 1: 'y', 2: 'z'}
+        self._first_rhs = True
+
+    def _finalize(self):
+        Physics._finalize(self)
+        if self.parameters['shear_rate'] != 0.:
+            raise NotImplementedError("shear (FourierShearRepresentation) is not in the CUDA path")
+        if self.parameters['Omega'] is not None:
+            raise NotImplementedError("rotation is not in the CUDA path")
+        if self._tracer:
+            raise NotImplementedError("the passive tracer is not in the CUDA path")
+        if self.forcing_functions:
+            raise NotImplementedError("forcing functions are not in the CUDA path")
+        self._shear = False
+        self._rotation = False
+
+    def _diffusivities(self):
+        """(field name, coefficient) pairs whose IF is coeff * k2**vo."""
+        return [('u', self.parameters['nu'])]
+
+    def _setup_integrating_factors(self, deriv):
+        # physics.py:504-522 (and the Boussinesq/MHD extensions)
+        vo = self.parameters['viscosity_order']
+        for fname, coeff in self._diffusivities():
+            for cindex, comp in deriv[fname]:
+                comp.integrating_factor = None if coeff == 0. else coeff * comp.k2() ** vo
+                comp._if_coeff = float(coeff)
+
+    def set_velocity_forcing(self, func):
+        self.forcing_functions['VelocityForcing'] = func
+
+    def _begin_rhs(self, data, deriv):
+        if not self._is_finalized:
+            self._finalize()
+        # The reference sets the factors on the first deriv it is given only
+        # (physics.py:538-540); a deriv that never received them gets them here
+        # instead of failing later in the integrator.
+        if self._first_rhs or not hasattr(next(iter(deriv.fields.values()))[0], 'integrating_factor'):
+            self._setup_integrating_factors(deriv)
+            self._first_rhs = False
+        for fname, field in data:
+            for i, c in field:
+                c.require_space('kspace')
+        deriv.set_time(data.time)
+
+    def _mark_kspace(self, deriv):
+        for fname, field in deriv:
+            for i, c in field:
+                c.data = c.kdata
+                c._curr_space = 'kspace'
+
+    def RHS(self, data, deriv):
+        """RHS(u) = P[-(u.grad)u] (physics.py:527-599), fused on the GPU."""
+        self._begin_rhs(data, deriv)
+        plan = self.plan(data)
+        if self.ndim != 3:
+            return self._rhs2d(data, deriv, plan)
+        prec = precision_code()
+        n = ctypes.c_size_t()
+        _lib.call("dd_hydro3d_workspace_size", plan.handle, prec, ctypes.byref(n))
+        ws = self.workspace(n.value)
+        up, _a = _ptrs([c.kdata for i, c in data['u']])
+        dp, _b = _ptrs([c.kdata for i, c in deriv['u']])
+        ik2 = self.inv_k2_table(plan)
+        _lib.call("dd_hydro3d_rhs", plan.handle, up, dp, None if ik2 is None else dptr(ik2), prec, 1,
+                  dptr(ws), ws.numel(), current_stream())
+        self._mark_kspace(deriv)
+
+    def _rhs2d(self, data, deriv, plan):
+        raise NotImplementedError("2D hydro RHS is not available yet")
+
+    def fused_rk4(self, data, dt):
+        """One fused RK4 step on the device (dd_hydro3d_rk4_step); returns
+        False when this physics/grid has no fused step."""
+        if self.ndim != 3 or type(self) is not IncompressibleHydro:
+            return False
+        if not self._is_finalized:
+            self._finalize()
+        for i, c in data['u']:
+            c.require_space('kspace')
+        plan = self.plan(data)
+        prec = precision_code()
+        nu, vo = float(self.parameters['nu']), int(self.parameters['viscosity_order'])
+        n = ctypes.c_size_t()
+        _lib.call("dd_hydro3d_workspace_size", plan.handle, prec, ctypes.byref(n))
+        ws = self.workspace(n.value)
+        ik2 = self.inv_k2_table(plan)
+        th = tf = None
+        if ik2 is not None:
+            th = self.phi_table(plan, nu, vo, dt / 2.)
+            tf = self.phi_table(plan, nu, vo, dt)
+        up, _a = _ptrs([c.kdata for i, c in data['u']])
+        flag = ctypes.c_int(1)
+        _lib.call("dd_hydro3d_rk4_step", plan.handle, up, None if ik2 is None else dptr(ik2),
+                  None if th is None else dptr(th), None if tf is None else dptr(tf), nu, vo, float(dt), prec,
+                  ctypes.byref(flag), dptr(ws), ws.numel(), current_stream())
+        return True
+
+    def max_abs_vel(self, data):
+        return np.sqrt(data['u'].max_square())
+
+    def set_dtlist(self, data):
+        dx = data['u']['x'].dx().min()
+        self.dtlist.append(dx / self.max_abs_vel(data))
+
+
+class BoussinesqHydro(IncompressibleHydro):
+    """physics.py:612-721."""
+
+    def __init__(self, *args, **kwargs):
+        IncompressibleHydro.__init__(self, *args, **kwargs)
+        self._field_list.append(('T', 'ScalarField'))
+        self.parameters['kappa'] = 0.
+        self.parameters['g'] = 1.
+        self.parameters['alpha_t'] = 1.
+        self.parameters['beta'] = 1.
+        self.parameters['boussinesq_direction'] = decfg.get('physics', 'boussinesq_direction')
+
+    def _diffusivities(self):
+        return [('u', self.parameters['nu']), ('T', self.parameters['kappa'])]
+
+    def set_thermal_forcing(self, func):
+        self.forcing_functions['ThermalForcing'] = func
+
+    def RHS(self, data, deriv):
+        raise NotImplementedError("Boussinesq RHS is not available yet")
+
+    def set_dtlist(self, data):
+        IncompressibleHydro.set_dtlist(self, data)
+        dx = data['u']['x'].dx().min()
+        N = np.sqrt(np.abs(self.parameters['alpha_t'] * self.parameters['g'] * self.parameters['beta']))
+        self.dtlist.append(dx / N)
+
+
+class IncompressibleMHD(IncompressibleHydro):
+    """physics.py:724-836."""
+
+    def __init__(self, *args, **kwargs):
+        IncompressibleHydro.__init__(self, *args, **kwargs)
+        self._field_list.append(('B', 'VectorField'))
+        self._aux_field_list.append(('mathvector2', 'VectorField'))
+        self.parameters['rho0'] = 1.
+        self.parameters['eta'] = 0.
+
+    def _diffusivities(self):
+        return [('u', self.parameters['nu']), ('B', self.parameters['eta'])]
+
+    def RHS(self, data, deriv):
+        raise NotImplementedError("MHD RHS is not available yet")
+
+    def max_alfven_speed(self, data):
+        fpr = 4 * np.pi * self.parameters['rho0']
+        return np.sqrt(data['B'].max_square() / fpr)
+
+    def set_dtlist(self, data):
+        IncompressibleHydro.set_dtlist(self, data)
+        dx = data['u']['x'].dx().min()
+        self.dtlist.append(dx / self.max_alfven_speed(data))

@@ -79,6 +79,15 @@ int dd_fft_c2r(const dd_plan* plan, int nfield, const void* const* k, double* co
  * (dedalus/data_objects/dealias_cy_3d.pyx:13-37, dealias_cy_2d.pyx:59-78). */
 int dd_dealias(const dd_plan* plan, void* k, void* stream);
 
+/* Spectral derivative out = in * (1j * k_axis) of one k array (axis 0 = x,
+ * 1 = y, 2 = z).  Replaces FourierRepresentation.deriv
+ * (dedalus/data_objects/representations.py:419-425). */
+int dd_deriv(const dd_plan* plan, int axis, const void* k_in, void* k_out, void* stream);
+
+/* y = x * w (accumulate == 0) or y += x * w for n complex128 entries: the RK4
+ * increment accumulation (dedalus/time_stepping/time_step.py:435, 452, 463, 474). */
+int dd_scale_add(const void* x, void* y, double w, int accumulate, int64_t n, void* stream);
+
 /* ------------------------------------------------------------ stage kernels
  * Same arguments and arithmetic as the reference's Cython kernels
  * (dedalus/time_stepping/forward_step_cy_3d.pyx:17-124 and
@@ -99,6 +108,38 @@ int dd_etd2rk2(int ndim, const void* start, void* output, const void* deriv1, co
  * reference's intfactor*dt for k2 == q (physics.py:504-522), evaluated with
  * the stage kernels' arithmetic.  Used by the fused timesteppers. */
 int dd_phi_table(int ndim, double nu, int viscosity_order, double h, int qmax, void* table, void* stream);
+
+/* ------------------------------------------------------ fused 3D hydro
+ * IncompressibleHydro.RHS (dedalus/physics/physics.py:527-599) for shear = 0,
+ * Omega = None, no tracer and no forcing, computed as P[u x w] (rotational
+ * form; equal on the kept modes to roundoff).  u and deriv are 3 component
+ * k arrays (x, y, z order, full reference layout).  inv_k2 is an optional
+ * device table 1/q for integer squared wavenumbers q (q = 0 -> 1); pass it
+ * when every wavenumber is an integer (length-2 pi axes), else NULL.
+ * zero_nonkept != 0 also writes zeros to the non-kept entries of deriv (the
+ * reference zeroes deriv first, physics.py:140-142).  precision selects FP64
+ * or FP32 transform/product arithmetic; the projection is FP64. */
+int dd_hydro3d_workspace_size(const dd_plan* plan, int precision, size_t* bytes);
+int dd_hydro3d_rhs(const dd_plan* plan, const void* const* u, void* const* deriv, const double* inv_k2,
+                   int precision, int zero_nonkept, void* work, size_t work_bytes, void* stream);
+
+/* One RK4 step of 3D hydro, in place on u.  Replaces RK4.do_advance
+ * (dedalus/time_stepping/time_step.py:426-483), whose forward_step calls
+ * undefined linear_step/intfac_step (time_step.py:209-218); the stage
+ * definition is k1=N(y); y2=etd1(y,k1,dt/2); k2=N(y2); y3=etd1(y,k2,dt/2);
+ * k3=N(y3); y4=etd1(y,k3,dt); k4=N(y4); y=etd1(y,k1/6+k2/3+k3/3+k4/6,dt).
+ * tab_half / tab_full are dd_phi_table tables for h = dt/2 and h = dt (3D
+ * variant) when inv_k2 is given; otherwise the phi functions are evaluated
+ * per entry from nu and viscosity_order.  *nonkept_flag (host int) != 0 means
+ * the state has energy outside the kept modes (see dd_any_nonkept); those
+ * modes then decay as etd1(y, 0, dt), as in the reference. */
+int dd_hydro3d_rk4_step(const dd_plan* plan, void* const* u, const double* inv_k2, const void* tab_half,
+                        const void* tab_full, double nu, int viscosity_order, double dt, int precision,
+                        int* nonkept_flag, void* work, size_t work_bytes, void* stream);
+
+/* Sets *dflag (device int) to 1 if any of the ncomp k arrays has a non-zero
+ * entry outside the kept (dealiased) modes; does not clear it. */
+int dd_any_nonkept(const dd_plan* plan, int ncomp, const void* const* k, int* dflag, void* stream);
 
 #ifdef __cplusplus
 }
