@@ -33,6 +33,10 @@ SZ = ctypes.c_size_t
 SIGNATURES = {
     "dd_version": [],
     "dd_last_error": [],
+    "dd_launch_count": [],
+    "dd_timing_enable": [I],
+    "dd_timing_reset": [],
+    "dd_timing_report": [ctypes.c_char_p, SZ],
     "dd_plan_create": [I, ctypes.POINTER(I64), P, P, P, I, I, I, ctypes.POINTER(P)],
     "dd_plan_destroy": [P],
     "dd_plan_workspace_size": [P, I, I, ctypes.POINTER(SZ)],
@@ -51,7 +55,30 @@ SIGNATURES = {
     "dd_hydro3d_rk4_step": [P, PP, P, P, P, D, I, D, I, ctypes.POINTER(I), P, SZ, P],
     "dd_any_nonkept": [P, I, PP, P, P],
 }
-_RESTYPE = {"dd_last_error": ctypes.c_char_p}
+_RESTYPE = {"dd_last_error": ctypes.c_char_p, "dd_launch_count": ctypes.c_longlong}
+
+
+def launch_count():
+    return int(lib().dd_launch_count())
+
+
+def timing_enable(on=True):
+    check(lib().dd_timing_enable(1 if on else 0))
+
+
+def timing_reset():
+    check(lib().dd_timing_reset())
+
+
+def timing_report():
+    """{label: (launches, total device ms)} since the last reset."""
+    buf = ctypes.create_string_buffer(1 << 20)
+    check(lib().dd_timing_report(buf, len(buf)))
+    out = {}
+    for line in buf.value.decode().splitlines():
+        name, n, ms = line.split()
+        out[name] = (int(n), float(ms))
+    return out
 
 _lib = None
 

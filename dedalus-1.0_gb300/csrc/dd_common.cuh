@@ -7,6 +7,8 @@
 #include <stdarg.h>
 
 #include "dd_gb300.h"
+#include "timing.cuh"
+#include <string>
 
 namespace dd {
 

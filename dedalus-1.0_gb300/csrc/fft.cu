@@ -186,7 +186,7 @@ int fft_r2c(const dd_plan* pl, int nf, const double* const* x, void* const* k, v
         DD_TRY((launch_pass_len<T, false, false, false>(g.Ny, b, g.Kx, g.Nz, nf, st)));
         OpZFwd3<T, double> c{g, w1c, ko, TwSel<T>::z(pl)};
         DD_TRY((launch_pass_len<T, false, false, false>(g.Nz, c, g.Kx, g.Ky, nf, st)));
-        k_zero_nonkept3<double><<<dim3(ew_grid(g.kcount()), nf), 256, 0, st>>>(g, ko);
+        DD_KT("zero_nonkept3", st, k_zero_nonkept3<double><<<dim3(ew_grid(g.kcount()), nf), 256, 0, st>>>(g, ko));
         DD_LAUNCH_CHECK();
     } else {
         const Geo2& g = pl->g2;
@@ -199,7 +199,7 @@ int fft_r2c(const dd_plan* pl, int nf, const double* const* x, void* const* k, v
         DD_TRY((launch_pass_len<T, false, false, true>(g.Ny, b, g.Kx, 1, nf, st)));
         const int64_t nz = g.kcount() - (int64_t)g.Kx * g.Ny;
         if (nz > 0) {
-            k_zero_nonkept2<double><<<dim3(ew_grid(nz), nf), 256, 0, st>>>(g, ko);
+            DD_KT("zero_nonkept2", st, k_zero_nonkept2<double><<<dim3(ew_grid(nz), nf), 256, 0, st>>>(g, ko));
             DD_LAUNCH_CHECK();
         }
     }
@@ -302,8 +302,8 @@ int dd_fft_c2r(const dd_plan* p, int nfield, const void* const* k, double* const
 int dd_dealias(const dd_plan* p, void* k, void* stream) {
     DD_CHECK_ARG(p && k, "dd_dealias: null pointer");
     cudaStream_t st = (cudaStream_t)stream;
-    if (p->ndim == 3) k_dealias3<<<ew_grid(p->g3.kcount()), 256, 0, st>>>(p->g3, (double2*)k);
-    else k_dealias2<<<ew_grid(p->g2.kcount()), 256, 0, st>>>(p->g2, (double2*)k);
+    if (p->ndim == 3) DD_KT("dealias3", st, k_dealias3<<<ew_grid(p->g3.kcount()), 256, 0, st>>>(p->g3, (double2*)k));
+    else DD_KT("dealias2", st, k_dealias2<<<ew_grid(p->g2.kcount()), 256, 0, st>>>(p->g2, (double2*)k));
     DD_LAUNCH_CHECK();
     return DD_OK;
 }

@@ -62,7 +62,8 @@ int launch_pass(const Op& op, int npencil, int nslow, int nfield, cudaStream_t s
         return DD_ERR_UNSUPPORTED;
     }
     dim3 grid(cdiv(npencil, P) * nfield, nslow > 65535 ? 65535 : nslow, nslow > 65535 ? nslow / 65535 : 1);
-    kern<<<grid, NT, smem, st>>>(op, nfield);
+    static const std::string label = std::string(Op::name) + "_" + std::to_string(L) + (sizeof(T) == 8 ? "_f64" : "_f32");
+    DD_KT(label.c_str(), st, kern<<<grid, NT, smem, st>>>(op, nfield));
     DD_LAUNCH_CHECK();
     return DD_OK;
 }
@@ -72,6 +73,7 @@ int launch_pass(const Op& op, int npencil, int nslow, int nfield, cudaStream_t s
 template <typename T, typename KT>
 struct OpZInv3 {
     using V = typename Vec2<T>::type;
+    static constexpr const char* name = "z_inv";
     using KV = typename Vec2<KT>::type;
     Geo3 g; CPtrs in; Ptrs out; const V* tw;
     __device__ int npencil() const { return g.Kx; }
@@ -91,6 +93,7 @@ struct OpZInv3 {
 template <typename T>
 struct OpYInv3 {
     using V = typename Vec2<T>::type;
+    static constexpr const char* name = "y_inv";
     Geo3 g; CPtrs in; Ptrs out; const V* tw;
     __device__ int npencil() const { return g.Kx; }
     __device__ int nstore() const { return g.Ny; }
@@ -132,6 +135,7 @@ __device__ __forceinline__ void unpack_rows(const C<T>* col, int PS, int k, int 
 template <typename T, typename XT>
 struct OpXc2r3 {
     using V = typename Vec2<T>::type;
+    static constexpr const char* name = "x_c2r";
     int nrows, Nx, Kx; CPtrs in; Ptrs out; const V* tw;
     __device__ int npencil() const { return (nrows + 1) / 2; }
     __device__ int nstore() const { return Nx; }
@@ -155,6 +159,7 @@ struct OpXc2r3 {
 template <typename T, typename XT>
 struct OpXr2c3 {
     using V = typename Vec2<T>::type;
+    static constexpr const char* name = "x_r2c";
     int nrows, Nx, Kx; T s; CPtrs in; Ptrs out; const V* tw;
     __device__ int npencil() const { return (nrows + 1) / 2; }
     __device__ int nstore() const { return Kx; }
@@ -177,6 +182,7 @@ struct OpXr2c3 {
 template <typename T>
 struct OpYFwd3 {
     using V = typename Vec2<T>::type;
+    static constexpr const char* name = "y_fwd";
     Geo3 g; CPtrs in; Ptrs out; const V* tw;
     __device__ int npencil() const { return g.Kx; }
     __device__ int nstore() const { return g.Ny; }
@@ -195,6 +201,7 @@ struct OpYFwd3 {
 template <typename T, typename KT>
 struct OpZFwd3 {
     using V = typename Vec2<T>::type;
+    static constexpr const char* name = "z_fwd";
     using KV = typename Vec2<KT>::type;
     Geo3 g; CPtrs in; Ptrs out; const V* tw;
     __device__ int npencil() const { return g.Kx; }
@@ -216,6 +223,7 @@ struct OpZFwd3 {
 template <typename T, typename KT>
 struct OpYInv2 {
     using V = typename Vec2<T>::type;
+    static constexpr const char* name = "y_inv2d";
     using KV = typename Vec2<KT>::type;
     Geo2 g; CPtrs in; Ptrs out; const V* tw;
     __device__ int npencil() const { return g.Kx; }
@@ -234,6 +242,7 @@ struct OpYInv2 {
 template <typename T, typename KT>
 struct OpYFwd2 {
     using V = typename Vec2<T>::type;
+    static constexpr const char* name = "y_fwd2d";
     using KV = typename Vec2<KT>::type;
     Geo2 g; CPtrs in; Ptrs out; const V* tw;
     __device__ int npencil() const { return g.Kx; }

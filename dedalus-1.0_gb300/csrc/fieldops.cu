@@ -58,8 +58,9 @@ int dd_deriv(const dd_plan* p, int axis, const void* k_in, void* k_out, void* st
     if (p->ndim == 3) { n0 = p->g3.Ny; n1 = p->g3.Nz; n2 = p->g3.Nh; }
     else { n0 = p->g2.Nh; n1 = p->g2.Ny; n2 = 1; }
     const int64_t n = (int64_t)n0 * n1 * n2;
-    k_deriv<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(p->ndim, n0, n1, n2, axis, p->kx, p->ky, p->kz,
-                                                           (const double2*)k_in, (double2*)k_out);
+    DD_KT("deriv", (cudaStream_t)stream,
+          k_deriv<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(p->ndim, n0, n1, n2, axis, p->kx, p->ky, p->kz,
+                                                                 (const double2*)k_in, (double2*)k_out));
     DD_LAUNCH_CHECK();
     return DD_OK;
 }
@@ -67,7 +68,8 @@ int dd_deriv(const dd_plan* p, int axis, const void* k_in, void* k_out, void* st
 int dd_scale_add(const void* x, void* y, double w, int accumulate, int64_t n, void* stream) {
     DD_CHECK_ARG(x && y && n >= 0, "dd_scale_add: bad arguments");
     if (n == 0) return DD_OK;
-    k_scale_add<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>((const double2*)x, (double2*)y, w, accumulate, n);
+    DD_KT("scale_add", (cudaStream_t)stream,
+          k_scale_add<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>((const double2*)x, (double2*)y, w, accumulate, n));
     DD_LAUNCH_CHECK();
     return DD_OK;
 }

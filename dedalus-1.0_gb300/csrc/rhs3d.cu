@@ -31,6 +31,7 @@ __device__ __forceinline__ double2 ideriv(double2 a, double k) {
 template <typename T, bool COMPACT>
 struct OpZInvCurl3 {
     using V = typename Vec2<T>::type;
+    static constexpr const char* name = "z_inv_curl";
     Geo3 g; CPtrs u; Ptrs out; const V* tw;
     const double* kx; const double* ky; const double* kz;
     __device__ int npencil() const { return g.Kx; }
@@ -144,7 +145,9 @@ static int launch_cross3(int nrows, int Kx, const CPtrs& win, const Ptrs& wout, 
         DD_CUDA(cudaFuncSetAttribute(k_x_cross3<T, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         configured = true;
     }
-    k_x_cross3<T, L><<<cdiv(nrows, CrossCfg<L>::Q), Pencil<L>::NT, smem, st>>>(nrows, Kx, win, wout, tw, scale);
+    static const std::string label = std::string("x_cross_") + std::to_string(L) + (sizeof(T) == 8 ? "_f64" : "_f32");
+    DD_KT(label.c_str(), st,
+          k_x_cross3<T, L><<<cdiv(nrows, CrossCfg<L>::Q), Pencil<L>::NT, smem, st>>>(nrows, Kx, win, wout, tw, scale));
     DD_LAUNCH_CHECK();
     return DD_OK;
 }
@@ -169,6 +172,7 @@ static int launch_cross3_len(int L, int nrows, int Kx, const CPtrs& win, const P
 template <typename T>
 struct OpZFwdCompact3 {
     using V = typename Vec2<T>::type;
+    static constexpr const char* name = "z_fwd_compact";
     Geo3 g; CPtrs in; Ptrs out; const V* tw;
     __device__ int npencil() const { return g.Kx; }
     __device__ int nstore() const { return g.Nz; }
@@ -445,10 +449,10 @@ int dd_hydro3d_rhs(const dd_plan* p, const void* const* u, void* const* deriv, c
         d.p[c] = deriv[c];
     }
     if (zero_nonkept) {
-        k_dealias3_all<<<dim3(ew_grid(g.kcount()), 3), 256, 0, st>>>(g, d);
+        DD_KT("zero_nonkept3", st, k_dealias3_all<<<dim3(ew_grid(g.kcount()), 3), 256, 0, st>>>(g, d));
         DD_LAUNCH_CHECK();
     }
-    k_project_to_deriv3<<<ew_grid((int64_t)g.Ky * g.Kz * g.Kx), 256, 0, st>>>(pa, nc, d);
+    DD_KT("project3", st, k_project_to_deriv3<<<ew_grid((int64_t)g.Ky * g.Kz * g.Kx), 256, 0, st>>>(pa, nc, d));
     DD_LAUNCH_CHECK();
     return DD_OK;
 }
@@ -493,12 +497,13 @@ int dd_hydro3d_rk4_step(const dd_plan* p, void* const* u, const double* inv_k2, 
             else DD_TRY((hydro3_nonlinear<float, true>(p, ysc, w, st)));
         }
         a.stage = s; a.h = hs[s - 1]; a.w = ws[s - 1]; a.tab = (const double4*)tabs[s - 1];
-        k_rk4_stage3<<<ew_grid((int64_t)kc), 256, 0, st>>>(a);
+        DD_KT("rk4_stage3", st, k_rk4_stage3<<<ew_grid((int64_t)kc), 256, 0, st>>>(a));
         DD_LAUNCH_CHECK();
     }
     if (nonkept_flag && *nonkept_flag) {
-        k_decay_nonkept3<<<dim3(ew_grid(g.kcount()), 3), 256, 0, st>>>(g, a.y, p->kx, p->ky, p->kz,
-                                                                     (const double4*)tab_full, nu, viscosity_order, dt);
+        DD_KT("decay_nonkept3", st,
+              k_decay_nonkept3<<<dim3(ew_grid(g.kcount()), 3), 256, 0, st>>>(g, a.y, p->kx, p->ky, p->kz,
+                                                                           (const double4*)tab_full, nu, viscosity_order, dt));
         DD_LAUNCH_CHECK();
     }
     return DD_OK;
@@ -509,7 +514,8 @@ int dd_any_nonkept(const dd_plan* p, int ncomp, const void* const* k, int* dflag
     DD_CHECK_ARG(p->ndim == 3, "dd_any_nonkept: 3D plans only");
     CPtrs y{};
     for (int c = 0; c < ncomp; c++) y.p[c] = k[c];
-    k_any_nonkept3<<<ew_grid(p->g3.kcount()), 256, 0, (cudaStream_t)stream>>>(p->g3, y, ncomp, dflag);
+    DD_KT("any_nonkept3", (cudaStream_t)stream,
+          k_any_nonkept3<<<ew_grid(p->g3.kcount()), 256, 0, (cudaStream_t)stream>>>(p->g3, y, ncomp, dflag));
     DD_LAUNCH_CHECK();
     return DD_OK;
 }

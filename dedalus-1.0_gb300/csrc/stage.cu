@@ -84,8 +84,9 @@ int dd_euler(const void* start, void* output, const void* deriv, double dt, int6
     DD_CHECK_ARG(start && output && deriv, "dd_euler: null pointer");
     DD_CHECK_ARG(n >= 0, "dd_euler: negative size");
     if (n == 0) return DD_OK;
-    k_euler<<<ew_blocks(n), 256, 0, (cudaStream_t)stream>>>((const double2*)start, (double2*)output,
-                                                            (const double2*)deriv, dt, n);
+    cudaStream_t st = (cudaStream_t)stream;
+    DD_KT("euler", st, k_euler<<<ew_blocks(n), 256, 0, st>>>((const double2*)start, (double2*)output,
+                                                             (const double2*)deriv, dt, n));
     DD_LAUNCH_CHECK();
     return DD_OK;
 }
@@ -98,9 +99,9 @@ int dd_etd1(int ndim, const void* start, void* output, const void* deriv, const 
     if (n == 0) return DD_OK;
     cudaStream_t st = (cudaStream_t)stream;
     if (ndim == 2)
-        k_etd1<2><<<ew_blocks(n), 256, 0, st>>>((const double2*)start, (double2*)output, (const double2*)deriv, intfactor, dt, n);
+        DD_KT("etd12", st, k_etd1<2><<<ew_blocks(n), 256, 0, st>>>((const double2*)start, (double2*)output, (const double2*)deriv, intfactor, dt, n));
     else
-        k_etd1<3><<<ew_blocks(n), 256, 0, st>>>((const double2*)start, (double2*)output, (const double2*)deriv, intfactor, dt, n);
+        DD_KT("etd13", st, k_etd1<3><<<ew_blocks(n), 256, 0, st>>>((const double2*)start, (double2*)output, (const double2*)deriv, intfactor, dt, n));
     DD_LAUNCH_CHECK();
     return DD_OK;
 }
@@ -113,11 +114,11 @@ int dd_etd2rk1(int ndim, const void* start, void* output, const void* deriv1, co
     if (n == 0) return DD_OK;
     cudaStream_t st = (cudaStream_t)stream;
     if (ndim == 2)
-        k_etd2rk1<2><<<ew_blocks(n), 256, 0, st>>>((const double2*)start, (double2*)output, (const double2*)deriv1,
-                                                   (const double2*)deriv2, intfactor, dt, n);
+        DD_KT("etd2rk12", st, k_etd2rk1<2><<<ew_blocks(n), 256, 0, st>>>((const double2*)start, (double2*)output, (const double2*)deriv1,
+                                                   (const double2*)deriv2, intfactor, dt, n));
     else
-        k_etd2rk1<3><<<ew_blocks(n), 256, 0, st>>>((const double2*)start, (double2*)output, (const double2*)deriv1,
-                                                   (const double2*)deriv2, intfactor, dt, n);
+        DD_KT("etd2rk13", st, k_etd2rk1<3><<<ew_blocks(n), 256, 0, st>>>((const double2*)start, (double2*)output, (const double2*)deriv1,
+                                                   (const double2*)deriv2, intfactor, dt, n));
     DD_LAUNCH_CHECK();
     return DD_OK;
 }
@@ -130,11 +131,11 @@ int dd_etd2rk2(int ndim, const void* start, void* output, const void* deriv1, co
     if (n == 0) return DD_OK;
     cudaStream_t st = (cudaStream_t)stream;
     if (ndim == 2)
-        k_etd2rk2<2><<<ew_blocks(n), 256, 0, st>>>((const double2*)start, (double2*)output, (const double2*)deriv1,
-                                                   (const double2*)deriv2, intfactor, dt, n);
+        DD_KT("etd2rk22", st, k_etd2rk2<2><<<ew_blocks(n), 256, 0, st>>>((const double2*)start, (double2*)output, (const double2*)deriv1,
+                                                   (const double2*)deriv2, intfactor, dt, n));
     else
-        k_etd2rk2<3><<<ew_blocks(n), 256, 0, st>>>((const double2*)start, (double2*)output, (const double2*)deriv1,
-                                                   (const double2*)deriv2, intfactor, dt, n);
+        DD_KT("etd2rk23", st, k_etd2rk2<3><<<ew_blocks(n), 256, 0, st>>>((const double2*)start, (double2*)output, (const double2*)deriv1,
+                                                   (const double2*)deriv2, intfactor, dt, n));
     DD_LAUNCH_CHECK();
     return DD_OK;
 }
@@ -146,8 +147,8 @@ int dd_phi_table(int ndim, double nu, int viscosity_order, double h, int qmax, v
     DD_CHECK_ARG(viscosity_order >= 1, "dd_phi_table: viscosity_order must be >= 1");
     cudaStream_t st = (cudaStream_t)stream;
     const unsigned nb = (unsigned)((qmax + 256) / 256);
-    if (ndim == 2) k_phi_table<2><<<nb, 256, 0, st>>>(nu, viscosity_order, h, qmax, (double4*)table);
-    else           k_phi_table<3><<<nb, 256, 0, st>>>(nu, viscosity_order, h, qmax, (double4*)table);
+    if (ndim == 2) DD_KT("phi_table2", st, k_phi_table<2><<<nb, 256, 0, st>>>(nu, viscosity_order, h, qmax, (double4*)table));
+    else           DD_KT("phi_table3", st, k_phi_table<3><<<nb, 256, 0, st>>>(nu, viscosity_order, h, qmax, (double4*)table));
     DD_LAUNCH_CHECK();
     return DD_OK;
 }

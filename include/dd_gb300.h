@@ -45,6 +45,18 @@ int dd_version(void);
 /* Message describing this host thread's most recent failure ("" if none). */
 const char* dd_last_error(void);
 
+/* ------------------------------------------------------- observability
+ * Launch accounting and per-kernel device timing, the GPU analogue of the
+ * reference's cumulative @timer (dedalus/utils/timer.py:29-65).
+ * dd_launch_count: kernels launched by this library since load.
+ * dd_timing_enable(1): bracket every launch with CUDA events on its stream;
+ * dd_timing_report fills buf with "label count total_ms" lines (synchronises
+ * the recorded events); dd_timing_reset clears the totals. */
+long long dd_launch_count(void);
+int dd_timing_enable(int on);
+int dd_timing_reset(void);
+int dd_timing_report(char* buf, size_t len);
+
 /* ------------------------------------------------------------------ plans
  * One plan per grid geometry, the analogue of the reference's FFTW plan pair
  * (dedalus/utils/fftw/_fftw.pyx:246-309 rPlan, created in

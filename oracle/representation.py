@@ -15,6 +15,11 @@ import numpy.fft as npfft
 
 from . import _cstage
 
+# Threads for the FFTs when timing the CPU baseline.  1 = numpy.fft exactly as
+# the reference's FFT.method = numpy; > 1 = the same pocketfft algorithm
+# through scipy.fft with that many workers (timing only, never in parity tests).
+FFT_WORKERS = 1
+
 # dedalus/config.py:29-53 (the keys the hot path reads)
 decfg = configparser.ConfigParser()
 decfg.add_section('FFT')
@@ -164,11 +169,21 @@ class FourierRepresentation:
     def fwd_np(self):
         # representations.py:327-329: divide first, rfftn, transpose axes 0<->1
         tr = [1, 0, 2][:self.ndim]
+        if FFT_WORKERS > 1:
+            import scipy.fft as spfft
+            self.kdata[:] = np.transpose(spfft.rfftn(self.xdata / self.global_shape['xspace'].prod(),
+                                                     workers=FFT_WORKERS), tr)
+            return
         self.kdata[:] = np.transpose(npfft.rfftn(self.xdata / self.global_shape['xspace'].prod()), tr)
 
     def rev_np(self):
         # representations.py:331-333
         tr = [1, 0, 2][:self.ndim]
+        if FFT_WORKERS > 1:
+            import scipy.fft as spfft
+            self.xdata[:] = spfft.irfftn(np.transpose(self.kdata, tr), s=tuple(self.global_shape['xspace']),
+                                         workers=FFT_WORKERS) * self.global_shape['xspace'].prod()
+            return
         self.xdata[:] = npfft.irfftn(np.transpose(self.kdata, tr)) * self.global_shape['xspace'].prod()
 
     def forward(self):

@@ -16,7 +16,7 @@ def _declared():
         if fn.endswith(".h"):
             txt = open(os.path.join(ROOT, "include", fn)).read()
             txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
-            names |= set(re.findall(r"^\s*(?:const\s+)?\w+\s*\**\s*(dd_\w+)\s*\(", txt, flags=re.M))
+            names |= set(re.findall(r"^\s*[A-Za-z_][\w \*]*?\b(dd_\w+)\s*\(", txt, flags=re.M))
     return names
 
 
