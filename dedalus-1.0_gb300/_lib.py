@@ -42,6 +42,7 @@ SIGNATURES = {
     "dd_plan_workspace_size": [P, I, I, ctypes.POINTER(SZ)],
     "dd_fft_r2c": [P, I, PP, PP, I, P, SZ, P],
     "dd_fft_c2r": [P, I, PP, PP, I, P, SZ, P],
+    "dd_fft_c2r_noalloc": [P, P, P, P],
     "dd_dealias": [P, P, P],
     "dd_deriv": [P, I, P, P, P],
     "dd_scale_add": [P, P, D, I, I64, P],

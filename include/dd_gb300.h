@@ -87,6 +87,19 @@ int dd_fft_r2c(const dd_plan* plan, int nfield, const double* const* x, void* co
 int dd_fft_c2r(const dd_plan* plan, int nfield, const void* const* k, double* const* x,
                int precision, void* work, size_t work_bytes, void* stream);
 
+/* Backward transform of one FP64 field, as dd_fft_c2r with nfield = 1, that
+ * allocates nothing and takes no workspace.  No counterpart in the reference:
+ * it exists for callers that cannot allocate device memory (an application
+ * pool owns all of it, a per-call cudaMalloc and its device-wide
+ * synchronisation are not allowed, or the caller's host language has no
+ * device allocator).  Intermediates live in a 4 MiB static device buffer in
+ * the library image (held on every GPU that loads the library): grids up to
+ * 64^3 (3D) and 512^2 (2D); larger ones return DD_ERR_UNSUPPORTED.  The first
+ * call on a device looks the buffer up (cudaGetSymbolAddress) and should come
+ * before any stream capture.  All calls share the buffer: calls whose GPU
+ * work overlaps race, so issue them in order on one stream. */
+int dd_fft_c2r_noalloc(const dd_plan* plan, const void* k, double* x, void* stream);
+
 /* In-place 2/3 dealiasing of one k array.  Replaces dealias_cy_{2d,3d}.dealias_23
  * (dedalus/data_objects/dealias_cy_3d.pyx:13-37, dealias_cy_2d.pyx:59-78). */
 int dd_dealias(const dd_plan* plan, void* k, void* stream);
