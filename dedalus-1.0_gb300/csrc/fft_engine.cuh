@@ -127,21 +127,36 @@ template <> struct FFTCfg<256>  { static constexpr int P = 16, NT = 256, R1 = 16
 template <> struct FFTCfg<512>  { static constexpr int P = 8,  NT = 256, R1 = 8,  R2 = 8,  R3 = 8; };
 template <> struct FFTCfg<1024> { static constexpr int P = 4,  NT = 256, R1 = 16, R2 = 16, R3 = 4; };
 
-template <int L>
-struct Pencil {
-    static constexpr int P = FFTCfg<L>::P;
-    static constexpr int NT = FFTCfg<L>::NT;
-    static constexpr int PS = P + 1;  // odd row stride (complex entries)
+// A schedule: length L, P pencils per tile, NT threads (TPP = NT / P per
+// pencil) and the radix sequence R1 R2 R3 (1 = unused).
+template <int L_, int P_, int NT_, int R1_, int R2_, int R3_>
+struct Sched {
+    static constexpr int L = L_, P = P_, NT = NT_, R1 = R1_, R2 = R2_, R3 = R3_;
+    static constexpr int PS = P | 1;   // odd row stride (complex entries), >= P
     static constexpr int TPP = NT / P;
+    static_assert(NT % P == 0, "threads must split evenly over pencils");
+    static_assert(R1 * R2 * R3 == L, "radix schedule does not multiply to L");
     template <typename T>
     static constexpr size_t smem_bytes() { return sizeof(C<T>) * ((size_t)L * PS + L); }
 };
 
+template <int L>
+using DefSched = Sched<L, FFTCfg<L>::P, FFTCfg<L>::NT, FFTCfg<L>::R1, FFTCfg<L>::R2, FFTCfg<L>::R3>;
+
+template <int L>
+struct Pencil {
+    static constexpr int P = FFTCfg<L>::P;
+    static constexpr int NT = FFTCfg<L>::NT;
+    static constexpr int PS = DefSched<L>::PS;
+    static constexpr int TPP = NT / P;
+    template <typename T>
+    static constexpr size_t smem_bytes() { return DefSched<L>::template smem_bytes<T>(); }
+};
+
 // One Stockham pass of radix R with current sub-transform length NS.
-template <typename T, int L, int R, int NS, bool INV>
+template <typename T, class S, int R, int NS, bool INV>
 __device__ __forceinline__ void stockham_pass(C<T>* tile, const C<T>* tw, int p, int jt) {
-    constexpr int PS = Pencil<L>::PS;
-    constexpr int TPP = Pencil<L>::TPP;
+    constexpr int L = S::L, PS = S::PS, TPP = S::TPP;
     constexpr int NB = L / R;          // butterflies per pencil
     constexpr int BPT = NB / TPP;      // butterflies per thread
     static_assert(BPT >= 1 && NB % TPP == 0, "bad radix schedule");
@@ -173,19 +188,28 @@ __device__ __forceinline__ void stockham_pass(C<T>* tile, const C<T>* tw, int p,
     __syncthreads();
 }
 
-// Transform every pencil of the tile in place.  Must be called by all NT
-// threads of the block; the caller synchronises before (tile filled) and this
-// returns synchronised (tile holds the result in natural order).
+// Transform the S::P pencils of the tile in place.  Called by the first S::NT
+// threads of the block (all of them must reach the barriers: threads beyond
+// S::NT call with active = false).  The caller synchronises before (tile
+// filled); this returns synchronised with the result in natural order.
+template <typename T, class S, bool INV>
+__device__ __forceinline__ void pencil_fft_s(C<T>* tile, const C<T>* tw, bool active = true) {
+    const int p = active ? threadIdx.x % S::P : 0;
+    const int jt = active ? threadIdx.x / S::P : 0;
+    if (active) {
+        stockham_pass<T, S, S::R1, 1, INV>(tile, tw, p, jt);
+        if constexpr (S::R2 > 1) stockham_pass<T, S, S::R2, S::R1, INV>(tile, tw, p, jt);
+        if constexpr (S::R3 > 1) stockham_pass<T, S, S::R3, S::R1 * S::R2, INV>(tile, tw, p, jt);
+    } else {
+        __syncthreads(); __syncthreads();
+        if constexpr (S::R2 > 1) { __syncthreads(); __syncthreads(); }
+        if constexpr (S::R3 > 1) { __syncthreads(); __syncthreads(); }
+    }
+}
+
 template <typename T, int L, bool INV>
 __device__ __forceinline__ void pencil_fft(C<T>* tile, const C<T>* tw) {
-    using Cfg = FFTCfg<L>;
-    constexpr int P = Pencil<L>::P;
-    const int p = threadIdx.x % P;
-    const int jt = threadIdx.x / P;
-    stockham_pass<T, L, Cfg::R1, 1, INV>(tile, tw, p, jt);
-    if constexpr (Cfg::R2 > 1) stockham_pass<T, L, Cfg::R2, Cfg::R1, INV>(tile, tw, p, jt);
-    if constexpr (Cfg::R3 > 1) stockham_pass<T, L, Cfg::R3, Cfg::R1 * Cfg::R2, INV>(tile, tw, p, jt);
-    static_assert(Cfg::R1 * Cfg::R2 * Cfg::R3 == L, "radix schedule does not multiply to L");
+    pencil_fft_s<T, DefSched<L>, INV>(tile, tw);
 }
 
 // Stage the length-L twiddle table (global, L entries) into shared memory.

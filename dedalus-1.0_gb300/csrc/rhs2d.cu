@@ -1,0 +1,398 @@
+// Fused 2D right-hand sides and RK2mid step for incompressible hydro and
+// Boussinesq flows, batched over independent runs of one grid size.
+//
+//   hydro:       RHS(u) = P[u x w z]^, w = d_x u_y - d_y u_x          (physics.py:527-599)
+//   Boussinesq:  RHS(u) = P[u x w z + g alpha T e_dir]^,
+//                RHS(T) = -(u.grad T)^ - beta u_dir                      (physics.py:664-712)
+// The rotational form of the momentum term equals the reference's advective
+// form on the kept modes to roundoff (the difference is a gradient removed by
+// the projection).  u.grad T is formed in x-space as u_x dT/dx + u_y dT/dy, the
+// reference's XgradY order (physics.py:221-225).
+//
+// Passes (k-layout [kx][ky], x-layout [y][x]; run b of a batch is offset by a
+// per-run stride):
+//   1  Y^-1 per kx row (kept ky), with w (and grad T) formed while loading
+//   2  X c2r -> pointwise products -> X r2c, scaled by 1/N   (k_x_prod)
+//   3  Y forward, kept ky, into a compact [kxc][kyc] buffer
+//   4  projection + buoyancy / stratification terms + RK2mid stage
+#include "launch_len.cuh"
+#include "xprod.cuh"
+#include "etd.cuh"
+
+namespace dd {
+
+__device__ __forceinline__ double2 ideriv2(double2 a, double k) { return make_double2(-(a.y * k), a.x * k); }
+
+enum { PHYS_HYDRO = 0, PHYS_BOUSS = 1 };
+
+template <int PHYS> struct Phys2;
+template <> struct Phys2<PHYS_HYDRO> { static constexpr int NF = 2, NI = 3, NO = 2; };
+template <> struct Phys2<PHYS_BOUSS> { static constexpr int NF = 3, NI = 5, NO = 3; };
+
+// ------------------------------------------------------------------ pass 1
+template <typename T, bool COMPACT, int PHYS>
+struct OpYInvPhys2 {
+    using V = typename Vec2<T>::type;
+    static constexpr const char* name = PHYS == PHYS_HYDRO ? "y_inv_hydro2d" : "y_inv_bouss2d";
+    Geo2 g; CPtrs st; int64_t st_rs; Ptrs out; int64_t w_rs; const V* tw;
+    const double* kx; const double* ky;
+    __device__ int npencil() const { return g.Kx; }
+    __device__ int nstore() const { return g.Ny; }
+    __device__ double2 get(int c, int run, int ix, int e) const {
+        const double2* S = (const double2*)st.p[c] + run * st_rs;
+        if (COMPACT) return S[(int64_t)ix * g.Ky + full_to_compact(e, g.Ny, g.Ky)];
+        return S[(int64_t)ix * g.Ny + e];
+    }
+    __device__ C<T> load(int fld, int run, int e, int ix) const {
+        if (!kept_full(e, g.Ny, g.My)) return zero<T>();
+        double2 r;
+        if (fld < 2) r = get(fld, run, ix, e);
+        else if (fld == 2) {  // curlX, N == 2: X[1].deriv(x) - X[0].deriv(y)  (physics.py:400)
+            const double2 a = ideriv2(get(1, run, ix, e), kx[ix]), b = ideriv2(get(0, run, ix, e), ky[e]);
+            r = make_double2(a.x - b.x, a.y - b.y);
+        } else if (fld == 3) r = ideriv2(get(2, run, ix, e), kx[ix]);
+        else r = ideriv2(get(2, run, ix, e), ky[e]);
+        return mk<T>((T)r.x, (T)r.y);
+    }
+    __device__ void store(int fld, int run, int e, int ix, const C<T>* col, int PS) const {
+        stc<T>((V*)out.p[fld] + run * w_rs + (int64_t)e * g.Kx + ix, col[e * PS]);
+    }
+};
+
+// ------------------------------------------------------------------ pass 2
+template <typename T>
+struct ProdHydro2 {
+    static constexpr int NI = 3, NO = 2;
+    __device__ void operator()(const T* in, T* out, int) const {
+        out[0] = in[1] * in[2];       // u_y w
+        out[1] = -(in[0] * in[2]);    // -u_x w
+    }
+};
+template <typename T>
+struct ProdBouss2 {
+    static constexpr int NI = 5, NO = 3;
+    __device__ void operator()(const T* in, T* out, int) const {
+        out[0] = in[1] * in[2];
+        out[1] = -(in[0] * in[2]);
+        out[2] = in[0] * in[3] + in[1] * in[4];   // u_x dT/dx + u_y dT/dy
+    }
+};
+
+// ------------------------------------------------------------------ pass 3
+template <typename T>
+struct OpYFwdCompact2 {
+    using V = typename Vec2<T>::type;
+    static constexpr const char* name = "y_fwd_compact2d";
+    Geo2 g; CPtrs in; int64_t w_rs; Ptrs out; int64_t nc_rs; const V* tw;
+    __device__ int npencil() const { return g.Kx; }
+    __device__ int nstore() const { return g.Ny; }
+    __device__ C<T> load(int fld, int run, int e, int ix) const {
+        return ldc<T>((const V*)in.p[fld] + run * w_rs + (int64_t)e * g.Kx + ix);
+    }
+    __device__ void store(int fld, int run, int e, int ix, const C<T>* col, int PS) const {
+        if (!kept_full(e, g.Ny, g.My)) return;
+        const C<T> c = col[e * PS];
+        ((double2*)out.p[fld])[run * nc_rs + (int64_t)ix * g.Ky + full_to_compact(e, g.Ny, g.Ky)] =
+            make_double2((double)c.x, (double)c.y);
+    }
+};
+
+// ------------------------------------------------------------------ pass 4
+struct Phys2Params {
+    double g, alpha_t, beta;
+    int dir;   // component receiving buoyancy (0 = x, 1 = y)
+};
+
+struct Stage2Args {
+    Geo2 g;
+    const double* kx; const double* ky; const double* inv_k2; int intk;
+    int phys; Phys2Params pp;
+    int nrun;
+    CPtrs nc; int64_t nc_rs;          // unprojected products (compact)
+    CPtrs rin; int64_t rin_rs; int rin_compact;   // state the RHS was evaluated on
+    Ptrs y; int64_t y_rs;             // state (full layout)
+    Ptrs ys; Ptrs k1; int64_t c_rs;   // stage state / first derivative (compact)
+    Ptrs deriv; int64_t d_rs;         // RHS output (full layout), mode 0
+    const double4* tab[3];            // phi tables per state field for this stage (q-indexed) or null
+    double nu[3]; int vo; double h;
+    int mode;                         // 0 = write deriv, 1 = RK2mid stage 1, 2 = RK2mid stage 2
+};
+
+__device__ __forceinline__ void project2(double2& nx, double2& ny, double kxv, double kyv, double s) {
+    const double2 dx = ideriv2(nx, kxv), dy = ideriv2(ny, kyv);
+    const double2 dv = make_double2(radd(dx.x, dy.x), radd(dx.y, dy.y));
+    const double2 ph = make_double2(-rmul(dv.x, s), -rmul(dv.y, s));
+    const double2 gx = ideriv2(ph, kxv), gy = ideriv2(ph, kyv);
+    nx = make_double2(rsub(nx.x, gx.x), rsub(nx.y, gx.y));
+    ny = make_double2(rsub(ny.x, gy.x), rsub(ny.y, gy.y));
+}
+
+__device__ __forceinline__ void phis2(const Stage2Args& a, int c, int q, double k2, double& Z, double& f0,
+                                      double& f1, double& f2) {
+    if (a.tab[c]) {
+        const double4 t = a.tab[c][q];
+        Z = t.x; f0 = t.y; f1 = t.z; f2 = t.w;
+    } else {
+        const double k2v = a.vo == 1 ? k2 : (a.vo == 2 ? rmul(k2, k2) : pow(k2, (double)a.vo));
+        Z = rmul(-rmul(a.nu[c], k2v), a.h);
+        f0 = 1.; f1 = 1.; f2 = 0.5;
+        if (Z != 0.) etd_phis<2>(Z, f0, f1, f2);
+    }
+}
+
+__global__ void k_stage2(Stage2Args a) {
+    const Geo2& g = a.g;
+    const int64_t per = (int64_t)g.Kx * g.Ky;
+    const int64_t n = per * a.nrun;
+    const int nf = a.phys == PHYS_HYDRO ? 2 : 3;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int run = (int)(i / per);
+        const int64_t j = i - run * per;
+        const int kyc = (int)(j % g.Ky), ix = (int)(j / g.Ky);
+        const int ky_i = compact_to_full(kyc, g.Ny, g.Ky);
+        const double kxv = a.kx[ix], kyv = a.ky[ky_i];
+        // k2 = (0 + kx^2) + ky^2 (2D k dict order x, y)
+        const double k2 = radd(rmul(kxv, kxv), rmul(kyv, kyv));
+        const int q = a.intk ? (int)k2 : 0;
+        double s;
+        if (a.intk && a.inv_k2) s = a.inv_k2[q];
+        else s = rdiv(1., k2 == 0. ? 1. : k2);
+        double2 N[3];
+        N[0] = ((const double2*)a.nc.p[0])[run * a.nc_rs + j];
+        N[1] = ((const double2*)a.nc.p[1])[run * a.nc_rs + j];
+        if (a.phys == PHYS_BOUSS) {
+            const int64_t ri = a.rin_compact ? run * a.rin_rs + j : run * a.rin_rs + (int64_t)ix * g.Ny + ky_i;
+            const double2 T = ((const double2*)a.rin.p[2])[ri];
+            const double2 ud = ((const double2*)a.rin.p[a.pp.dir])[ri];
+            // buoyancy: ((T * g) * alpha_t) added to u_dir (physics.py:691-694)
+            const double2 b = make_double2(rmul(rmul(T.x, a.pp.g), a.pp.alpha_t), rmul(rmul(T.y, a.pp.g), a.pp.alpha_t));
+            N[a.pp.dir] = make_double2(radd(N[a.pp.dir].x, b.x), radd(N[a.pp.dir].y, b.y));
+            // temperature: (-(u.grad T)) - (u_dir * beta) (physics.py:702-708)
+            const double2 adv = ((const double2*)a.nc.p[2])[run * a.nc_rs + j];
+            N[2] = make_double2(rsub(-adv.x, rmul(ud.x, a.pp.beta)), rsub(-adv.y, rmul(ud.y, a.pp.beta)));
+        }
+        project2(N[0], N[1], kxv, kyv, s);
+        const int64_t full = run * a.y_rs + (int64_t)ix * g.Ny + ky_i;
+        for (int c = 0; c < nf; c++) {
+            if (a.mode == 0) {
+                ((double2*)a.deriv.p[c])[run * a.d_rs + (int64_t)ix * g.Ny + ky_i] = N[c];
+                continue;
+            }
+            double Z, f0, f1, f2;
+            phis2(a, c, q, k2, Z, f0, f1, f2);
+            const double2 y0 = ((const double2*)a.y.p[c])[full];
+            const int64_t ci = run * a.c_rs + j;
+            if (a.mode == 1) {
+                ((double2*)a.k1.p[c])[ci] = N[c];
+                ((double2*)a.ys.p[c])[ci] = etd1_entry(y0, N[c], Z, f0, f1, a.h);
+            } else {
+                const double2 d1 = ((const double2*)a.k1.p[c])[ci];
+                ((double2*)a.y.p[c])[full] = etd2rk2_entry(y0, d1, N[c], Z, f0, f1, f2, a.h);
+            }
+        }
+    }
+}
+
+// Non-kept modes see no forcing: RK2mid gives y <- etd2rk2(y, 0, 0, dt) = f0 y.
+__global__ void k_decay_nonkept2(Geo2 g, Ptrs y, int64_t y_rs, int nf, int nrun, const double* kx,
+                                 const double* ky, Stage2Args a) {
+    const int64_t per = g.kcount(), n = per * nrun;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int run = (int)(i / per);
+        const int64_t j = i - run * per;
+        const int ky_i = (int)(j % g.Ny), ix = (int)(j / g.Ny);
+        if (ix <= g.Mx && kept_full(ky_i, g.Ny, g.My)) continue;
+        const double k2 = radd(rmul(kx[ix], kx[ix]), rmul(ky[ky_i], ky[ky_i]));
+        const int q = a.intk ? (int)k2 : 0;
+        for (int c = 0; c < nf; c++) {
+            double2* Y = (double2*)y.p[c] + run * y_rs;
+            const double2 y0 = Y[j];
+            if (y0.x == 0. && y0.y == 0.) continue;
+            double Z, f0, f1, f2;
+            phis2(a, c, q, k2, Z, f0, f1, f2);
+            const double2 z = make_double2(0., 0.);
+            Y[j] = etd2rk2_entry(y0, z, z, Z, f0, f1, f2, a.h);
+        }
+    }
+}
+
+__global__ void k_zero_nonkept2_all(Geo2 g, Ptrs k, int64_t rs, int nrun) {
+    double2* K = (double2*)k.p[blockIdx.y];
+    const int64_t per = g.kcount(), n = per * nrun;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int run = (int)(i / per);
+        const int64_t j = i - run * per;
+        const int ky_i = (int)(j % g.Ny), ix = (int)(j / g.Ny);
+        if (ix > g.Mx || !kept_full(ky_i, g.Ny, g.My)) K[run * rs + j] = make_double2(0., 0.);
+    }
+}
+
+static unsigned ew_grid2(int64_t n) {
+    int64_t b = (n + 255) / 256;
+    if (b > 152 * 16) b = 152 * 16;
+    return (unsigned)(b < 1 ? 1 : b);
+}
+
+// ------------------------------------------------------------ driver
+struct Work2 {
+    size_t w, kc;  // complex entries per (field, run): W = Ny*Kx, compact = Kx*Ky
+    int nrun;
+    char* base;
+    template <typename T> C<T>* W(int f) const { return (C<T>*)base + (size_t)f * nrun * w; }
+    template <typename T> double2* NC(int f) const {
+        return (double2*)((char*)base + sizeof(C<T>) * 5 * nrun * w) + (size_t)f * nrun * kc;
+    }
+    template <typename T> double2* K1(int f) const { return NC<T>(3) + (size_t)f * nrun * kc; }
+    template <typename T> double2* YS(int f) const { return NC<T>(6) + (size_t)f * nrun * kc; }
+    template <typename T> static size_t bytes(const Geo2& g, int nrun) {
+        return sizeof(C<T>) * 5 * (size_t)nrun * g.wcount() + sizeof(double2) * 9 * (size_t)nrun * g.Kx * g.Ky;
+    }
+};
+
+template <typename T, bool COMPACT, int PHYS>
+static int nonlinear2(const dd_plan* pl, const Work2& w, const void* const* st, int64_t st_rs, cudaStream_t s) {
+    const Geo2& g = pl->g2;
+    using PH = Phys2<PHYS>;
+    CPtrs sin{}; Ptrs wo{}; CPtrs wi{}; Ptrs nc{};
+    for (int c = 0; c < PH::NF; c++) sin.p[c] = st[c];
+    for (int f = 0; f < PH::NI; f++) { wo.p[f] = w.W<T>(f); wi.p[f] = wo.p[f]; }
+    for (int f = 0; f < PH::NO; f++) nc.p[f] = w.NC<T>(f);
+    OpYInvPhys2<T, COMPACT, PHYS> a{g, sin, st_rs, wo, (int64_t)w.w, TwSel<T>::y(pl), pl->kx, pl->ky};
+    DD_TRY((launch_pass_len<T, true, true, false>(g.Ny, a, g.Kx, w.nrun, PH::NI, s)));
+    if (PHYS == PHYS_HYDRO) {
+        DD_TRY((launch_x_prod_len<T>("x_prod_hydro2d", g.Nx, g.Ny, g.Kx, wi, wo, w.nrun, (int64_t)w.w, (int64_t)w.w,
+                                     TwSel<T>::x(pl), (T)pl->inv_n, ProdHydro2<T>{}, s)));
+    } else {
+        DD_TRY((launch_x_prod_len<T>("x_prod_bouss2d", g.Nx, g.Ny, g.Kx, wi, wo, w.nrun, (int64_t)w.w, (int64_t)w.w,
+                                     TwSel<T>::x(pl), (T)pl->inv_n, ProdBouss2<T>{}, s)));
+    }
+    OpYFwdCompact2<T> c{g, wi, (int64_t)w.w, nc, (int64_t)w.kc, TwSel<T>::y(pl)};
+    DD_TRY((launch_pass_len<T, false, false, true>(g.Ny, c, g.Kx, w.nrun, PH::NO, s)));
+    return DD_OK;
+}
+
+template <int PHYS>
+static int nonlinear2_any(const dd_plan* pl, int prec, bool compact, const Work2& w, const void* const* st,
+                          int64_t st_rs, cudaStream_t s) {
+    if (prec == DD_FP64) return compact ? nonlinear2<double, true, PHYS>(pl, w, st, st_rs, s)
+                                        : nonlinear2<double, false, PHYS>(pl, w, st, st_rs, s);
+    return compact ? nonlinear2<float, true, PHYS>(pl, w, st, st_rs, s)
+                   : nonlinear2<float, false, PHYS>(pl, w, st, st_rs, s);
+}
+
+static int nonlinear2_phys(int phys, const dd_plan* pl, int prec, bool compact, const Work2& w,
+                           const void* const* st, int64_t st_rs, cudaStream_t s) {
+    if (phys == PHYS_HYDRO) return nonlinear2_any<PHYS_HYDRO>(pl, prec, compact, w, st, st_rs, s);
+    return nonlinear2_any<PHYS_BOUSS>(pl, prec, compact, w, st, st_rs, s);
+}
+
+static void fill_common(Stage2Args& a, const dd_plan* p, int phys, const double* pp, const double* inv_k2,
+                        int nrun, const Work2& w, int prec) {
+    a.g = p->g2; a.kx = p->kx; a.ky = p->ky; a.inv_k2 = inv_k2; a.intk = inv_k2 != nullptr;
+    a.phys = phys; a.nrun = nrun;
+    if (pp) { a.pp.g = pp[0]; a.pp.alpha_t = pp[1]; a.pp.beta = pp[2]; a.pp.dir = (int)pp[3]; }
+    const int no = phys == PHYS_HYDRO ? 2 : 3;
+    for (int f = 0; f < no; f++)
+        a.nc.p[f] = prec == DD_FP64 ? (void*)w.NC<double>(f) : (void*)w.NC<float>(f);
+    a.nc_rs = (int64_t)w.kc; a.c_rs = (int64_t)w.kc;
+}
+
+static int check2(const dd_plan* p, int phys, int nrun, const double* pp) {
+    DD_CHECK_ARG(p && p->ndim == 2, "plan must be 2D");
+    DD_CHECK_ARG(phys == PHYS_HYDRO || phys == PHYS_BOUSS, "physics must be 0 (hydro) or 1 (Boussinesq)");
+    DD_CHECK_ARG(nrun >= 1 && nrun <= 65535, "nrun must be in [1, 65535]");
+    if (phys == PHYS_BOUSS) {
+        DD_CHECK_ARG(pp, "Boussinesq parameters required");
+        DD_CHECK_ARG(pp[3] == 0. || pp[3] == 1., "boussinesq direction must be 0 (x) or 1 (y) in 2D");
+    }
+    return DD_OK;
+}
+
+}  // namespace dd
+
+using namespace dd;
+
+extern "C" {
+
+int dd_rhs2d_workspace_size(const dd_plan* p, int nrun, int precision, size_t* bytes) {
+    DD_CHECK_ARG(p && bytes && p->ndim == 2 && nrun >= 1, "dd_rhs2d_workspace_size: bad arguments");
+    *bytes = precision == DD_FP32 ? Work2::bytes<float>(p->g2, nrun) : Work2::bytes<double>(p->g2, nrun);
+    return DD_OK;
+}
+
+int dd_rhs2d(const dd_plan* p, int phys, const double* params, int nrun, const void* const* state, int64_t state_rs,
+             void* const* deriv, int64_t deriv_rs, const double* inv_k2, int precision, int zero_nonkept, void* work,
+             size_t work_bytes, void* stream) {
+    DD_TRY(check2(p, phys, nrun, params));
+    DD_CHECK_ARG(state && deriv && work, "dd_rhs2d: null pointer");
+    const int nf = phys == PHYS_HYDRO ? 2 : 3;
+    for (int c = 0; c < nf; c++) DD_CHECK_ARG(state[c] && deriv[c], "dd_rhs2d: null field pointer %d", c);
+    DD_CHECK_ARG(precision == DD_FP64 || precision == DD_FP32, "bad precision");
+    const size_t need = precision == DD_FP32 ? Work2::bytes<float>(p->g2, nrun) : Work2::bytes<double>(p->g2, nrun);
+    DD_CHECK_ARG(work_bytes >= need, "workspace too small: %zu < %zu", work_bytes, need);
+    cudaStream_t st = (cudaStream_t)stream;
+    Work2 w{(size_t)p->g2.wcount(), (size_t)p->g2.Kx * p->g2.Ky, nrun, (char*)work};
+    DD_TRY(nonlinear2_phys(phys, p, precision, false, w, state, state_rs, st));
+    Stage2Args a{};
+    fill_common(a, p, phys, params, inv_k2, nrun, w, precision);
+    for (int c = 0; c < nf; c++) { a.rin.p[c] = state[c]; a.deriv.p[c] = deriv[c]; }
+    a.rin_rs = state_rs; a.rin_compact = 0; a.d_rs = deriv_rs; a.mode = 0; a.y_rs = 0;
+    if (zero_nonkept) {
+        Ptrs d{};
+        for (int c = 0; c < nf; c++) d.p[c] = deriv[c];
+        DD_KT("zero_nonkept2", st, k_zero_nonkept2_all<<<dim3(ew_grid2(p->g2.kcount() * nrun), nf), 256, 0, st>>>(
+                                       p->g2, d, deriv_rs, nrun));
+        DD_LAUNCH_CHECK();
+    }
+    DD_KT("stage2d", st, k_stage2<<<ew_grid2((int64_t)p->g2.Kx * p->g2.Ky * nrun), 256, 0, st>>>(a));
+    DD_LAUNCH_CHECK();
+    return DD_OK;
+}
+
+int dd_rk2mid_step2d(const dd_plan* p, int phys, const double* params, int nrun, void* const* state,
+                     int64_t state_rs, const double* inv_k2, const void* const* tab_half,
+                     const void* const* tab_full, const double* nu, int viscosity_order, double dt,
+                     int precision, void* work, size_t work_bytes, void* stream) {
+    DD_TRY(check2(p, phys, nrun, params));
+    DD_CHECK_ARG(state && work && nu, "dd_rk2mid_step2d: null pointer");
+    DD_CHECK_ARG(viscosity_order >= 1, "viscosity_order must be >= 1");
+    const int nf = phys == PHYS_HYDRO ? 2 : 3;
+    for (int c = 0; c < nf; c++) DD_CHECK_ARG(state[c], "dd_rk2mid_step2d: null field pointer %d", c);
+    DD_CHECK_ARG(precision == DD_FP64 || precision == DD_FP32, "bad precision");
+    const bool intk = inv_k2 != nullptr;
+    DD_CHECK_ARG(!intk || (tab_half && tab_full), "phi tables required with integer wavenumbers");
+    const size_t need = precision == DD_FP32 ? Work2::bytes<float>(p->g2, nrun) : Work2::bytes<double>(p->g2, nrun);
+    DD_CHECK_ARG(work_bytes >= need, "workspace too small: %zu < %zu", work_bytes, need);
+    cudaStream_t st = (cudaStream_t)stream;
+    Work2 w{(size_t)p->g2.wcount(), (size_t)p->g2.Kx * p->g2.Ky, nrun, (char*)work};
+    Stage2Args a{};
+    fill_common(a, p, phys, params, inv_k2, nrun, w, precision);
+    a.vo = viscosity_order;
+    for (int c = 0; c < nf; c++) {
+        a.y.p[c] = state[c];
+        a.nu[c] = nu[c];
+        a.ys.p[c] = precision == DD_FP64 ? (void*)w.YS<double>(c) : (void*)w.YS<float>(c);
+        a.k1.p[c] = precision == DD_FP64 ? (void*)w.K1<double>(c) : (void*)w.K1<float>(c);
+    }
+    a.y_rs = state_rs;
+    const unsigned nb = ew_grid2((int64_t)p->g2.Kx * p->g2.Ky * nrun);
+    // stage 1: k1 = N(y); y2 = etd1(y, k1, dt/2)            (time_step.py:286-294)
+    DD_TRY(nonlinear2_phys(phys, p, precision, false, w, (const void* const*)state, state_rs, st));
+    for (int c = 0; c < nf; c++) { a.rin.p[c] = state[c]; a.tab[c] = intk ? (const double4*)tab_half[c] : nullptr; }
+    a.rin_rs = state_rs; a.rin_compact = 0; a.h = dt / 2.; a.mode = 1;
+    DD_KT("rk2mid_stage2d", st, k_stage2<<<nb, 256, 0, st>>>(a));
+    DD_LAUNCH_CHECK();
+    // stage 2: k2 = N(y2); y = etd2rk2(y, k1, k2, dt)       (time_step.py:297-305)
+    const void* ysp[3] = {a.ys.p[0], a.ys.p[1], a.ys.p[2]};
+    DD_TRY(nonlinear2_phys(phys, p, precision, true, w, ysp, (int64_t)w.kc, st));
+    for (int c = 0; c < nf; c++) { a.rin.p[c] = ysp[c]; a.tab[c] = intk ? (const double4*)tab_full[c] : nullptr; }
+    a.rin_rs = (int64_t)w.kc; a.rin_compact = 1; a.h = dt; a.mode = 2;
+    DD_KT("rk2mid_stage2d", st, k_stage2<<<nb, 256, 0, st>>>(a));
+    DD_LAUNCH_CHECK();
+    DD_KT("decay_nonkept2", st, k_decay_nonkept2<<<ew_grid2(p->g2.kcount() * nrun), 256, 0, st>>>(
+                                    p->g2, a.y, state_rs, nf, nrun, p->kx, p->ky, a));
+    DD_LAUNCH_CHECK();
+    return DD_OK;
+}
+
+}  // extern "C"

@@ -15,6 +15,7 @@
 //   6  solenoidal projection (physics.py:588-599, laplace_solve
 //      407-416) fused with the RK stage update (etd1 with phi tables).
 #include "launch_len.cuh"
+#include "xprod.cuh"
 #include "etd.cuh"
 
 namespace dd {
@@ -63,109 +64,17 @@ struct OpZInvCurl3 {
 };
 
 // ------------------------------------------------------------------ pass 3
-template <int L> struct CrossCfg {
-    static constexpr int P = Pencil<L>::P;
-    static constexpr int Q = ((P / 3) / 2) * 2;   // rows per block (even)
-    static constexpr int NT = Pencil<L>::NT;
-    static constexpr int NPT = (L * Q + NT - 1) / NT;
-};
-
-template <typename T, int L>
-__global__ void __launch_bounds__(FFTCfg<L>::NT)
-k_x_cross3(int nrows, int Kx, CPtrs win, Ptrs wout, const typename Vec2<T>::type* gtw, T scale) {
-    using V = typename Vec2<T>::type;
-    extern __shared__ __align__(16) unsigned char dd_smem[];
-    constexpr int PS = Pencil<L>::PS, NT = Pencil<L>::NT;
-    constexpr int Q = CrossCfg<L>::Q, NPT = CrossCfg<L>::NPT;
-    static_assert(Q >= 2, "need at least two rows per block");
-    C<T>* tile = reinterpret_cast<C<T>*>(dd_smem);
-    C<T>* tw = tile + L * PS;
-    load_twiddles<T, L>(tw, gtw);
-    const int row0 = blockIdx.x * Q;
-    const int nr = min(Q, nrows - row0);
-    // packed inverse pencils: 3r + j holds fields (2j, 2j+1) of row r
-    for (int idx = threadIdx.x; idx < L * 3 * Q; idx += NT) {
-        const int e = idx % L, pj = idx / L, r = pj / 3, j = pj % 3;
-        C<T> z = zero<T>();
-        if (r < nr) {
-            const int64_t off = (int64_t)(row0 + r) * Kx;
-            z = pack_rows<T>((const V*)win.p[2 * j] + off, (const V*)win.p[2 * j + 1] + off, e, L, Kx);
-        }
-        tile[e * PS + pj] = z;
-    }
-    __syncthreads();
-    pencil_fft<T, L, true>(tile, tw);
-    // u x w, pointwise
-    T cx[NPT], cy[NPT], cz[NPT];
-#pragma unroll
-    for (int i = 0; i < NPT; i++) {
-        const int idx = threadIdx.x + i * NT;
-        if (idx < L * Q) {
-            const int e = idx % L, r = idx / L;
-            const C<T> a = tile[e * PS + 3 * r], b = tile[e * PS + 3 * r + 1], c = tile[e * PS + 3 * r + 2];
-            const T ux = a.x, uy = a.y, uz = b.x, wx = b.y, wy = c.x, wz = c.y;
-            cx[i] = uy * wz - uz * wy;
-            cy[i] = uz * wx - ux * wz;
-            cz[i] = ux * wy - uy * wx;
-        }
-    }
-    __syncthreads();
-    // forward pencils: r holds (cx, cy) of row r; Q + r/2 holds cz of rows (2i, 2i+1)
-#pragma unroll
-    for (int i = 0; i < NPT; i++) {
-        const int idx = threadIdx.x + i * NT;
-        if (idx < L * Q) {
-            const int e = idx % L, r = idx / L;
-            tile[e * PS + r] = mk<T>(cx[i], cy[i]);
-            if (r & 1) tile[e * PS + Q + r / 2].y = cz[i];
-            else tile[e * PS + Q + r / 2].x = cz[i];
-        }
-    }
-    __syncthreads();
-    pencil_fft<T, L, false>(tile, tw);
-    for (int idx = threadIdx.x; idx < Kx * Q; idx += NT) {
-        const int k = idx % Kx, r = idx / Kx;
-        if (r >= nr) continue;
-        const int64_t off = (int64_t)(row0 + r) * Kx + k;
-        C<T> A, B;
-        unpack_rows<T>(tile + r, PS, k, L, scale, A, B);
-        stc<T>((V*)wout.p[0] + off, A);
-        stc<T>((V*)wout.p[1] + off, B);
-        unpack_rows<T>(tile + Q + r / 2, PS, k, L, scale, A, B);
-        stc<T>((V*)wout.p[2] + off, (r & 1) ? B : A);
-    }
-}
-
-template <typename T, int L>
-static int launch_cross3(int nrows, int Kx, const CPtrs& win, const Ptrs& wout, const typename Vec2<T>::type* tw,
-                         T scale, cudaStream_t st) {
-    const size_t smem = Pencil<L>::template smem_bytes<T>();
-    static bool configured = false;
-    if (!configured) {
-        DD_CUDA(cudaFuncSetAttribute(k_x_cross3<T, L>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        configured = true;
-    }
-    static const std::string label = std::string("x_cross_") + std::to_string(L) + (sizeof(T) == 8 ? "_f64" : "_f32");
-    DD_KT(label.c_str(), st,
-          k_x_cross3<T, L><<<cdiv(nrows, CrossCfg<L>::Q), Pencil<L>::NT, smem, st>>>(nrows, Kx, win, wout, tw, scale));
-    DD_LAUNCH_CHECK();
-    return DD_OK;
-}
-
+// X c2r of u and w (fields 0..5) -> u x w -> X r2c (k_x_prod, xprod.cuh).
 template <typename T>
-static int launch_cross3_len(int L, int nrows, int Kx, const CPtrs& win, const Ptrs& wout,
-                             const typename Vec2<T>::type* tw, T scale, cudaStream_t st) {
-    switch (L) {
-        case 8:   return launch_cross3<T, 8>(nrows, Kx, win, wout, tw, scale, st);
-        case 16:  return launch_cross3<T, 16>(nrows, Kx, win, wout, tw, scale, st);
-        case 32:  return launch_cross3<T, 32>(nrows, Kx, win, wout, tw, scale, st);
-        case 64:  return launch_cross3<T, 64>(nrows, Kx, win, wout, tw, scale, st);
-        case 128: return launch_cross3<T, 128>(nrows, Kx, win, wout, tw, scale, st);
-        case 256: return launch_cross3<T, 256>(nrows, Kx, win, wout, tw, scale, st);
-        case 512: return launch_cross3<T, 512>(nrows, Kx, win, wout, tw, scale, st);
-        default: set_error("unsupported x length %d", L); return DD_ERR_UNSUPPORTED;
+struct ProdHydro3 {
+    static constexpr int NI = 6, NO = 3;
+    __device__ void operator()(const T* in, T* out, int) const {
+        const T ux = in[0], uy = in[1], uz = in[2], wx = in[3], wy = in[4], wz = in[5];
+        out[0] = uy * wz - uz * wy;
+        out[1] = uz * wx - ux * wz;
+        out[2] = ux * wy - uy * wx;
     }
-}
+};
 
 // ------------------------------------------------------------------ pass 5
 // Forward along z into the compact kept buffer NC[kyc][kzc][kx].
@@ -400,7 +309,8 @@ static int hydro3_nonlinear(const dd_plan* pl, const void* const* u, const Hydro
     OpYInv3<T> b{g, w1c, w2, TwSel<T>::y(pl)};
     DD_TRY((launch_pass_len<T, true, false, false>(g.Ny, b, g.Kx, g.Nz, 6, st)));
     // products overwrite fields 0..2 of W2 row by row (each block reads its rows first)
-    DD_TRY(launch_cross3_len<T>(g.Nx, g.Nz * g.Ny, g.Kx, w2c, w2, TwSel<T>::x(pl), (T)pl->inv_n, st));
+    DD_TRY((launch_x_prod_len<T>("x_cross", g.Nx, g.Nz * g.Ny, g.Kx, w2c, w2, 1, 0, 0, TwSel<T>::x(pl), (T)pl->inv_n,
+                                 ProdHydro3<T>{}, st)));
     OpYFwd3<T> d{g, w2c, w1, TwSel<T>::y(pl)};
     DD_TRY((launch_pass_len<T, false, false, false>(g.Ny, d, g.Kx, g.Nz, 3, st)));
     OpZFwdCompact3<T> e{g, w1c, nc, TwSel<T>::z(pl)};

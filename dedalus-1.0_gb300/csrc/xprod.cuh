@@ -1,0 +1,192 @@
+// Fused x-direction pass: NI half-spectrum fields -> c2r -> pointwise
+// nonlinear products in shared memory -> r2c of NO fields, for Q rows per block.
+//
+// Real rows are paired into complex pencils in row-major (row, field) order:
+// real row t = r*NI + f lives in pencil t/2, real part if t is even, imaginary
+// part if odd.  The forward side pairs its outputs the same way with NO.  The
+// inverse and forward transforms use their own schedules (SI, SF) so the
+// pencil slots of the block can be filled on both sides.
+//
+// Op provides: static NI, NO; __device__ void operator()(const T* in, T* out,
+// int run) on the NI grid values of one point, producing NO values.  Blocks
+// are (row block, run): run b's fields start at win.p[f] + b * in_rs and
+// wout.p[g] + b * out_rs (complex entries).
+#pragma once
+#include "fft_passes.cuh"
+
+namespace dd {
+
+template <int L, int NI, int NO>
+struct ProdCfg {
+    using SI = DefSched<L>;
+    using SF = DefSched<L>;
+    static constexpr int q_of(int n) { return ((2 * SI::P) / n) & ~1; }
+    static constexpr int Q = (q_of(NI) < q_of(NO) ? q_of(NI) : q_of(NO));
+    static constexpr int NT = SI::NT;
+};
+// Hydro (6 -> 3) and MHD (12 -> 6): forward pencils are half the inverse
+// ones, so SF doubles the threads per pencil and both sides are full.
+template <> struct ProdCfg<64, 6, 3> {
+    using SI = Sched<64, 24, 192, 8, 8, 1>;  using SF = Sched<64, 12, 192, 4, 4, 4>;
+    static constexpr int Q = 8, NT = 192;
+};
+template <> struct ProdCfg<128, 6, 3> {
+    using SI = Sched<128, 24, 192, 16, 8, 1>;  using SF = Sched<128, 12, 192, 8, 4, 4>;
+    static constexpr int Q = 8, NT = 192;
+};
+template <> struct ProdCfg<256, 6, 3> {
+    using SI = Sched<256, 12, 192, 16, 16, 1>;  using SF = Sched<256, 6, 192, 8, 8, 4>;
+    static constexpr int Q = 4, NT = 192;
+};
+template <> struct ProdCfg<512, 6, 3> {
+    using SI = Sched<512, 6, 192, 8, 8, 8>;  using SF = Sched<512, 3, 192, 8, 8, 8>;
+    static constexpr int Q = 2, NT = 192;
+};
+template <> struct ProdCfg<64, 12, 6> {
+    using SI = Sched<64, 24, 192, 8, 8, 1>;  using SF = Sched<64, 12, 192, 4, 4, 4>;
+    static constexpr int Q = 4, NT = 192;
+};
+template <> struct ProdCfg<128, 12, 6> {
+    using SI = Sched<128, 24, 192, 16, 8, 1>;  using SF = Sched<128, 12, 192, 8, 4, 4>;
+    static constexpr int Q = 4, NT = 192;
+};
+template <> struct ProdCfg<256, 12, 6> {
+    using SI = Sched<256, 12, 192, 16, 16, 1>;  using SF = Sched<256, 6, 192, 8, 8, 4>;
+    static constexpr int Q = 2, NT = 192;
+};
+template <> struct ProdCfg<512, 12, 6> {
+    using SI = Sched<512, 12, 384, 8, 8, 8>;  using SF = Sched<512, 6, 384, 8, 8, 8>;
+    static constexpr int Q = 2, NT = 384;
+};
+
+template <int L, int NI, int NO>
+constexpr size_t prod_smem(size_t csize) {
+    using CC = ProdCfg<L, NI, NO>;
+    const size_t a = (size_t)L * CC::SI::PS, b = (size_t)L * CC::SF::PS;
+    return csize * ((a > b ? a : b) + L);
+}
+
+template <typename T, int L, class Op>
+__global__ void __launch_bounds__(ProdCfg<L, Op::NI, Op::NO>::NT)
+k_x_prod(int nrows, int Kx, CPtrs win, Ptrs wout, int64_t in_rs, int64_t out_rs,
+         const typename Vec2<T>::type* gtw, T scale, const Op op) {
+    using V = typename Vec2<T>::type;
+    constexpr int NI = Op::NI, NO = Op::NO;
+    using CC = ProdCfg<L, NI, NO>;
+    using SI = typename CC::SI;
+    using SF = typename CC::SF;
+    extern __shared__ __align__(16) unsigned char dd_smem[];
+    constexpr int NT = CC::NT, Q = CC::Q;
+    constexpr int PSI = SI::PS, PSF = SF::PS;
+    constexpr int NPT = (L * Q + NT - 1) / NT;
+    static_assert(Q >= 2 && Q % 2 == 0, "need an even number of rows per block");
+    static_assert((NI * Q + 1) / 2 <= SI::P && (NO * Q + 1) / 2 <= SF::P, "schedule too small for Q rows");
+    static_assert(SI::NT == NT && SF::NT <= NT, "schedules must fit the block");
+    C<T>* tile = reinterpret_cast<C<T>*>(dd_smem);
+    constexpr size_t TA = (size_t)L * PSI, TB = (size_t)L * PSF;
+    C<T>* tw = tile + (TA > TB ? TA : TB);
+    load_twiddles<T, L>(tw, gtw);
+    const int row0 = blockIdx.x * Q;
+    const int nr = min(Q, nrows - row0);
+    const int64_t ib = blockIdx.y * in_rs, ob = blockIdx.y * out_rs;  // run (batch) offsets
+    constexpr int NPI = (NI * Q + 1) / 2;  // inverse pencils in use
+    for (int idx = threadIdx.x; idx < L * SI::P; idx += NT) {
+        const int e = idx % L, pj = idx / L;
+        C<T> z = zero<T>();
+        if (pj < NPI) {
+            const int ta = 2 * pj, tb = 2 * pj + 1;
+            const int ra = ta / NI, fa = ta % NI, rb = tb / NI, fb = tb % NI;
+            const bool va = ra < nr, vb = tb < NI * Q && rb < nr;
+            if (va || vb) {
+                const V* pa = (const V*)win.p[fa] + ib + (int64_t)(row0 + (va ? ra : rb)) * Kx;
+                const V* pb = (const V*)win.p[vb ? fb : fa] + ib + (int64_t)(row0 + (vb ? rb : ra)) * Kx;
+                z = pack_rows<T>(pa, pb, e, L, Kx);
+                if (!va) z.x = T(0);
+                if (!vb) z.y = T(0);
+            }
+        }
+        tile[e * PSI + pj] = z;
+    }
+    __syncthreads();
+    pencil_fft_s<T, SI, true>(tile, tw);
+    T outv[NPT][NO];
+#pragma unroll
+    for (int i = 0; i < NPT; i++) {
+        const int idx = threadIdx.x + i * NT;
+        if (idx < L * Q) {
+            const int e = idx % L, r = idx / L;
+            T in[NI];
+#pragma unroll
+            for (int f = 0; f < NI; f++) {
+                const int t = r * NI + f;
+                const C<T> c = tile[e * PSI + t / 2];
+                in[f] = (t & 1) ? c.y : c.x;
+            }
+            op(in, outv[i], blockIdx.y);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < NPT; i++) {
+        const int idx = threadIdx.x + i * NT;
+        if (idx < L * Q) {
+            const int e = idx % L, r = idx / L;
+#pragma unroll
+            for (int g = 0; g < NO; g++) {
+                const int t = r * NO + g;
+                if (t & 1) tile[e * PSF + t / 2].y = outv[i][g];
+                else tile[e * PSF + t / 2].x = outv[i][g];
+            }
+        }
+    }
+    if constexpr ((NO * Q) & 1) {  // the last pencil's imaginary half is unused
+        for (int e = threadIdx.x; e < L; e += NT) tile[e * PSF + (NO * Q) / 2].y = T(0);
+    }
+    __syncthreads();
+    pencil_fft_s<T, SF, false>(tile, tw, threadIdx.x < SF::NT);
+    for (int idx = threadIdx.x; idx < Kx * Q * NO; idx += NT) {
+        const int k = idx % Kx, t = idx / Kx;
+        const int r = t / NO, g = t % NO;
+        if (r >= nr) continue;
+        C<T> A, B;
+        unpack_rows<T>(tile + t / 2, PSF, k, L, scale, A, B);
+        stc<T>((V*)wout.p[g] + ob + (int64_t)(row0 + r) * Kx + k, (t & 1) ? B : A);
+    }
+}
+
+template <typename T, int L, class Op>
+int launch_x_prod(const char* name, int nrows, int Kx, const CPtrs& win, const Ptrs& wout, int nrun, int64_t in_rs,
+                  int64_t out_rs, const typename Vec2<T>::type* tw, T scale, const Op& op, cudaStream_t st) {
+    using CC = ProdCfg<L, Op::NI, Op::NO>;
+    const size_t smem = prod_smem<L, Op::NI, Op::NO>(sizeof(C<T>));
+    static bool configured = false;
+    if (!configured) {
+        DD_CUDA(cudaFuncSetAttribute(k_x_prod<T, L, Op>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        configured = true;
+    }
+    static const std::string label = std::string(name) + "_" + std::to_string(L) + (sizeof(T) == 8 ? "_f64" : "_f32");
+    DD_KT(label.c_str(), st,
+          k_x_prod<T, L, Op><<<dim3(cdiv(nrows, CC::Q), nrun), CC::NT, smem, st>>>(nrows, Kx, win, wout, in_rs, out_rs,
+                                                                                  tw, scale, op));
+    DD_LAUNCH_CHECK();
+    return DD_OK;
+}
+
+template <typename T, class Op>
+int launch_x_prod_len(const char* name, int L, int nrows, int Kx, const CPtrs& win, const Ptrs& wout, int nrun,
+                      int64_t in_rs, int64_t out_rs, const typename Vec2<T>::type* tw, T scale, const Op& op,
+                      cudaStream_t st) {
+    DD_CHECK_SUPPORTED(nrun >= 1 && nrun <= 65535, "run batch of %d not supported", nrun);
+    switch (L) {
+        case 8: return launch_x_prod<T, 8>(name, nrows, Kx, win, wout, nrun, in_rs, out_rs, tw, scale, op, st);
+        case 16: return launch_x_prod<T, 16>(name, nrows, Kx, win, wout, nrun, in_rs, out_rs, tw, scale, op, st);
+        case 32: return launch_x_prod<T, 32>(name, nrows, Kx, win, wout, nrun, in_rs, out_rs, tw, scale, op, st);
+        case 64: return launch_x_prod<T, 64>(name, nrows, Kx, win, wout, nrun, in_rs, out_rs, tw, scale, op, st);
+        case 128: return launch_x_prod<T, 128>(name, nrows, Kx, win, wout, nrun, in_rs, out_rs, tw, scale, op, st);
+        case 256: return launch_x_prod<T, 256>(name, nrows, Kx, win, wout, nrun, in_rs, out_rs, tw, scale, op, st);
+        case 512: return launch_x_prod<T, 512>(name, nrows, Kx, win, wout, nrun, in_rs, out_rs, tw, scale, op, st);
+        default: set_error("unsupported x length %d", L); return DD_ERR_UNSUPPORTED;
+    }
+}
+
+}  // namespace dd

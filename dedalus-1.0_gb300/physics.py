@@ -188,8 +188,68 @@ class IncompressibleHydro(Physics):
                   dptr(ws), ws.numel(), current_stream())
         self._mark_kspace(deriv)
 
+    # ------------------------------------------------------------ 2D
+    _phys2d = 0
+
+    def _state_names(self):
+        return [('u', 0), ('u', 1)]
+
+    def _params2d(self):
+        return None
+
     def _rhs2d(self, data, deriv, plan):
-        raise NotImplementedError("2D hydro RHS is not available yet")
+        prec = precision_code()
+        n = ctypes.c_size_t()
+        _lib.call("dd_rhs2d_workspace_size", plan.handle, 1, prec, ctypes.byref(n))
+        ws = self.workspace(n.value)
+        names = self._state_names()
+        sp, _a = _ptrs([data[f][c].kdata for f, c in names])
+        dp, _b = _ptrs([deriv[f][c].kdata for f, c in names])
+        pp = self._params2d()
+        ppa = None if pp is None else (ctypes.c_double * 4)(*pp)
+        ik2 = self.inv_k2_table(plan)
+        _lib.call("dd_rhs2d", plan.handle, self._phys2d, ppa, 1, sp, 0, dp, 0,
+                  None if ik2 is None else dptr(ik2), prec, 1, dptr(ws), ws.numel(), current_stream())
+        self._mark_kspace(deriv)
+
+    def _coeff_of(self, fname):
+        return dict(self._diffusivities())[fname]
+
+    def fused_rk2mid(self, data, dt, ti=None):
+        """One fused RK2mid step on the device (dd_rk2mid_step2d) for 2D
+        hydro / Boussinesq; returns False when there is no fused step."""
+        if self.ndim != 2 or type(self) not in (IncompressibleHydro, BoussinesqHydro):
+            return False
+        if not self._is_finalized:
+            self._finalize()
+        names = self._state_names()
+        for f, c in names:
+            data[f][c].require_space('kspace')
+        plan = self.plan(data)
+        prec = precision_code()
+        vo = int(self.parameters['viscosity_order'])
+        coeffs = [float(self._coeff_of(f)) for f, c in names]
+        n = ctypes.c_size_t()
+        _lib.call("dd_rhs2d_workspace_size", plan.handle, 1, prec, ctypes.byref(n))
+        ws = self.workspace(n.value)
+        ik2 = self.inv_k2_table(plan)
+        th = tf = None
+        keep = []
+        if ik2 is not None:
+            tabs_h = [self.phi_table(plan, cf, vo, dt / 2.) for cf in coeffs]
+            tabs_f = [self.phi_table(plan, cf, vo, dt) for cf in coeffs]
+            keep = tabs_h + tabs_f
+            th, _h = _ptrs(tabs_h)
+            tf, _f = _ptrs(tabs_f)
+            keep += [_h, _f]
+        sp, _a = _ptrs([data[f][c].kdata for f, c in names])
+        pp = self._params2d()
+        ppa = None if pp is None else (ctypes.c_double * 4)(*pp)
+        nus = (ctypes.c_double * 3)(*(coeffs + [0.] * (3 - len(coeffs))))
+        _lib.call("dd_rk2mid_step2d", plan.handle, self._phys2d, ppa, 1, sp, 0,
+                  None if ik2 is None else dptr(ik2), th, tf, nus, vo, float(dt), prec,
+                  dptr(ws), ws.numel(), current_stream())
+        return True
 
     def fused_rk4(self, data, dt):
         """One fused RK4 step on the device (dd_hydro3d_rk4_step); returns
@@ -244,8 +304,29 @@ class BoussinesqHydro(IncompressibleHydro):
     def set_thermal_forcing(self, func):
         self.forcing_functions['ThermalForcing'] = func
 
+    _phys2d = 1
+
+    def _state_names(self):
+        return [('u', 0), ('u', 1), ('T', 0)]
+
+    def _direction_index(self):
+        d = self.parameters['boussinesq_direction']
+        ctrans = {'x': 0, 'y': 1} if self.ndim == 2 else {'x': 0, 'y': 1, 'z': 2}
+        if d not in ctrans:
+            raise KeyError(d)   # as data['u'][d] does for a 2D VectorField (fields.py:148-151)
+        return ctrans[d]
+
+    def _params2d(self):
+        return [float(self.parameters['g']), float(self.parameters['alpha_t']), float(self.parameters['beta']),
+                float(self._direction_index())]
+
     def RHS(self, data, deriv):
-        raise NotImplementedError("Boussinesq RHS is not available yet")
+        """physics.py:664-712, fused on the GPU (2D)."""
+        if self.ndim != 2:
+            raise NotImplementedError("3D Boussinesq is not in the CUDA path")
+        self._direction_index()
+        self._begin_rhs(data, deriv)
+        self._rhs2d(data, deriv, self.plan(data))
 
     def set_dtlist(self, data):
         IncompressibleHydro.set_dtlist(self, data)

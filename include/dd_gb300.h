@@ -162,6 +162,28 @@ int dd_hydro3d_rk4_step(const dd_plan* plan, void* const* u, const double* inv_k
                         const void* tab_full, double nu, int viscosity_order, double dt, int precision,
                         int* nonkept_flag, void* work, size_t work_bytes, void* stream);
 
+/* ------------------------------------------------------ fused 2D physics
+ * physics 0 = IncompressibleHydro (physics.py:527-599), state (u_x, u_y);
+ * physics 1 = BoussinesqHydro (physics.py:664-712), state (u_x, u_y, T) with
+ * params = {g, alpha_t, beta, direction} (direction 0 = x, 1 = y; the
+ * reference's default 'z' has no 2D component, physics.py:646, fields.py:148).
+ * Shear, rotation, tracer and forcing are not implemented.  A call covers
+ * nrun independent runs of the plan's grid: run b's field c is at
+ * state[c] + b * state_rs complex entries (state_rs = 0 and nrun = 1 for one
+ * run).  dd_rhs2d writes the dealiased RHS into deriv (zero_nonkept != 0 also
+ * zeroes the non-kept entries); dd_rk2mid_step2d advances the state in place
+ * by one RK2mid step (time_step.py:275-309; euler/etd1/etd2rk2 with the 2D
+ * Taylor branch), tab_half[c] / tab_full[c] being dd_phi_table(2, nu[c], vo, dt/2 or dt)
+ * tables per state field when inv_k2 is given. */
+int dd_rhs2d_workspace_size(const dd_plan* plan, int nrun, int precision, size_t* bytes);
+int dd_rhs2d(const dd_plan* plan, int physics, const double* params, int nrun, const void* const* state,
+             int64_t state_rs, void* const* deriv, int64_t deriv_rs, const double* inv_k2, int precision,
+             int zero_nonkept, void* work, size_t work_bytes, void* stream);
+int dd_rk2mid_step2d(const dd_plan* plan, int physics, const double* params, int nrun, void* const* state,
+                     int64_t state_rs, const double* inv_k2, const void* const* tab_half,
+                     const void* const* tab_full, const double* nu, int viscosity_order, double dt,
+                     int precision, void* work, size_t work_bytes, void* stream);
+
 /* Sets *dflag (device int) to 1 if any of the ncomp k arrays has a non-zero
  * entry outside the kept (dealiased) modes; does not clear it. */
 int dd_any_nonkept(const dd_plan* plan, int ncomp, const void* const* k, int* dflag, void* stream);

@@ -1,0 +1,127 @@
+"""2D parity against the oracle: incompressible hydro (the 128^2, nu = 1e-3,
+RK2mid, dt = 1e-3 configuration, including its full 100 steps) and
+Boussinesq (direction 'y', N^2 = g alpha beta = 1, nu = kappa = 2e-3).
+Tolerance: relative L2 over all fields <= 1e-12 (per step)."""
+import numpy as np
+import pytest
+
+from oracle import physics as OP, time_step as OT
+from oracle.representation import FourierRepresentation as OracleRep
+
+
+def rel_l2(got, ref):
+    num = sum(np.sum(np.abs(g - r) ** 2) for g, r in zip(got, ref))
+    den = sum(np.sum(np.abs(r) ** 2) for r in ref)
+    return float(np.sqrt(num / den))
+
+
+def setup(dd, cls_name, shape, params, fields):
+    M = dd.mods
+    ro = getattr(OP, cls_name)(shape, OracleRep)
+    rg = getattr(M, cls_name)(shape, M.FourierRepresentation)
+    for r in (ro, rg):
+        r.parameters.update(params)
+    do, dg = ro.create_fields(0.), rg.create_fields(0.)
+    for (name, i), arr in fields.items():
+        do[name][i]['kspace'] = arr.copy()
+        dg[name][i]['kspace'] = arr
+    return ro, do, rg, dg
+
+
+def state(data, names, gpu):
+    return [data[f][c].to_numpy('kspace') if gpu else data[f][c]['kspace'] for f, c in names]
+
+
+HYD = [('u', 0), ('u', 1)]
+BOU = [('u', 0), ('u', 1), ('T', 0)]
+
+
+def hydro_fields(dd, shape, seed):
+    u = dd.init_cond.turbulence_2d(shape, seed=seed)
+    return {('u', 0): u[0], ('u', 1): u[1]}
+
+
+def bouss_fields(dd, shape, seed, with_u=True):
+    T = dd.init_cond.band_limited_noise_2d(shape, seed=seed)
+    u = dd.init_cond.turbulence_2d(shape, seed=seed + 1, energy_target=1e-2)
+    if not with_u:
+        u = [np.zeros_like(T), np.zeros_like(T)]
+    return {('u', 0): u[0], ('u', 1): u[1], ('T', 0): T}
+
+
+BPAR = {'nu': 2e-3, 'kappa': 2e-3, 'g': 1., 'alpha_t': 1., 'beta': 1., 'boussinesq_direction': 'y'}
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape", [(32, 32), (128, 128), (64, 256), (512, 512)])
+def test_hydro2d_rhs(dd, cuda, shape):
+    ro, do, rg, dg = setup(dd, 'IncompressibleHydro', shape, {'nu': 1e-3}, hydro_fields(dd, shape, 1))
+    eo, eg = ro.create_fields(0.), rg.create_fields(0.)
+    ro.RHS(do, eo)
+    rg.RHS(dg, eg)
+    assert rel_l2(state(eg, HYD, True), state(eo, HYD, False)) < 1e-12
+
+
+@pytest.mark.gpu
+def test_hydro2d_config1_100_steps(dd, cuda):
+    shape = (128, 128)
+    ro, do, rg, dg = setup(dd, 'IncompressibleHydro', shape, {'nu': 1e-3}, hydro_fields(dd, shape, 0))
+    to, tg = OT.RK2mid(ro), dd.mods.RK2mid(rg)
+    worst = 0.
+    for step in range(100):
+        to.do_advance(do, 1e-3)
+        tg.do_advance(dg, 1e-3)
+        if step % 10 == 9 or step < 3:
+            worst = max(worst, rel_l2(state(dg, HYD, True), state(do, HYD, False)))
+    assert worst < 1e-12, worst
+    assert tg.iteration == 100 and abs(dg.time - 0.1) < 1e-12
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape", [(64, 64), (128, 128), (256, 256)])
+@pytest.mark.parametrize("with_u", [False, True])
+def test_boussinesq2d_rhs(dd, cuda, shape, with_u):
+    ro, do, rg, dg = setup(dd, 'BoussinesqHydro', shape, BPAR, bouss_fields(dd, shape, 2, with_u))
+    eo, eg = ro.create_fields(0.), rg.create_fields(0.)
+    ro.RHS(do, eo)
+    rg.RHS(dg, eg)
+    assert rel_l2(state(eg, BOU, True), state(eo, BOU, False)) < 1e-12
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape", [(64, 64), (256, 256)])
+def test_boussinesq2d_rk2mid_steps(dd, cuda, shape):
+    ro, do, rg, dg = setup(dd, 'BoussinesqHydro', shape, BPAR, bouss_fields(dd, shape, 3))
+    to, tg = OT.RK2mid(ro), dd.mods.RK2mid(rg)
+    for step in range(5):
+        to.do_advance(do, 1e-2)
+        tg.do_advance(dg, 1e-2)
+        assert rel_l2(state(dg, BOU, True), state(do, BOU, False)) < 1e-12
+
+
+@pytest.mark.gpu
+def test_boussinesq2d_generic_rk2mid_and_rk4(dd, cuda):
+    shape = (64, 64)
+    ro, do, rg, dg = setup(dd, 'BoussinesqHydro', shape, BPAR, bouss_fields(dd, shape, 4))
+    to, tg = OT.RK2mid(ro), dd.mods.RK2mid(rg)
+    tg.use_fused = False
+    for _ in range(3):
+        to.do_advance(do, 1e-2)
+        tg.do_advance(dg, 1e-2)
+    assert rel_l2(state(dg, BOU, True), state(do, BOU, False)) < 1e-12
+    ro, do, rg, dg = setup(dd, 'BoussinesqHydro', shape, BPAR, bouss_fields(dd, shape, 5))
+    OT.RK4(ro).do_advance(do, 1e-2)
+    dd.mods.RK4(rg).do_advance(dg, 1e-2)
+    assert rel_l2(state(dg, BOU, True), state(do, BOU, False)) < 1e-12
+
+
+@pytest.mark.gpu
+def test_boussinesq2d_default_direction_raises_keyerror(dd, cuda):
+    """The reference's default direction 'z' has no 2D velocity component."""
+    shape = (32, 32)
+    M = dd.mods
+    rg = M.BoussinesqHydro(shape, M.FourierRepresentation)
+    rg.parameters['boussinesq_direction'] = 'z'
+    dg = rg.create_fields(0.)
+    with pytest.raises(KeyError):
+        rg.RHS(dg, rg.create_fields(0.))
