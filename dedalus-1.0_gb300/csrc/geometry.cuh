@@ -37,12 +37,13 @@ __host__ __device__ __forceinline__ bool kept_full(int i, int N, int M) { return
 __host__ __device__ __forceinline__ int full_to_compact(int i, int N, int K) { return i <= (K - 1) / 2 ? i : i - (N - K); }
 __host__ __device__ __forceinline__ int compact_to_full(int c, int N, int K) { return c <= (K - 1) / 2 ? c : c + (N - K); }
 
-// Up to 8 field pointers passed by value.
+// Field pointers passed by value to kernels (MHD uses 12 transform fields).
+#define DD_MAXF 16
 struct Ptrs {
-    void* p[8];
+    void* p[DD_MAXF];
 };
 struct CPtrs {
-    const void* p[8];
+    const void* p[DD_MAXF];
 };
 
 }  // namespace dd

@@ -28,6 +28,7 @@ enum { PHYS_HYDRO = 0, PHYS_BOUSS = 1 };
 template <int PHYS> struct Phys2;
 template <> struct Phys2<PHYS_HYDRO> { static constexpr int NF = 2, NI = 3, NO = 2; };
 template <> struct Phys2<PHYS_BOUSS> { static constexpr int NF = 3, NI = 5, NO = 3; };
+static_assert(Phys2<PHYS_BOUSS>::NI <= DD_MAXF, "too many transform fields for Ptrs");
 
 // ------------------------------------------------------------------ pass 1
 template <typename T, bool COMPACT, int PHYS>
@@ -239,13 +240,14 @@ struct Work2 {
     int nrun;
     char* base;
     template <typename T> C<T>* W(int f) const { return (C<T>*)base + (size_t)f * nrun * w; }
+    static size_t up256(size_t b) { return (b + 255) & ~(size_t)255; }
     template <typename T> double2* NC(int f) const {
-        return (double2*)((char*)base + sizeof(C<T>) * 5 * nrun * w) + (size_t)f * nrun * kc;
+        return (double2*)((char*)base + up256(sizeof(C<T>) * 5 * nrun * w)) + (size_t)f * nrun * kc;
     }
     template <typename T> double2* K1(int f) const { return NC<T>(3) + (size_t)f * nrun * kc; }
     template <typename T> double2* YS(int f) const { return NC<T>(6) + (size_t)f * nrun * kc; }
     template <typename T> static size_t bytes(const Geo2& g, int nrun) {
-        return sizeof(C<T>) * 5 * (size_t)nrun * g.wcount() + sizeof(double2) * 9 * (size_t)nrun * g.Kx * g.Ky;
+        return up256(sizeof(C<T>) * 5 * (size_t)nrun * g.wcount()) + sizeof(double2) * 9 * (size_t)nrun * g.Kx * g.Ky;
     }
 };
 

@@ -1,59 +1,69 @@
-// Fused 3D incompressible-hydro right-hand side and RK4 step.
+// Fused 3D right-hand sides and RK4 step for incompressible hydro and MHD.
 //
-// RHS(u) = P[u x w]^ (2/3 dealiased), w = curl u: the rotational form of the
-// reference's P[-(u.grad)u]^ (physics.py:527-599).  The two agree on the kept
-// modes to roundoff: their difference is a gradient, which the projection
+//   hydro: RHS(u) = P[u x w]^, w = curl u                  (physics.py:527-599)
+//   MHD:   RHS(u) = P[u x w + (J x B) / (4 pi rho0)]^, J = curl B,
+//          RHS(B) = curl (u x B)^                            (physics.py:770-819)
+// The rotational form u x w equals the reference's -(u.grad)u on the kept
+// modes to roundoff: the difference is a gradient, which the projection
 // removes, and products of dealiased fields alias only onto non-kept modes.
+// The Lorentz term is added in x-space before the forward transform (one
+// transform per component instead of two; equal by linearity).
 //
-// Passes (all pruned to the kept modes, FP64 or FP32 arithmetic T):
-//   1  Z^-1 of u and w = i k x u (curl formed while loading)      6 fields
-//   2  Y^-1                                                         6 fields
-//   3  X c2r of (ux,uy),(uz,wx),(wy,wz) packed rows -> u x w in
-//      shared memory -> X r2c of the 3 products, scaled by 1/N      3 fields
-//   4  Y forward, kept ky only                                      3 fields
+// Passes (all pruned to the kept modes; T = FP64 or FP32 arithmetic):
+//   1  Z^-1 of each vector field and its curl (formed while loading)
+//   2  Y^-1
+//   3  X c2r -> pointwise products -> X r2c, scaled by 1/N   (k_x_prod)
+//   4  Y forward, kept ky only
 //   5  Z forward, kept kz only, into a compact [kyc][kzc][kx] buffer
-//   6  solenoidal projection (physics.py:588-599, laplace_solve
-//      407-416) fused with the RK stage update (etd1 with phi tables).
+//   6  projection (physics.py:588-599, laplace_solve 407-416) and, for B,
+//      the spectral curl (physics.py:394-396), fused with the RK4 stage.
 #include "launch_len.cuh"
 #include "xprod.cuh"
 #include "etd.cuh"
 
 namespace dd {
 
-// ------------------------------------------------------------------ pass 1
-// Fields 0..2 = u_x,u_y,u_z ; 3..5 = w_x,w_y,w_z (physics.py:394-396 curlX).
-// The state is read either from the full reference layout [ky][kz][kx] or
-// from the compact kept layout [kyc][kzc][kx] used for RK stage states.
-__device__ __forceinline__ double2 ideriv(double2 a, double k) {
-    // a * (1j * k) as numpy computes it (representations.py:423)
-    return make_double2(-(a.y * k), a.x * k);
-}
+enum { P3_HYDRO = 0, P3_MHD = 1 };
+template <int PH> struct Phys3;
+template <> struct Phys3<P3_HYDRO> { static constexpr int NG = 1, NF = 3, NI = 6, NO = 3; };
+template <> struct Phys3<P3_MHD>   { static constexpr int NG = 2, NF = 6, NI = 12, NO = 6; };
+static_assert(Phys3<P3_MHD>::NI <= DD_MAXF, "too many transform fields for Ptrs");
 
-template <typename T, bool COMPACT>
+// a * (1j * k) as numpy computes it (representations.py:423)
+__device__ __forceinline__ double2 ideriv(double2 a, double k) { return make_double2(-(a.y * k), a.x * k); }
+
+// ------------------------------------------------------------------ pass 1
+// Field f: group g = f / 6 (vector field g of the state), j = f % 6:
+// j < 3 -> component j; j >= 3 -> component j - 3 of its curl (curlX,
+// physics.py:394-396: (d_y X_z - d_z X_y, d_z X_x - d_x X_z, d_x X_y - d_y X_x)).
+// The state is read from the full reference layout [ky][kz][kx] or from the
+// compact kept layout [kyc][kzc][kx] used for RK stage states.
+template <typename T, bool COMPACT, int NG>
 struct OpZInvCurl3 {
     using V = typename Vec2<T>::type;
-    static constexpr const char* name = "z_inv_curl";
+    static constexpr const char* name = NG == 1 ? "z_inv_curl" : "z_inv_curl_mhd";
     Geo3 g; CPtrs u; Ptrs out; const V* tw;
     const double* kx; const double* ky; const double* kz;
     __device__ int npencil() const { return g.Kx; }
     __device__ int nstore() const { return g.Nz; }
-    __device__ double2 get(int c, int kyc, int ky, int e, int ix) const {
+    __device__ double2 get(int c, int kyc, int ky_i, int e, int ix) const {
         const double2* U = (const double2*)u.p[c];
         if (COMPACT) return U[((int64_t)kyc * g.Kz + full_to_compact(e, g.Nz, g.Kz)) * g.Kx + ix];
-        return U[((int64_t)ky * g.Nz + e) * g.Nh + ix];
+        return U[((int64_t)ky_i * g.Nz + e) * g.Nh + ix];
     }
     __device__ C<T> load(int fld, int kyc, int e, int ix) const {
         if (!kept_full(e, g.Nz, g.Mz)) return zero<T>();
         const int ky_i = compact_to_full(kyc, g.Ny, g.Ky);
+        const int grp = fld / 6, j = fld % 6, c0 = 3 * grp;
         double2 r;
-        if (fld < 3) {
-            r = get(fld, kyc, ky_i, e, ix);
+        if (j < 3) {
+            r = get(c0 + j, kyc, ky_i, e, ix);
         } else {
             const double kxv = kx[ix], kyv = ky[ky_i], kzv = kz[e];
             double2 a, b;
-            if (fld == 3) { a = ideriv(get(2, kyc, ky_i, e, ix), kyv); b = ideriv(get(1, kyc, ky_i, e, ix), kzv); }
-            else if (fld == 4) { a = ideriv(get(0, kyc, ky_i, e, ix), kzv); b = ideriv(get(2, kyc, ky_i, e, ix), kxv); }
-            else { a = ideriv(get(1, kyc, ky_i, e, ix), kxv); b = ideriv(get(0, kyc, ky_i, e, ix), kyv); }
+            if (j == 3) { a = ideriv(get(c0 + 2, kyc, ky_i, e, ix), kyv); b = ideriv(get(c0 + 1, kyc, ky_i, e, ix), kzv); }
+            else if (j == 4) { a = ideriv(get(c0 + 0, kyc, ky_i, e, ix), kzv); b = ideriv(get(c0 + 2, kyc, ky_i, e, ix), kxv); }
+            else { a = ideriv(get(c0 + 1, kyc, ky_i, e, ix), kxv); b = ideriv(get(c0 + 0, kyc, ky_i, e, ix), kyv); }
             r = make_double2(a.x - b.x, a.y - b.y);
         }
         return mk<T>((T)r.x, (T)r.y);
@@ -64,7 +74,6 @@ struct OpZInvCurl3 {
 };
 
 // ------------------------------------------------------------------ pass 3
-// X c2r of u and w (fields 0..5) -> u x w -> X r2c (k_x_prod, xprod.cuh).
 template <typename T>
 struct ProdHydro3 {
     static constexpr int NI = 6, NO = 3;
@@ -76,8 +85,24 @@ struct ProdHydro3 {
     }
 };
 
+// in: u, w, B, J;  out: u x w + (J x B) / (4 pi rho0), u x B  (physics.py:795-815)
+template <typename T>
+struct ProdMHD3 {
+    static constexpr int NI = 12, NO = 6;
+    T inv_fpr;
+    __device__ void operator()(const T* in, T* out, int) const {
+        const T ux = in[0], uy = in[1], uz = in[2], wx = in[3], wy = in[4], wz = in[5];
+        const T bx = in[6], by = in[7], bz = in[8], jx = in[9], jy = in[10], jz = in[11];
+        out[0] = (uy * wz - uz * wy) + (jy * bz - jz * by) * inv_fpr;
+        out[1] = (uz * wx - ux * wz) + (jz * bx - jx * bz) * inv_fpr;
+        out[2] = (ux * wy - uy * wx) + (jx * by - jy * bx) * inv_fpr;
+        out[3] = uy * bz - uz * by;
+        out[4] = uz * bx - ux * bz;
+        out[5] = ux * by - uy * bx;
+    }
+};
+
 // ------------------------------------------------------------------ pass 5
-// Forward along z into the compact kept buffer NC[kyc][kzc][kx].
 template <typename T>
 struct OpZFwdCompact3 {
     using V = typename Vec2<T>::type;
@@ -111,30 +136,51 @@ __device__ __forceinline__ void kept_index(const Geo3& g, int64_t i, int& kyc, i
     kyc = (int)(r / g.Kz);
 }
 
-// Solenoidal projection with the reference's operation order:
-// div = ((i kx Nx) + i ky Ny) + i kz Nz; phi = -(div * (1/k2)); N_i -= i k_i phi.
+// div = ((i kx Nx) + i ky Ny) + i kz Nz; phi = -(div * (1/k2)); N_i -= i k_i phi
 __device__ __forceinline__ void project(double2& nx, double2& ny, double2& nz, double kxv, double kyv,
                                         double kzv, double s) {
-    double2 dx = ideriv(nx, kxv), dy = ideriv(ny, kyv), dz = ideriv(nz, kzv);
-    double2 dv = make_double2(radd(radd(dx.x, dy.x), dz.x), radd(radd(dx.y, dy.y), dz.y));
-    double2 ph = make_double2(-rmul(dv.x, s), -rmul(dv.y, s));
-    double2 gx = ideriv(ph, kxv), gy = ideriv(ph, kyv), gz = ideriv(ph, kzv);
+    const double2 dx = ideriv(nx, kxv), dy = ideriv(ny, kyv), dz = ideriv(nz, kzv);
+    const double2 dv = make_double2(radd(radd(dx.x, dy.x), dz.x), radd(radd(dx.y, dy.y), dz.y));
+    const double2 ph = make_double2(-rmul(dv.x, s), -rmul(dv.y, s));
+    const double2 gx = ideriv(ph, kxv), gy = ideriv(ph, kyv), gz = ideriv(ph, kzv);
     nx = make_double2(rsub(nx.x, gx.x), rsub(nx.y, gx.y));
     ny = make_double2(rsub(ny.x, gy.x), rsub(ny.y, gy.y));
     nz = make_double2(rsub(nz.x, gz.x), rsub(nz.y, gz.y));
 }
 
-__device__ __forceinline__ double inv_k2_of(const ProjArgs& a, int ix, int ky_i, int kz_i, int& q) {
-    const double kxv = a.kx[ix], kyv = a.ky[ky_i], kzv = a.kz[kz_i];
-    // k2 = ((0 + ky^2) + kz^2) + kx^2 (representations.py:434-436, k dict order y, z, x)
-    double k2 = radd(radd(rmul(kyv, kyv), rmul(kzv, kzv)), rmul(kxv, kxv));
-    q = a.intk ? (int)k2 : 0;
-    if (a.intk && a.inv_k2) return a.inv_k2[q];
-    if (k2 == 0.) k2 = 1.;
-    return rdiv(1., k2);
+// curlX of a k-space vector (physics.py:394-396), in place.
+__device__ __forceinline__ void curl_k(double2& vx, double2& vy, double2& vz, double kxv, double kyv, double kzv) {
+    const double2 a0 = ideriv(vz, kyv), b0 = ideriv(vy, kzv);
+    const double2 a1 = ideriv(vx, kzv), b1 = ideriv(vz, kxv);
+    const double2 a2 = ideriv(vy, kxv), b2 = ideriv(vx, kyv);
+    vx = make_double2(a0.x - b0.x, a0.y - b0.y);
+    vy = make_double2(a1.x - b1.x, a1.y - b1.y);
+    vz = make_double2(a2.x - b2.x, a2.y - b2.y);
 }
 
-// Projection only, into the full-layout derivative arrays (kept entries).
+__device__ __forceinline__ double k2_of(const ProjArgs& a, int ix, int ky_i, int kz_i) {
+    const double kxv = a.kx[ix], kyv = a.ky[ky_i], kzv = a.kz[kz_i];
+    // ((0 + ky^2) + kz^2) + kx^2 (representations.py:434-436, k dict order y, z, x)
+    return radd(radd(rmul(kyv, kyv), rmul(kzv, kzv)), rmul(kxv, kxv));
+}
+
+__device__ __forceinline__ double inv_k2_of(const ProjArgs& a, double k2, int& q) {
+    q = a.intk ? (int)k2 : 0;
+    if (a.intk && a.inv_k2) return a.inv_k2[q];
+    return rdiv(1., k2 == 0. ? 1. : k2);
+}
+
+// RHS of every state component at one kept entry from the compact products.
+template <int PH>
+__device__ __forceinline__ void rhs_at(const CPtrs& nc, int64_t i, double kxv, double kyv, double kzv, double s,
+                                       double2* k) {
+#pragma unroll
+    for (int c = 0; c < Phys3<PH>::NO; c++) k[c] = ((const double2*)nc.p[c])[i];
+    project(k[0], k[1], k[2], kxv, kyv, kzv, s);
+    if constexpr (PH == P3_MHD) curl_k(k[3], k[4], k[5], kxv, kyv, kzv);
+}
+
+template <int PH>
 __global__ void k_project_to_deriv3(ProjArgs a, CPtrs nc, Ptrs deriv) {
     const Geo3& g = a.g;
     const int64_t n = (int64_t)g.Ky * g.Kz * g.Kx;
@@ -142,18 +188,16 @@ __global__ void k_project_to_deriv3(ProjArgs a, CPtrs nc, Ptrs deriv) {
         int kyc, kzc, ix, q;
         kept_index(g, i, kyc, kzc, ix);
         const int ky_i = compact_to_full(kyc, g.Ny, g.Ky), kz_i = compact_to_full(kzc, g.Nz, g.Kz);
-        const double s = inv_k2_of(a, ix, ky_i, kz_i, q);
-        double2 nx = ((const double2*)nc.p[0])[i], ny = ((const double2*)nc.p[1])[i], nz = ((const double2*)nc.p[2])[i];
-        project(nx, ny, nz, a.kx[ix], a.ky[ky_i], a.kz[kz_i], s);
+        const double s = inv_k2_of(a, k2_of(a, ix, ky_i, kz_i), q);
+        double2 k[6];
+        rhs_at<PH>(nc, i, a.kx[ix], a.ky[ky_i], a.kz[kz_i], s, k);
         const int64_t o = ((int64_t)ky_i * g.Nz + kz_i) * g.Nh + ix;
-        ((double2*)deriv.p[0])[o] = nx;
-        ((double2*)deriv.p[1])[o] = ny;
-        ((double2*)deriv.p[2])[o] = nz;
+#pragma unroll
+        for (int c = 0; c < Phys3<PH>::NF; c++) ((double2*)deriv.p[c])[o] = k[c];
     }
 }
 
-// One RK4 stage (time_step.py:426-483 as restated by the project; see the
-// oracle): k = P[N];
+// One RK4 stage (time_step.py:426-483 as restated; see the oracle):
 //   stage 1: tot = k*(1/6);  y1 = etd1(y, k, dt/2)
 //   stage 2: tot += k*(1/3); y2 = etd1(y, k, dt/2)
 //   stage 3: tot += k*(1/3); y3 = etd1(y, k, dt)
@@ -161,48 +205,51 @@ __global__ void k_project_to_deriv3(ProjArgs a, CPtrs nc, Ptrs deriv) {
 // y (state) is full layout; stage states and tot are compact.
 struct RK4Args {
     ProjArgs pa;
-    CPtrs nc;          // unprojected RHS, compact
-    Ptrs y;            // state, full layout (read; written at stage 4)
-    Ptrs ys;           // next stage state, compact (stages 1-3)
-    Ptrs tot;          // accumulated increment, compact
-    const double4* tab;  // phi table for this stage's step (q-indexed), or null
-    double h;            // this stage's step (dt/2 or dt)
-    double nu; int vo;   // used when tab is null (non-integer wavenumbers)
+    CPtrs nc;            // unprojected products, compact
+    Ptrs y;              // state, full layout (written at stage 4)
+    Ptrs ys;             // next stage state, compact (stages 1-3)
+    Ptrs tot;            // accumulated increment, compact
+    const double4* tab[2];  // phi table per vector group for this stage's step, or null
+    double coeff[2];     // diffusivity per group (nu, eta), used when tab is null
+    double h; int vo;
     double w;            // increment weight: 1/6 or 1/3
     int stage;
 };
 
-template <int NDIM>
-__device__ __forceinline__ void phis_for(const RK4Args& a, int q, double k2, double& Z, double& f0, double& f1) {
-    if (a.tab) {
-        const double4 t = a.tab[q];
+__device__ __forceinline__ void phis_for(const RK4Args& a, int grp, int q, double k2, double& Z, double& f0,
+                                         double& f1) {
+    if (a.tab[grp]) {
+        const double4 t = a.tab[grp][q];
         Z = t.x; f0 = t.y; f1 = t.z;
     } else {
         const double k2v = a.vo == 1 ? k2 : (a.vo == 2 ? rmul(k2, k2) : pow(k2, (double)a.vo));
-        Z = rmul(-rmul(a.nu, k2v), a.h);
+        Z = rmul(-rmul(a.coeff[grp], k2v), a.h);
         double f2;
         f0 = 1.; f1 = 1.;
-        if (Z != 0.) etd_phis<NDIM>(Z, f0, f1, f2);
+        if (Z != 0.) etd_phis<3>(Z, f0, f1, f2);
     }
 }
 
+template <int PH>
 __global__ void k_rk4_stage3(RK4Args a) {
     const Geo3& g = a.pa.g;
+    constexpr int NF = Phys3<PH>::NF, NG = Phys3<PH>::NG;
     const int64_t n = (int64_t)g.Ky * g.Kz * g.Kx;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         int kyc, kzc, ix, q;
         kept_index(g, i, kyc, kzc, ix);
         const int ky_i = compact_to_full(kyc, g.Ny, g.Ky), kz_i = compact_to_full(kzc, g.Nz, g.Kz);
-        const double kxv = a.pa.kx[ix], kyv = a.pa.ky[ky_i], kzv = a.pa.kz[kz_i];
-        const double s = inv_k2_of(a.pa, ix, ky_i, kz_i, q);
-        double2 k[3] = {((const double2*)a.nc.p[0])[i], ((const double2*)a.nc.p[1])[i], ((const double2*)a.nc.p[2])[i]};
-        project(k[0], k[1], k[2], kxv, kyv, kzv, s);
-        const double k2 = radd(radd(rmul(kyv, kyv), rmul(kzv, kzv)), rmul(kxv, kxv));
-        double Z, f0, f1;
-        phis_for<3>(a, q, k2, Z, f0, f1);
+        const double k2 = k2_of(a.pa, ix, ky_i, kz_i);
+        const double s = inv_k2_of(a.pa, k2, q);
+        double2 k[6];
+        rhs_at<PH>(a.nc, i, a.pa.kx[ix], a.pa.ky[ky_i], a.pa.kz[kz_i], s, k);
+        double Z[NG], f0[NG], f1[NG];
+#pragma unroll
+        for (int grp = 0; grp < NG; grp++) phis_for(a, grp, q, k2, Z[grp], f0[grp], f1[grp]);
         const int64_t o = ((int64_t)ky_i * g.Nz + kz_i) * g.Nh + ix;
 #pragma unroll
-        for (int c = 0; c < 3; c++) {
+        for (int c = 0; c < NF; c++) {
+            const int grp = c / 3;
             const double2 kw = make_double2(rmul(k[c].x, a.w), rmul(k[c].y, a.w));
             double2 t;
             if (a.stage == 1) t = kw;
@@ -210,20 +257,22 @@ __global__ void k_rk4_stage3(RK4Args a) {
             const double2 y0 = ((const double2*)a.y.p[c])[o];
             if (a.stage < 4) {
                 ((double2*)a.tot.p[c])[i] = t;
-                ((double2*)a.ys.p[c])[i] = etd1_entry(y0, k[c], Z, f0, f1, a.h);
+                ((double2*)a.ys.p[c])[i] = etd1_entry(y0, k[c], Z[grp], f0[grp], f1[grp], a.h);
             } else {
-                ((double2*)a.y.p[c])[o] = etd1_entry(y0, t, Z, f0, f1, a.h);
+                ((double2*)a.y.p[c])[o] = etd1_entry(y0, t, Z[grp], f0[grp], f1[grp], a.h);
             }
         }
     }
 }
 
 // Non-kept modes of the state see no nonlinear forcing: y <- etd1(y, 0, dt).
-__global__ void k_decay_nonkept3(Geo3 g, Ptrs y, const double* kx, const double* ky, const double* kz,
-                                 const double4* tab, double nu, int vo, double dt) {
+__global__ void k_decay_nonkept3(RK4Args a, int ncomp) {
+    const Geo3& g = a.pa.g;
     const int64_t n = g.kcount();
     const int c = blockIdx.y;
-    double2* Y = (double2*)y.p[c];
+    if (c >= ncomp) return;
+    const int grp = c / 3;
+    double2* Y = (double2*)a.y.p[c];
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const int ix = (int)(i % g.Nh);
         const int64_t r = i / g.Nh;
@@ -231,15 +280,11 @@ __global__ void k_decay_nonkept3(Geo3 g, Ptrs y, const double* kx, const double*
         if (ix <= g.Mx && kept_full(ky_i, g.Ny, g.My) && kept_full(kz_i, g.Nz, g.Mz)) continue;
         const double2 y0 = Y[i];
         if (y0.x == 0. && y0.y == 0.) continue;
-        const double k2 = radd(radd(rmul(ky[ky_i], ky[ky_i]), rmul(kz[kz_i], kz[kz_i])), rmul(kx[ix], kx[ix]));
-        double Z, f0 = 1., f1 = 1., f2;
-        if (tab) { const double4 t = tab[(int)k2]; Z = t.x; f0 = t.y; f1 = t.z; }
-        else {
-            const double k2v = vo == 1 ? k2 : (vo == 2 ? rmul(k2, k2) : pow(k2, (double)vo));
-            Z = rmul(-rmul(nu, k2v), dt);
-            if (Z != 0.) etd_phis<3>(Z, f0, f1, f2);
-        }
-        Y[i] = etd1_entry(y0, make_double2(0., 0.), Z, f0, f1, dt);
+        const double k2 = k2_of(a.pa, ix, ky_i, kz_i);
+        const int q = a.pa.intk ? (int)k2 : 0;
+        double Z, f0, f1;
+        phis_for(a, grp, q, k2, Z, f0, f1);
+        Y[i] = etd1_entry(y0, make_double2(0., 0.), Z, f0, f1, a.h);
     }
 }
 
@@ -261,7 +306,7 @@ __global__ void k_any_nonkept3(Geo3 g, CPtrs y, int ncomp, int* flag) {
     if (__syncthreads_or(found) && threadIdx.x == 0) atomicOr(flag, 1);
 }
 
-// Zero every non-kept entry of ncomp full-layout arrays (grid.y = component).
+// Zero every non-kept entry of full-layout arrays (grid.y = component).
 __global__ void k_dealias3_all(Geo3 g, Ptrs k) {
     double2* K = (double2*)k.p[blockIdx.y];
     const int64_t n = g.kcount();
@@ -279,42 +324,144 @@ static unsigned ew_grid(int64_t n) {
     return (unsigned)(b < 1 ? 1 : b);
 }
 
-// ------------------------------------------------------------ RHS driver
-struct Hydro3Work {
-    size_t w1, w2, kc;   // complex entries per field
+// ------------------------------------------------------------ drivers
+// workspace: W1 (NI fields), W2 (NI), NC (NO, complex128), then for the RK4
+// step tot (NF) and the stage state (NF), both compact complex128.
+struct Work3 {
+    size_t w1, w2, kc;
+    int ni, no, nf;
     char* base;
     template <typename T> C<T>* W1(int f) const { return (C<T>*)base + f * w1; }
-    template <typename T> C<T>* W2(int f) const { return (C<T>*)base + 6 * w1 + f * w2; }
+    template <typename T> C<T>* W2(int f) const { return (C<T>*)base + ni * w1 + f * w2; }
+    // transform intermediates first, then the complex128 regions from a
+    // 256-byte boundary
+    static size_t up256(size_t b) { return (b + 255) & ~(size_t)255; }
     template <typename T> double2* NC(int f) const {
-        return (double2*)((char*)base + sizeof(C<T>) * (6 * w1 + 6 * w2)) + f * kc;
+        return (double2*)((char*)base + up256(sizeof(C<T>) * ni * (w1 + w2))) + f * kc;
     }
-    template <typename T> static size_t bytes(const Geo3& g) {
-        return sizeof(C<T>) * (6 * g.w1count() + 6 * g.w2count()) + sizeof(double2) * 3 * (size_t)g.Ky * g.Kz * g.Kx;
+    template <typename T> double2* TOT(int f) const { return NC<T>(no) + f * kc; }
+    template <typename T> double2* YS(int f) const { return NC<T>(no + nf) + f * kc; }
+    template <typename T> static size_t bytes(const Geo3& g, int ni, int no, int nf, bool step) {
+        const size_t kc = (size_t)g.Ky * g.Kz * g.Kx;
+        return up256(sizeof(C<T>) * ni * (size_t)(g.w1count() + g.w2count())) +
+               sizeof(double2) * kc * (no + (step ? 2 * nf : 0));
     }
 };
 
-// Passes 1-5: state u (3 comps; full layout, or compact when COMPACT) ->
-// unprojected dealiased RHS in NC (compact).
-template <typename T, bool COMPACT>
-static int hydro3_nonlinear(const dd_plan* pl, const void* const* u, const Hydro3Work& w, cudaStream_t st) {
+template <int PH>
+static Work3 make_work(const Geo3& g, void* base) {
+    using P = Phys3<PH>;
+    return Work3{(size_t)g.w1count(), (size_t)g.w2count(), (size_t)g.Ky * g.Kz * g.Kx, P::NI, P::NO, P::NF,
+                 (char*)base};
+}
+
+template <typename T, bool COMPACT, int PH>
+static int nonlinear3(const dd_plan* pl, const void* const* u, double inv_fpr, const Work3& w, cudaStream_t st) {
+    using P = Phys3<PH>;
     const Geo3& g = pl->g3;
     CPtrs uin{}; Ptrs w1{}, w2{}, nc{}; CPtrs w1c{}, w2c{};
-    for (int c = 0; c < 3; c++) { uin.p[c] = u[c]; nc.p[c] = w.NC<T>(c); }
-    for (int f = 0; f < 6; f++) {
+    for (int c = 0; c < P::NF; c++) uin.p[c] = u[c];
+    for (int c = 0; c < P::NO; c++) nc.p[c] = w.NC<T>(c);
+    for (int f = 0; f < P::NI; f++) {
         w1.p[f] = w.W1<T>(f); w1c.p[f] = w1.p[f];
         w2.p[f] = w.W2<T>(f); w2c.p[f] = w2.p[f];
     }
-    OpZInvCurl3<T, COMPACT> a{g, uin, w1, TwSel<T>::z(pl), pl->kx, pl->ky, pl->kz};
-    DD_TRY((launch_pass_len<T, true, false, false>(g.Nz, a, g.Kx, g.Ky, 6, st)));
+    OpZInvCurl3<T, COMPACT, P::NG> a{g, uin, w1, TwSel<T>::z(pl), pl->kx, pl->ky, pl->kz};
+    DD_TRY((launch_pass_len<T, true, false, false>(g.Nz, a, g.Kx, g.Ky, P::NI, st)));
     OpYInv3<T> b{g, w1c, w2, TwSel<T>::y(pl)};
-    DD_TRY((launch_pass_len<T, true, false, false>(g.Ny, b, g.Kx, g.Nz, 6, st)));
-    // products overwrite fields 0..2 of W2 row by row (each block reads its rows first)
-    DD_TRY((launch_x_prod_len<T>("x_cross", g.Nx, g.Nz * g.Ny, g.Kx, w2c, w2, 1, 0, 0, TwSel<T>::x(pl), (T)pl->inv_n,
-                                 ProdHydro3<T>{}, st)));
+    DD_TRY((launch_pass_len<T, true, false, false>(g.Ny, b, g.Kx, g.Nz, P::NI, st)));
+    // products overwrite fields 0..NO-1 of W2 row by row (each block reads its rows first)
+    if constexpr (PH == P3_HYDRO) {
+        DD_TRY((launch_x_prod_len<T>("x_cross", g.Nx, g.Nz * g.Ny, g.Kx, w2c, w2, 1, 0, 0, TwSel<T>::x(pl),
+                                     (T)pl->inv_n, ProdHydro3<T>{}, st)));
+    } else {
+        DD_TRY((launch_x_prod_len<T>("x_cross_mhd", g.Nx, g.Nz * g.Ny, g.Kx, w2c, w2, 1, 0, 0, TwSel<T>::x(pl),
+                                     (T)pl->inv_n, ProdMHD3<T>{(T)inv_fpr}, st)));
+    }
     OpYFwd3<T> d{g, w2c, w1, TwSel<T>::y(pl)};
-    DD_TRY((launch_pass_len<T, false, false, false>(g.Ny, d, g.Kx, g.Nz, 3, st)));
+    DD_TRY((launch_pass_len<T, false, false, false>(g.Ny, d, g.Kx, g.Nz, P::NO, st)));
     OpZFwdCompact3<T> e{g, w1c, nc, TwSel<T>::z(pl)};
-    DD_TRY((launch_pass_len<T, false, false, false>(g.Nz, e, g.Kx, g.Ky, 3, st)));
+    DD_TRY((launch_pass_len<T, false, false, false>(g.Nz, e, g.Kx, g.Ky, P::NO, st)));
+    return DD_OK;
+}
+
+template <int PH>
+static int nonlinear3_any(const dd_plan* pl, int prec, bool compact, const void* const* u, double inv_fpr,
+                          const Work3& w, cudaStream_t st) {
+    if (prec == DD_FP64) return compact ? nonlinear3<double, true, PH>(pl, u, inv_fpr, w, st)
+                                        : nonlinear3<double, false, PH>(pl, u, inv_fpr, w, st);
+    return compact ? nonlinear3<float, true, PH>(pl, u, inv_fpr, w, st)
+                   : nonlinear3<float, false, PH>(pl, u, inv_fpr, w, st);
+}
+
+// 1 / (4 pi rho0): fpr = 4 * np.pi * rho0 (physics.py:791); numpy divides a
+// complex array by a float by multiplying with the reciprocal.
+static double inv_fpr_of(const double* params) { return 1.0 / ((4.0 * M_PI) * params[0]); }
+
+template <int PH>
+static int rhs3(const dd_plan* p, const double* params, const void* const* u, void* const* deriv,
+                const double* inv_k2, int prec, int zero_nonkept, void* work, size_t wb, cudaStream_t st) {
+    using P = Phys3<PH>;
+    const Geo3& g = p->g3;
+    const size_t need = prec == DD_FP32 ? Work3::bytes<float>(g, P::NI, P::NO, P::NF, false)
+                                        : Work3::bytes<double>(g, P::NI, P::NO, P::NF, false);
+    DD_CHECK_ARG(wb >= need, "workspace too small: %zu < %zu", wb, need);
+    const double inv_fpr = PH == P3_MHD ? inv_fpr_of(params) : 0.;
+    Work3 w = make_work<PH>(g, work);
+    DD_TRY(nonlinear3_any<PH>(p, prec, false, u, inv_fpr, w, st));
+    ProjArgs pa{g, p->kx, p->ky, p->kz, inv_k2, inv_k2 != nullptr};
+    CPtrs nc{}; Ptrs d{};
+    for (int c = 0; c < P::NO; c++) nc.p[c] = prec == DD_FP64 ? (void*)w.NC<double>(c) : (void*)w.NC<float>(c);
+    for (int c = 0; c < P::NF; c++) d.p[c] = deriv[c];
+    if (zero_nonkept) {
+        DD_KT("zero_nonkept3", st, k_dealias3_all<<<dim3(ew_grid(g.kcount()), P::NF), 256, 0, st>>>(g, d));
+        DD_LAUNCH_CHECK();
+    }
+    DD_KT("project3", st, k_project_to_deriv3<PH><<<ew_grid((int64_t)g.Ky * g.Kz * g.Kx), 256, 0, st>>>(pa, nc, d));
+    DD_LAUNCH_CHECK();
+    return DD_OK;
+}
+
+template <int PH>
+static int rk4_3(const dd_plan* p, const double* params, void* const* u, const double* inv_k2,
+                 const void* const* tab_half, const void* const* tab_full, const double* coeff, int vo, double dt,
+                 int prec, const int* nonkept_flag, void* work, size_t wb, cudaStream_t st) {
+    using P = Phys3<PH>;
+    const Geo3& g = p->g3;
+    const size_t need = prec == DD_FP32 ? Work3::bytes<float>(g, P::NI, P::NO, P::NF, true)
+                                        : Work3::bytes<double>(g, P::NI, P::NO, P::NF, true);
+    DD_CHECK_ARG(wb >= need, "workspace too small: %zu < %zu", wb, need);
+    const bool intk = inv_k2 != nullptr;
+    DD_CHECK_ARG(!intk || (tab_half && tab_full), "phi tables required with integer wavenumbers");
+    const double inv_fpr = PH == P3_MHD ? inv_fpr_of(params) : 0.;
+    Work3 w = make_work<PH>(g, work);
+    RK4Args a{};
+    a.pa = ProjArgs{g, p->kx, p->ky, p->kz, inv_k2, intk};
+    a.vo = vo;
+    for (int grp = 0; grp < P::NG; grp++) a.coeff[grp] = coeff[grp];
+    const void* ysc[6] = {};
+    for (int c = 0; c < P::NO; c++) a.nc.p[c] = prec == DD_FP64 ? (void*)w.NC<double>(c) : (void*)w.NC<float>(c);
+    for (int c = 0; c < P::NF; c++) {
+        a.y.p[c] = u[c];
+        a.ys.p[c] = prec == DD_FP64 ? (void*)w.YS<double>(c) : (void*)w.YS<float>(c);
+        a.tot.p[c] = prec == DD_FP64 ? (void*)w.TOT<double>(c) : (void*)w.TOT<float>(c);
+        ysc[c] = a.ys.p[c];
+    }
+    const double hs[4] = {dt / 2., dt / 2., dt, dt};
+    const double ws[4] = {1. / 6., 1. / 3., 1. / 3., 1. / 6.};
+    const unsigned nb = ew_grid((int64_t)w.kc);
+    for (int s = 1; s <= 4; s++) {
+        DD_TRY(nonlinear3_any<PH>(p, prec, s > 1, s == 1 ? (const void* const*)u : ysc, inv_fpr, w, st));
+        a.stage = s; a.h = hs[s - 1]; a.w = ws[s - 1];
+        for (int grp = 0; grp < P::NG; grp++)
+            a.tab[grp] = intk ? (const double4*)(s <= 2 ? tab_half[grp] : tab_full[grp]) : nullptr;
+        DD_KT("rk4_stage3", st, k_rk4_stage3<PH><<<nb, 256, 0, st>>>(a));
+        DD_LAUNCH_CHECK();
+    }
+    if (!nonkept_flag || *nonkept_flag) {
+        DD_KT("decay_nonkept3", st, k_decay_nonkept3<<<dim3(ew_grid(g.kcount()), P::NF), 256, 0, st>>>(a, P::NF));
+        DD_LAUNCH_CHECK();
+    }
     return DD_OK;
 }
 
@@ -322,101 +469,76 @@ static int hydro3_nonlinear(const dd_plan* pl, const void* const* u, const Hydro
 
 using namespace dd;
 
-static int check_hydro3(const dd_plan* p, const void* const* a, const void* const* b) {
+static int check3(const dd_plan* p, int phys, const double* params, const void* const* a, const void* const* b) {
     DD_CHECK_ARG(p, "null plan");
     DD_CHECK_ARG(p->ndim == 3, "plan is not 3D");
-    DD_CHECK_ARG(a && a[0] && a[1] && a[2], "null field pointer");
-    if (b) DD_CHECK_ARG(b[0] && b[1] && b[2], "null field pointer");
+    DD_CHECK_ARG(phys == P3_HYDRO || phys == P3_MHD, "physics must be 0 (hydro) or 1 (MHD)");
+    DD_CHECK_ARG(phys == P3_HYDRO || (params && params[0] > 0.), "MHD needs params = {rho0 > 0}");
+    const int nf = phys == P3_HYDRO ? 3 : 6;
+    DD_CHECK_ARG(a, "null field array");
+    for (int c = 0; c < nf; c++) {
+        DD_CHECK_ARG(a[c], "null field pointer %d", c);
+        if (b) DD_CHECK_ARG(b[c], "null output field pointer %d", c);
+    }
     return DD_OK;
 }
 
 extern "C" {
 
-int dd_hydro3d_workspace_size(const dd_plan* p, int precision, size_t* bytes) {
-    DD_CHECK_ARG(p && bytes && p->ndim == 3, "dd_hydro3d_workspace_size: bad arguments");
-    const Geo3& g = p->g3;
-    const size_t stage = sizeof(double2) * 3 * (size_t)g.Ky * g.Kz * g.Kx * 2;  // tot + stage state
-    *bytes = (precision == DD_FP32 ? Hydro3Work::bytes<float>(g) : Hydro3Work::bytes<double>(g)) + stage;
+int dd_rhs3d_workspace_size(const dd_plan* p, int physics, int precision, size_t* bytes) {
+    DD_CHECK_ARG(p && bytes && p->ndim == 3, "dd_rhs3d_workspace_size: bad arguments");
+    DD_CHECK_ARG(physics == P3_HYDRO || physics == P3_MHD, "physics must be 0 (hydro) or 1 (MHD)");
+    const int ni = physics == P3_HYDRO ? 6 : 12, no = ni / 2, nf = no;
+    *bytes = precision == DD_FP32 ? Work3::bytes<float>(p->g3, ni, no, nf, true)
+                                  : Work3::bytes<double>(p->g3, ni, no, nf, true);
     return DD_OK;
+}
+
+int dd_rhs3d(const dd_plan* p, int physics, const double* params, const void* const* state, void* const* deriv,
+             const double* inv_k2, int precision, int zero_nonkept, void* work, size_t work_bytes, void* stream) {
+    DD_TRY(check3(p, physics, params, state, (const void* const*)deriv));
+    DD_CHECK_ARG(work, "null workspace");
+    DD_CHECK_ARG(precision == DD_FP64 || precision == DD_FP32, "bad precision");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (physics == P3_HYDRO)
+        return rhs3<P3_HYDRO>(p, params, state, deriv, inv_k2, precision, zero_nonkept, work, work_bytes, st);
+    return rhs3<P3_MHD>(p, params, state, deriv, inv_k2, precision, zero_nonkept, work, work_bytes, st);
+}
+
+int dd_rk4_step3d(const dd_plan* p, int physics, const double* params, void* const* state, const double* inv_k2,
+                  const void* const* tab_half, const void* const* tab_full, const double* coeff,
+                  int viscosity_order, double dt, int precision, const int* nonkept_flag, void* work,
+                  size_t work_bytes, void* stream) {
+    DD_TRY(check3(p, physics, params, (const void* const*)state, nullptr));
+    DD_CHECK_ARG(work && coeff, "null workspace or coefficients");
+    DD_CHECK_ARG(precision == DD_FP64 || precision == DD_FP32, "bad precision");
+    DD_CHECK_ARG(viscosity_order >= 1, "viscosity_order must be >= 1");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (physics == P3_HYDRO)
+        return rk4_3<P3_HYDRO>(p, params, state, inv_k2, tab_half, tab_full, coeff, viscosity_order, dt, precision,
+                               nonkept_flag, work, work_bytes, st);
+    return rk4_3<P3_MHD>(p, params, state, inv_k2, tab_half, tab_full, coeff, viscosity_order, dt, precision,
+                         nonkept_flag, work, work_bytes, st);
+}
+
+// Hydro-only forms of the first interface.
+int dd_hydro3d_workspace_size(const dd_plan* p, int precision, size_t* bytes) {
+    return dd_rhs3d_workspace_size(p, P3_HYDRO, precision, bytes);
 }
 
 int dd_hydro3d_rhs(const dd_plan* p, const void* const* u, void* const* deriv, const double* inv_k2,
                    int precision, int zero_nonkept, void* work, size_t work_bytes, void* stream) {
-    DD_TRY(check_hydro3(p, (const void* const*)u, (const void* const*)deriv));
-    DD_CHECK_ARG(work, "null workspace");
-    DD_CHECK_ARG(precision == DD_FP64 || precision == DD_FP32, "bad precision");
-    const Geo3& g = p->g3;
-    cudaStream_t st = (cudaStream_t)stream;
-    Hydro3Work w{(size_t)g.w1count(), (size_t)g.w2count(), (size_t)g.Ky * g.Kz * g.Kx, (char*)work};
-    const size_t need = precision == DD_FP32 ? Hydro3Work::bytes<float>(g) : Hydro3Work::bytes<double>(g);
-    DD_CHECK_ARG(work_bytes >= need, "workspace too small: %zu < %zu", work_bytes, need);
-    if (precision == DD_FP64) DD_TRY((hydro3_nonlinear<double, false>(p, u, w, st)));
-    else DD_TRY((hydro3_nonlinear<float, false>(p, u, w, st)));
-    ProjArgs pa{g, p->kx, p->ky, p->kz, inv_k2, inv_k2 != nullptr};
-    CPtrs nc{}; Ptrs d{};
-    for (int c = 0; c < 3; c++) {
-        nc.p[c] = precision == DD_FP64 ? (void*)w.NC<double>(c) : (void*)w.NC<float>(c);
-        d.p[c] = deriv[c];
-    }
-    if (zero_nonkept) {
-        DD_KT("zero_nonkept3", st, k_dealias3_all<<<dim3(ew_grid(g.kcount()), 3), 256, 0, st>>>(g, d));
-        DD_LAUNCH_CHECK();
-    }
-    DD_KT("project3", st, k_project_to_deriv3<<<ew_grid((int64_t)g.Ky * g.Kz * g.Kx), 256, 0, st>>>(pa, nc, d));
-    DD_LAUNCH_CHECK();
-    return DD_OK;
+    return dd_rhs3d(p, P3_HYDRO, nullptr, u, deriv, inv_k2, precision, zero_nonkept, work, work_bytes, stream);
 }
 
 int dd_hydro3d_rk4_step(const dd_plan* p, void* const* u, const double* inv_k2, const void* tab_half,
                         const void* tab_full, double nu, int viscosity_order, double dt, int precision,
                         int* nonkept_flag, void* work, size_t work_bytes, void* stream) {
-    DD_TRY(check_hydro3(p, (const void* const*)u, nullptr));
-    DD_CHECK_ARG(work, "null workspace");
-    DD_CHECK_ARG(precision == DD_FP64 || precision == DD_FP32, "bad precision");
-    DD_CHECK_ARG(viscosity_order >= 1, "viscosity_order must be >= 1");
-    const Geo3& g = p->g3;
-    cudaStream_t st = (cudaStream_t)stream;
-    Hydro3Work w{(size_t)g.w1count(), (size_t)g.w2count(), (size_t)g.Ky * g.Kz * g.Kx, (char*)work};
-    const size_t base = precision == DD_FP32 ? Hydro3Work::bytes<float>(g) : Hydro3Work::bytes<double>(g);
-    const size_t kc = (size_t)g.Ky * g.Kz * g.Kx;
-    DD_CHECK_ARG(work_bytes >= base + sizeof(double2) * 6 * kc, "workspace too small");
-    double2* tot = (double2*)((char*)work + base);
-    double2* ys = tot + 3 * kc;
-    const bool intk = inv_k2 != nullptr;
-    DD_CHECK_ARG(!intk || (tab_half && tab_full), "phi tables required with integer wavenumbers");
-    ProjArgs pa{g, p->kx, p->ky, p->kz, inv_k2, intk};
-    RK4Args a{};
-    a.pa = pa;
-    a.nu = nu; a.vo = viscosity_order;
-    for (int c = 0; c < 3; c++) {
-        a.nc.p[c] = precision == DD_FP64 ? (void*)w.NC<double>(c) : (void*)w.NC<float>(c);
-        a.y.p[c] = u[c];
-        a.ys.p[c] = ys + c * kc;
-        a.tot.p[c] = tot + c * kc;
-    }
-    const void* ysc[3] = {ys, ys + kc, ys + 2 * kc};
-    const double hs[4] = {dt / 2., dt / 2., dt, dt};
-    const double ws[4] = {1. / 6., 1. / 3., 1. / 3., 1. / 6.};
-    const void* tabs[4] = {tab_half, tab_half, tab_full, tab_full};
-    for (int s = 1; s <= 4; s++) {
-        if (s == 1) {
-            if (precision == DD_FP64) DD_TRY((hydro3_nonlinear<double, false>(p, (const void* const*)u, w, st)));
-            else DD_TRY((hydro3_nonlinear<float, false>(p, (const void* const*)u, w, st)));
-        } else {
-            if (precision == DD_FP64) DD_TRY((hydro3_nonlinear<double, true>(p, ysc, w, st)));
-            else DD_TRY((hydro3_nonlinear<float, true>(p, ysc, w, st)));
-        }
-        a.stage = s; a.h = hs[s - 1]; a.w = ws[s - 1]; a.tab = (const double4*)tabs[s - 1];
-        DD_KT("rk4_stage3", st, k_rk4_stage3<<<ew_grid((int64_t)kc), 256, 0, st>>>(a));
-        DD_LAUNCH_CHECK();
-    }
-    if (nonkept_flag && *nonkept_flag) {
-        DD_KT("decay_nonkept3", st,
-              k_decay_nonkept3<<<dim3(ew_grid(g.kcount()), 3), 256, 0, st>>>(g, a.y, p->kx, p->ky, p->kz,
-                                                                           (const double4*)tab_full, nu, viscosity_order, dt));
-        DD_LAUNCH_CHECK();
-    }
-    return DD_OK;
+    const void* th[1] = {tab_half};
+    const void* tf[1] = {tab_full};
+    const double c[1] = {nu};
+    return dd_rk4_step3d(p, P3_HYDRO, nullptr, u, inv_k2, th, tf, c, viscosity_order, dt, precision, nonkept_flag,
+                         work, work_bytes, stream);
 }
 
 int dd_any_nonkept(const dd_plan* p, int ncomp, const void* const* k, int* dflag, void* stream) {

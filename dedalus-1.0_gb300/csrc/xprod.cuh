@@ -72,6 +72,7 @@ k_x_prod(int nrows, int Kx, CPtrs win, Ptrs wout, int64_t in_rs, int64_t out_rs,
          const typename Vec2<T>::type* gtw, T scale, const Op op) {
     using V = typename Vec2<T>::type;
     constexpr int NI = Op::NI, NO = Op::NO;
+    static_assert(NI <= DD_MAXF && NO <= DD_MAXF, "too many fields for Ptrs");
     using CC = ProdCfg<L, NI, NO>;
     using SI = typename CC::SI;
     using SF = typename CC::SF;

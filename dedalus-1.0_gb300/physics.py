@@ -171,22 +171,74 @@ class IncompressibleHydro(Physics):
                 c.data = c.kdata
                 c._curr_space = 'kspace'
 
+    # ------------------------------------------------------------ 3D
+    _phys3d = 0
+
+    def _state3d(self):
+        return [('u', 0), ('u', 1), ('u', 2)]
+
+    def _params3d(self):
+        return None
+
+    def _groups3d(self):
+        return ['u']
+
     def RHS(self, data, deriv):
         """RHS(u) = P[-(u.grad)u] (physics.py:527-599), fused on the GPU."""
         self._begin_rhs(data, deriv)
         plan = self.plan(data)
         if self.ndim != 3:
             return self._rhs2d(data, deriv, plan)
+        self._rhs3d(data, deriv, plan)
+
+    def _rhs3d(self, data, deriv, plan):
         prec = precision_code()
         n = ctypes.c_size_t()
-        _lib.call("dd_hydro3d_workspace_size", plan.handle, prec, ctypes.byref(n))
+        _lib.call("dd_rhs3d_workspace_size", plan.handle, self._phys3d, prec, ctypes.byref(n))
         ws = self.workspace(n.value)
-        up, _a = _ptrs([c.kdata for i, c in data['u']])
-        dp, _b = _ptrs([c.kdata for i, c in deriv['u']])
+        names = self._state3d()
+        sp, _a = _ptrs([data[f][c].kdata for f, c in names])
+        dp, _b = _ptrs([deriv[f][c].kdata for f, c in names])
+        pp = self._params3d()
+        ppa = None if pp is None else (ctypes.c_double * len(pp))(*pp)
         ik2 = self.inv_k2_table(plan)
-        _lib.call("dd_hydro3d_rhs", plan.handle, up, dp, None if ik2 is None else dptr(ik2), prec, 1,
+        _lib.call("dd_rhs3d", plan.handle, self._phys3d, ppa, sp, dp, None if ik2 is None else dptr(ik2), prec, 1,
                   dptr(ws), ws.numel(), current_stream())
         self._mark_kspace(deriv)
+
+    def fused_rk4(self, data, dt):
+        """One fused RK4 step on the device (dd_rk4_step3d) for 3D hydro / MHD;
+        returns False when this physics/grid has no fused step."""
+        if self.ndim != 3 or type(self) not in (IncompressibleHydro, IncompressibleMHD):
+            return False
+        if not self._is_finalized:
+            self._finalize()
+        names = self._state3d()
+        for f, c in names:
+            data[f][c].require_space('kspace')
+        plan = self.plan(data)
+        prec = precision_code()
+        vo = int(self.parameters['viscosity_order'])
+        coeffs = [float(self._coeff_of(g)) for g in self._groups3d()]
+        n = ctypes.c_size_t()
+        _lib.call("dd_rhs3d_workspace_size", plan.handle, self._phys3d, prec, ctypes.byref(n))
+        ws = self.workspace(n.value)
+        ik2 = self.inv_k2_table(plan)
+        th = tf = None
+        keep = []
+        if ik2 is not None:
+            tabs_h = [self.phi_table(plan, cf, vo, dt / 2.) for cf in coeffs]
+            tabs_f = [self.phi_table(plan, cf, vo, dt) for cf in coeffs]
+            th, _h = _ptrs(tabs_h)
+            tf, _f = _ptrs(tabs_f)
+            keep = [tabs_h, tabs_f, _h, _f]
+        sp, _a = _ptrs([data[f][c].kdata for f, c in names])
+        pp = self._params3d()
+        ppa = None if pp is None else (ctypes.c_double * len(pp))(*pp)
+        cf = (ctypes.c_double * len(coeffs))(*coeffs)
+        _lib.call("dd_rk4_step3d", plan.handle, self._phys3d, ppa, sp, None if ik2 is None else dptr(ik2), th, tf,
+                  cf, vo, float(dt), prec, None, dptr(ws), ws.numel(), current_stream())
+        return True
 
     # ------------------------------------------------------------ 2D
     _phys2d = 0
@@ -249,33 +301,6 @@ class IncompressibleHydro(Physics):
         _lib.call("dd_rk2mid_step2d", plan.handle, self._phys2d, ppa, 1, sp, 0,
                   None if ik2 is None else dptr(ik2), th, tf, nus, vo, float(dt), prec,
                   dptr(ws), ws.numel(), current_stream())
-        return True
-
-    def fused_rk4(self, data, dt):
-        """One fused RK4 step on the device (dd_hydro3d_rk4_step); returns
-        False when this physics/grid has no fused step."""
-        if self.ndim != 3 or type(self) is not IncompressibleHydro:
-            return False
-        if not self._is_finalized:
-            self._finalize()
-        for i, c in data['u']:
-            c.require_space('kspace')
-        plan = self.plan(data)
-        prec = precision_code()
-        nu, vo = float(self.parameters['nu']), int(self.parameters['viscosity_order'])
-        n = ctypes.c_size_t()
-        _lib.call("dd_hydro3d_workspace_size", plan.handle, prec, ctypes.byref(n))
-        ws = self.workspace(n.value)
-        ik2 = self.inv_k2_table(plan)
-        th = tf = None
-        if ik2 is not None:
-            th = self.phi_table(plan, nu, vo, dt / 2.)
-            tf = self.phi_table(plan, nu, vo, dt)
-        up, _a = _ptrs([c.kdata for i, c in data['u']])
-        flag = ctypes.c_int(1)
-        _lib.call("dd_hydro3d_rk4_step", plan.handle, up, None if ik2 is None else dptr(ik2),
-                  None if th is None else dptr(th), None if tf is None else dptr(tf), nu, vo, float(dt), prec,
-                  ctypes.byref(flag), dptr(ws), ws.numel(), current_stream())
         return True
 
     def max_abs_vel(self, data):
@@ -348,8 +373,23 @@ class IncompressibleMHD(IncompressibleHydro):
     def _diffusivities(self):
         return [('u', self.parameters['nu']), ('B', self.parameters['eta'])]
 
+    _phys3d = 1
+
+    def _state3d(self):
+        return [('u', 0), ('u', 1), ('u', 2), ('B', 0), ('B', 1), ('B', 2)]
+
+    def _params3d(self):
+        return [float(self.parameters['rho0'])]
+
+    def _groups3d(self):
+        return ['u', 'B']
+
     def RHS(self, data, deriv):
-        raise NotImplementedError("MHD RHS is not available yet")
+        """physics.py:770-819, fused on the GPU (3D)."""
+        if self.ndim != 3:
+            raise NotImplementedError("2D MHD is not in the CUDA path")
+        self._begin_rhs(data, deriv)
+        self._rhs3d(data, deriv, self.plan(data))
 
     def max_alfven_speed(self, data):
         fpr = 4 * np.pi * self.parameters['rho0']

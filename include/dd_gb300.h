@@ -184,6 +184,24 @@ int dd_rk2mid_step2d(const dd_plan* plan, int physics, const double* params, int
                      const void* const* tab_full, const double* nu, int viscosity_order, double dt,
                      int precision, void* work, size_t work_bytes, void* stream);
 
+/* ------------------------------------------------------ fused 3D physics
+ * physics 0 = IncompressibleHydro (state u_x, u_y, u_z; physics.py:527-599),
+ * physics 1 = IncompressibleMHD (state u_x, u_y, u_z, B_x, B_y, B_z;
+ * physics.py:770-819) with params = {rho0}.  Shear, rotation, tracer and
+ * forcing are not implemented.  dd_rhs3d writes the dealiased RHS of every
+ * state component into deriv (full layout); dd_rk4_step3d advances the state
+ * in place by one RK4 step (definition as for dd_hydro3d_rk4_step) with one
+ * diffusivity per vector field, coeff = {nu} or {nu, eta}, and one pair of
+ * dd_phi_table tables per vector field.  nonkept_flag: host int, or NULL to
+ * always treat modes outside the kept set (they decay as etd1(y, 0, dt)). */
+int dd_rhs3d_workspace_size(const dd_plan* plan, int physics, int precision, size_t* bytes);
+int dd_rhs3d(const dd_plan* plan, int physics, const double* params, const void* const* state, void* const* deriv,
+             const double* inv_k2, int precision, int zero_nonkept, void* work, size_t work_bytes, void* stream);
+int dd_rk4_step3d(const dd_plan* plan, int physics, const double* params, void* const* state, const double* inv_k2,
+                  const void* const* tab_half, const void* const* tab_full, const double* coeff,
+                  int viscosity_order, double dt, int precision, const int* nonkept_flag, void* work,
+                  size_t work_bytes, void* stream);
+
 /* Sets *dflag (device int) to 1 if any of the ncomp k arrays has a non-zero
  * entry outside the kept (dealiased) modes; does not clear it. */
 int dd_any_nonkept(const dd_plan* plan, int ncomp, const void* const* k, int* dflag, void* stream);

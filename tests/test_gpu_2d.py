@@ -125,3 +125,34 @@ def test_boussinesq2d_default_direction_raises_keyerror(dd, cuda):
     dg = rg.create_fields(0.)
     with pytest.raises(KeyError):
         rg.RHS(dg, rg.create_fields(0.))
+
+
+@pytest.mark.gpu
+def test_gravity_wave_known_answer(dd, cuda):
+    """Gravity-wave eigenmode of the reference's sample
+    (samples/boussinesq_hydro/gravity_wave/2d_gmode_kx1_kz1.py:36-54), in 2D
+    with gravity along y: at k = (1, 1) the amplitudes rotate as exp(-i w t),
+    w = beta sqrt(kx^2 / (kx^2 + ky^2)) with N^2 = g alpha beta = 1."""
+    shape = (32, 32)
+    M = dd.mods
+    rhs = M.BoussinesqHydro(shape, M.FourierRepresentation)
+    rhs.parameters.update({'g': 1., 'alpha_t': 1., 'beta': 1., 'nu': 0., 'kappa': 0.,
+                           'boussinesq_direction': 'y'})
+    data = rhs.create_fields(0.)
+    kx, ky, uy = 1., 1., 0.5
+    omega = np.sqrt(kx ** 2 / (kx ** 2 + ky ** 2)) * rhs.parameters['beta']
+    mode = data['u']['y'].find_mode(np.array([kx, ky]))
+    init = {('u', 1): uy, ('u', 0): -ky / kx * uy,
+            ('T', 0): -1j * rhs.parameters['beta'] / np.sqrt(kx ** 2 / (kx ** 2 + ky ** 2)) * uy}
+    for (f, c), v in init.items():
+        a = np.zeros(data[f][c].kdata.shape, complex)
+        a[mode] = v
+        data[f][c]['kspace'] = a
+    ti = M.RK2mid(rhs)
+    dt, nsteps = 1e-3, 2000
+    for _ in range(nsteps):
+        ti.do_advance(data, dt)
+    phase = np.exp(-1j * omega * dt * nsteps)
+    for (f, c), v in init.items():
+        got = data[f][c].to_numpy('kspace')[mode]
+        assert abs(got - v * phase) < 1e-5 * abs(v), (f, c, got, v * phase)
