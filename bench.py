@@ -33,6 +33,7 @@ WORKLOADS = {
     "hydro3d-256-fp64": dict(shape=(256, 256, 256), nu=5e-3, dt=2e-3, precision="fp64"),
     "hydro3d-256-fp32": dict(shape=(256, 256, 256), nu=5e-3, dt=2e-3, precision="fp32"),
     "hydro3d-128-fp64": dict(shape=(128, 128, 128), nu=5e-3, dt=2e-3, precision="fp64"),
+    "hydro3d-256-df64": dict(shape=(256, 256, 256), nu=5e-3, dt=2e-3, precision="df64"),
 }
 
 
@@ -50,7 +51,7 @@ def kernel_bytes(label, shape, precision):
     Nz, Ny, Nx = shape
     Mx, My, Mz = (Nx - 1) // 3, (Ny - 1) // 3, (Nz - 1) // 3
     Kx, Ky, Kz = Mx + 1, 2 * My + 1, 2 * Mz + 1
-    cs = 16 if precision == "fp64" else 8           # intermediate complex entry
+    cs = 8 if precision == "fp32" else 16           # intermediate complex entry
     kc = Ky * Kz * Kx * 16                          # compact kept complex128 array
     w1 = Ky * Nz * Kx * cs
     w2 = Nz * Ny * Kx * cs
@@ -204,6 +205,7 @@ def main():
     ap.add_argument("--workload", default="hydro3d-256-fp64", choices=sorted(WORKLOADS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-variants", action="store_true")
     args = ap.parse_args()
     wl = WORKLOADS[args.workload]
     ws, rank, local = setup_dist()
@@ -323,6 +325,47 @@ def main():
         e2e = {"value": ws * ke / (me / 1e3), "unit": "steps/s", "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb,
                "steps": ke, "host_wall_s": wall}
 
+    # the same workload with the other transform arithmetics, from the same
+    # initial state, with their difference from the FP64 state after the
+    # same steps (FP64 native is the reference; it is the headline value)
+    variants = None
+    if not args.no_variants and wl["precision"] == "fp64":
+        variants = {}
+        kv = max(3, min(args.steps, 10))
+        ref = None
+
+        def run_prec(prec):
+            dd.config.decfg.set("FFT", "precision", prec)
+            try:
+                r = M.IncompressibleHydro(shape, M.FourierRepresentation)
+                r.parameters["nu"] = wl["nu"]
+                d = r.create_fields(0.)
+                for i in range(3):
+                    d["u"][i]["kspace"] = u0[i]
+                t = M.RK4(r)
+                t.do_advance(d, dt)  # warm-up step, part of the compared trajectory
+                torch.cuda.synchronize()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                for _ in range(kv):
+                    t.do_advance(d, dt)
+                b.record(stream)
+                torch.cuda.synchronize()
+                out = [d["u"][i].kdata.clone() for i in range(3)]
+                del r, d, t
+                return a.elapsed_time(b) / kv, out
+            finally:
+                dd.config.decfg.set("FFT", "precision", "fp64")
+
+        ms64, ref = run_prec("fp64")
+        den = sum(float(torch.sum(torch.abs(x) ** 2)) for x in ref)
+        for prec in ("df64", "fp32"):
+            msv, outv = run_prec(prec)
+            num = sum(float(torch.sum(torch.abs(x - y) ** 2)) for x, y in zip(outv, ref))
+            variants[prec] = {"steps_per_s": ws * 1e3 / msv, "ms_per_step": msv,
+                              "rel_l2_vs_fp64_after_%d_steps" % (kv + 1): (num / den) ** 0.5}
+        variants["fp64_repeat"] = {"steps_per_s": ws * 1e3 / ms64, "ms_per_step": ms64}
+
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         times = cpu_reference_steps(wl, 0, 1, 1, 60.0)
@@ -338,10 +381,11 @@ def main():
     vs = None
     line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": vs, "dtype": "f64" if wl["precision"] == "fp64" else "f32",
+            "vs_baseline": vs, "dtype": {"fp64": "f64", "df64": "df64", "fp32": "f32"}[wl["precision"]],
             "data": "synthetic (seeded random-phase solenoidal field, E(k)~k^4 exp(-2(k/4)^2), unit energy)",
             "config": config_of(args, wl, ws), "clocks": clocks, "e2e": e2e, "gpu_launches": launches,
-            "roofline": roofline, "step_roofline": step_hbm, "kernels": kernels, "cpu_baseline": cpu}
+            "roofline": roofline, "step_roofline": step_hbm, "kernels": kernels, "variants": variants,
+            "cpu_baseline": cpu}
     print(json.dumps(line))
     return 0
 

@@ -12,7 +12,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libdd_gb300.so")
 
 DD_OK, DD_ERR_INVALID, DD_ERR_UNSUPPORTED, DD_ERR_CUDA, DD_ERR_TIMEOUT, DD_ERR_WORKSPACE = range(6)
-DD_FP64, DD_FP32 = 0, 1
+DD_FP64, DD_FP32, DD_DF64 = 0, 1, 2
 
 _EXC = {
     DD_ERR_INVALID: ValueError,

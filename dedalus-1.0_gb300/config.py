@@ -2,8 +2,8 @@
 path reads, with the CUDA backend as the default FFT method.
 
 Keys: ``FFT.method`` ('cuda'), ``FFT.dealiasing`` ('2/3 cython', '2/3',
-'None'), ``FFT.precision`` ('fp64' | 'fp32', transform and nonlinear-product
-arithmetic), ``physics.use_tracer``, ``physics.boussinesq_direction``.  User
+'None'), ``FFT.precision`` ('fp64' | 'df64' | 'fp32': transform and nonlinear-product
+arithmetic; df64 = double-float on the FP32 pipes, 3D hydro only), ``physics.use_tracer``, ``physics.boussinesq_direction``.  User
 files ``~/.dedalus/config`` and ``./dedalus.cfg`` override the defaults, as in
 the reference.
 """
@@ -27,4 +27,6 @@ def precision_code():
         return 0
     if p == 'fp32':
         return 1
-    raise NotImplementedError("FFT.precision must be fp64 or fp32 (got %r)" % p)
+    if p == 'df64':
+        return 2
+    raise NotImplementedError("FFT.precision must be fp64, df64 or fp32 (got %r)" % p)

@@ -101,6 +101,11 @@ __device__ __forceinline__ void stc(typename Vec2<T>::type* p, C<T> a) {
     typename Vec2<T>::type v; v.x = a.x; v.y = a.y; *p = v;
 }
 
+// Short precision tag for labels: f64, f32, df64.
+template <typename T> struct PrecName;
+template <> struct PrecName<double> { static constexpr const char* s = "_f64"; };
+template <> struct PrecName<float> { static constexpr const char* s = "_f32"; };
+
 inline unsigned cdiv(long long a, long long b) { return (unsigned)((a + b - 1) / b); }
 
 }  // namespace dd

@@ -5,7 +5,7 @@
 #include <string.h>
 #include <vector>
 
-#include "launch_len.cuh"
+#include "fft_impl.cuh"
 
 namespace dd {
 
@@ -52,19 +52,24 @@ static void make_twiddles(int L, std::vector<double>& re, std::vector<double>& i
     }
 }
 
-static int upload_twiddles(int L, double2** d64, float2** d32) {
+static int upload_twiddles(int L, double2** d64, float2** d32, float4** ddf) {
     std::vector<double> re, im;
     make_twiddles(L, re, im);
     std::vector<double2> h64(L);
     std::vector<float2> h32(L);
+    std::vector<float4> hdf(L);
     for (int m = 0; m < L; m++) {
         h64[m] = make_double2(re[m], im[m]);
         h32[m] = make_float2((float)re[m], (float)im[m]);
+        const df64 a(re[m]), b(im[m]);
+        hdf[m] = make_float4(a.hi, a.lo, b.hi, b.lo);
     }
     DD_CUDA(cudaMalloc((void**)d64, sizeof(double2) * L));
     DD_CUDA(cudaMalloc((void**)d32, sizeof(float2) * L));
+    DD_CUDA(cudaMalloc((void**)ddf, sizeof(float4) * L));
     DD_CUDA(cudaMemcpy(*d64, h64.data(), sizeof(double2) * L, cudaMemcpyHostToDevice));
     DD_CUDA(cudaMemcpy(*d32, h32.data(), sizeof(float2) * L, cudaMemcpyHostToDevice));
+    DD_CUDA(cudaMemcpy(*ddf, hdf.data(), sizeof(float4) * L, cudaMemcpyHostToDevice));
     return DD_OK;
 }
 
@@ -74,137 +79,8 @@ static int upload_doubles(const double* h, int n, double** d) {
     return DD_OK;
 }
 
-// -------------------------------------------------------- zero / dealias
-template <typename KT>
-__global__ void k_zero_nonkept3(Geo3 g, Ptrs k) {
-    using KV = typename Vec2<KT>::type;
-    KV* K = (KV*)k.p[blockIdx.y];
-    const int64_t n = g.kcount();
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const int kx = (int)(i % g.Nh);
-        const int ky = (int)(i / ((int64_t)g.Nh * g.Nz));
-        if (kx >= g.Kx || !kept_full(ky, g.Ny, g.My)) { KV z; z.x = 0; z.y = 0; K[i] = z; }
-    }
-}
-
-template <typename KT>
-__global__ void k_zero_nonkept2(Geo2 g, Ptrs k) {
-    using KV = typename Vec2<KT>::type;
-    KV* K = (KV*)k.p[blockIdx.y];
-    const int64_t n0 = (int64_t)g.Kx * g.Ny, n = g.kcount();
-    for (int64_t i = n0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        KV z; z.x = 0; z.y = 0; K[i] = z;
-    }
-}
-
-__global__ void k_dealias3(Geo3 g, double2* K) {
-    const int64_t n = g.kcount();
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const int kx = (int)(i % g.Nh);
-        const int64_t r = i / g.Nh;
-        const int kz = (int)(r % g.Nz), ky = (int)(r / g.Nz);
-        if (kx > g.Mx || !kept_full(ky, g.Ny, g.My) || !kept_full(kz, g.Nz, g.Mz)) K[i] = make_double2(0., 0.);
-    }
-}
-
-__global__ void k_dealias2(Geo2 g, double2* K) {
-    const int64_t n = g.kcount();
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const int ky = (int)(i % g.Ny), kx = (int)(i / g.Ny);
-        if (kx > g.Mx || !kept_full(ky, g.Ny, g.My)) K[i] = make_double2(0., 0.);
-    }
-}
-
-static unsigned ew_grid(int64_t n) {
-    int64_t b = (n + 255) / 256;
-    if (b > 152 * 16) b = 152 * 16;
-    return (unsigned)(b < 1 ? 1 : b);
-}
-
-// -------------------------------------------------------- transforms
-template <typename T>
-size_t ws_bytes(const dd_plan* pl, int nf) {
-    if (pl->ndim == 3) return (size_t)nf * (pl->g3.w1count() + pl->g3.w2count()) * sizeof(C<T>);
-    return (size_t)nf * pl->g2.wcount() * sizeof(C<T>);
-}
-
-template <typename T>
-int fft_c2r(const dd_plan* pl, int nf, const void* const* k, double* const* x, void* work, size_t wb,
-            cudaStream_t st) {
-    DD_CHECK_ARG(wb >= ws_bytes<T>(pl, nf), "workspace too small: %zu < %zu bytes", wb, ws_bytes<T>(pl, nf));
-    CPtrs kin{}; Ptrs xo{};
-    for (int f = 0; f < nf; f++) { kin.p[f] = k[f]; xo.p[f] = x[f]; }
-    if (pl->ndim == 3) {
-        const Geo3& g = pl->g3;
-        C<T>* W1 = (C<T>*)work;
-        C<T>* W2 = W1 + (size_t)nf * g.w1count();
-        Ptrs w1{}, w2{}; CPtrs w1c{}, w2c{};
-        for (int f = 0; f < nf; f++) {
-            w1.p[f] = W1 + f * g.w1count(); w1c.p[f] = w1.p[f];
-            w2.p[f] = W2 + f * g.w2count(); w2c.p[f] = w2.p[f];
-        }
-        OpZInv3<T, double> a{g, kin, w1, TwSel<T>::z(pl)};
-        DD_TRY((launch_pass_len<T, true, false, false>(g.Nz, a, g.Kx, g.Ky, nf, st)));
-        OpYInv3<T> b{g, w1c, w2, TwSel<T>::y(pl)};
-        DD_TRY((launch_pass_len<T, true, false, false>(g.Ny, b, g.Kx, g.Nz, nf, st)));
-        const int nrows = g.Nz * g.Ny;
-        OpXc2r3<T, double> c{nrows, g.Nx, g.Kx, w2c, xo, TwSel<T>::x(pl)};
-        DD_TRY((launch_pass_len<T, true, true, true>(g.Nx, c, (nrows + 1) / 2, 1, nf, st)));
-    } else {
-        const Geo2& g = pl->g2;
-        C<T>* W = (C<T>*)work;
-        Ptrs w{}; CPtrs wc{};
-        for (int f = 0; f < nf; f++) { w.p[f] = W + f * g.wcount(); wc.p[f] = w.p[f]; }
-        OpYInv2<T, double> a{g, kin, w, TwSel<T>::y(pl)};
-        DD_TRY((launch_pass_len<T, true, true, false>(g.Ny, a, g.Kx, 1, nf, st)));
-        OpXc2r3<T, double> c{g.Ny, g.Nx, g.Kx, wc, xo, TwSel<T>::x(pl)};
-        DD_TRY((launch_pass_len<T, true, true, true>(g.Nx, c, (g.Ny + 1) / 2, 1, nf, st)));
-    }
-    return DD_OK;
-}
-
-template <typename T>
-int fft_r2c(const dd_plan* pl, int nf, const double* const* x, void* const* k, void* work, size_t wb,
-            cudaStream_t st) {
-    DD_CHECK_ARG(wb >= ws_bytes<T>(pl, nf), "workspace too small: %zu < %zu bytes", wb, ws_bytes<T>(pl, nf));
-    CPtrs xin{}; Ptrs ko{};
-    for (int f = 0; f < nf; f++) { xin.p[f] = x[f]; ko.p[f] = k[f]; }
-    const T s = (T)pl->inv_n;
-    if (pl->ndim == 3) {
-        const Geo3& g = pl->g3;
-        C<T>* W1 = (C<T>*)work;
-        C<T>* W2 = W1 + (size_t)nf * g.w1count();
-        Ptrs w1{}, w2{}; CPtrs w1c{}, w2c{};
-        for (int f = 0; f < nf; f++) {
-            w1.p[f] = W1 + f * g.w1count(); w1c.p[f] = w1.p[f];
-            w2.p[f] = W2 + f * g.w2count(); w2c.p[f] = w2.p[f];
-        }
-        const int nrows = g.Nz * g.Ny;
-        OpXr2c3<T, double> a{nrows, g.Nx, g.Kx, s, xin, w2, TwSel<T>::x(pl)};
-        DD_TRY((launch_pass_len<T, false, true, true>(g.Nx, a, (nrows + 1) / 2, 1, nf, st)));
-        OpYFwd3<T> b{g, w2c, w1, TwSel<T>::y(pl)};
-        DD_TRY((launch_pass_len<T, false, false, false>(g.Ny, b, g.Kx, g.Nz, nf, st)));
-        OpZFwd3<T, double> c{g, w1c, ko, TwSel<T>::z(pl)};
-        DD_TRY((launch_pass_len<T, false, false, false>(g.Nz, c, g.Kx, g.Ky, nf, st)));
-        DD_KT("zero_nonkept3", st, k_zero_nonkept3<double><<<dim3(ew_grid(g.kcount()), nf), 256, 0, st>>>(g, ko));
-        DD_LAUNCH_CHECK();
-    } else {
-        const Geo2& g = pl->g2;
-        C<T>* W = (C<T>*)work;
-        Ptrs w{}; CPtrs wc{};
-        for (int f = 0; f < nf; f++) { w.p[f] = W + f * g.wcount(); wc.p[f] = w.p[f]; }
-        OpXr2c3<T, double> a{g.Ny, g.Nx, g.Kx, s, xin, w, TwSel<T>::x(pl)};
-        DD_TRY((launch_pass_len<T, false, true, true>(g.Nx, a, (g.Ny + 1) / 2, 1, nf, st)));
-        OpYFwd2<T, double> b{g, wc, ko, TwSel<T>::y(pl)};
-        DD_TRY((launch_pass_len<T, false, false, true>(g.Ny, b, g.Kx, 1, nf, st)));
-        const int64_t nz = g.kcount() - (int64_t)g.Kx * g.Ny;
-        if (nz > 0) {
-            DD_KT("zero_nonkept2", st, k_zero_nonkept2<double><<<dim3(ew_grid(nz), nf), 256, 0, st>>>(g, ko));
-            DD_LAUNCH_CHECK();
-        }
-    }
-    return DD_OK;
-}
+DD_FFT_INSTANTIATE(extern, double)
+DD_FFT_INSTANTIATE(extern, float)
 
 }  // namespace dd
 
@@ -255,16 +131,18 @@ int dd_plan_create(int ndim, const int64_t* xshape, const double* kx, const doub
         p->inv_n = 1.0 / ((double)Nx * Ny);
         if ((rc = upload_doubles(kx, Nh, &p->kx)) || (rc = upload_doubles(ky, Ny, &p->ky))) return fail(rc);
     }
-    if ((rc = upload_twiddles(Nx, &p->tw64_x, &p->tw32_x)) || (rc = upload_twiddles(Ny, &p->tw64_y, &p->tw32_y)))
+    if ((rc = upload_twiddles(Nx, &p->tw64_x, &p->tw32_x, &p->twdf_x)) ||
+        (rc = upload_twiddles(Ny, &p->tw64_y, &p->tw32_y, &p->twdf_y)))
         return fail(rc);
-    if (ndim == 3 && (rc = upload_twiddles(Nz, &p->tw64_z, &p->tw32_z))) return fail(rc);
+    if (ndim == 3 && (rc = upload_twiddles(Nz, &p->tw64_z, &p->tw32_z, &p->twdf_z))) return fail(rc);
     *out = p;
     return DD_OK;
 }
 
 int dd_plan_destroy(dd_plan* p) {
     if (!p) return DD_OK;
-    void* bufs[] = {p->kx, p->ky, p->kz, p->tw64_x, p->tw64_y, p->tw64_z, p->tw32_x, p->tw32_y, p->tw32_z};
+    void* bufs[] = {p->kx, p->ky, p->kz, p->tw64_x, p->tw64_y, p->tw64_z, p->tw32_x, p->tw32_y, p->tw32_z,
+                    p->twdf_x, p->twdf_y, p->twdf_z};
     for (void* b : bufs)
         if (b) cudaFree(b);
     free(p);
@@ -274,8 +152,8 @@ int dd_plan_destroy(dd_plan* p) {
 int dd_plan_workspace_size(const dd_plan* p, int nfield, int precision, size_t* bytes) {
     DD_CHECK_ARG(p && bytes, "dd_plan_workspace_size: null pointer");
     DD_CHECK_ARG(nfield >= 1 && nfield <= 8, "nfield must be in [1, 8]");
-    DD_CHECK_ARG(precision == DD_FP64 || precision == DD_FP32, "precision must be DD_FP64 or DD_FP32");
-    *bytes = precision == DD_FP64 ? ws_bytes<double>(p, nfield) : ws_bytes<float>(p, nfield);
+    DD_CHECK_ARG(precision >= DD_FP64 && precision <= DD_DF64, "precision must be DD_FP64, DD_FP32 or DD_DF64");
+    DD_PREC_DISPATCH(precision, T, *bytes = ws_bytes<T>(p, nfield));
     return DD_OK;
 }
 
@@ -284,9 +162,10 @@ int dd_fft_r2c(const dd_plan* p, int nfield, const double* const* x, void* const
     DD_CHECK_ARG(p && x && k && work, "dd_fft_r2c: null pointer");
     DD_CHECK_ARG(nfield >= 1 && nfield <= 8, "nfield must be in [1, 8]");
     for (int f = 0; f < nfield; f++) DD_CHECK_ARG(x[f] && k[f], "dd_fft_r2c: null field pointer %d", f);
-    if (precision == DD_FP64) return fft_r2c<double>(p, nfield, x, k, work, work_bytes, (cudaStream_t)stream);
-    if (precision == DD_FP32) return fft_r2c<float>(p, nfield, x, k, work, work_bytes, (cudaStream_t)stream);
-    DD_CHECK_ARG(false, "precision must be DD_FP64 or DD_FP32");
+    DD_CHECK_ARG(precision >= DD_FP64 && precision <= DD_DF64, "precision must be DD_FP64, DD_FP32 or DD_DF64");
+    DD_CHECK_SUPPORTED(precision != DD_DF64, "the standalone transforms run in FP64 or FP32");
+    DD_PREC_DISPATCH_2(precision, T, return fft_r2c<T>(p, nfield, x, k, work, work_bytes, (cudaStream_t)stream));
+    return DD_OK;
 }
 
 int dd_fft_c2r(const dd_plan* p, int nfield, const void* const* k, double* const* x, int precision,
@@ -294,9 +173,10 @@ int dd_fft_c2r(const dd_plan* p, int nfield, const void* const* k, double* const
     DD_CHECK_ARG(p && x && k && work, "dd_fft_c2r: null pointer");
     DD_CHECK_ARG(nfield >= 1 && nfield <= 8, "nfield must be in [1, 8]");
     for (int f = 0; f < nfield; f++) DD_CHECK_ARG(x[f] && k[f], "dd_fft_c2r: null field pointer %d", f);
-    if (precision == DD_FP64) return fft_c2r<double>(p, nfield, k, x, work, work_bytes, (cudaStream_t)stream);
-    if (precision == DD_FP32) return fft_c2r<float>(p, nfield, k, x, work, work_bytes, (cudaStream_t)stream);
-    DD_CHECK_ARG(false, "precision must be DD_FP64 or DD_FP32");
+    DD_CHECK_ARG(precision >= DD_FP64 && precision <= DD_DF64, "precision must be DD_FP64, DD_FP32 or DD_DF64");
+    DD_CHECK_SUPPORTED(precision != DD_DF64, "the standalone transforms run in FP64 or FP32");
+    DD_PREC_DISPATCH_2(precision, T, return fft_c2r<T>(p, nfield, k, x, work, work_bytes, (cudaStream_t)stream));
+    return DD_OK;
 }
 
 int dd_dealias(const dd_plan* p, void* k, void* stream) {

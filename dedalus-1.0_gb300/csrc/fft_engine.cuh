@@ -14,6 +14,7 @@
 // Forward transforms use exp(-i...), inverse exp(+i...); neither is scaled.
 #pragma once
 #include "dd_common.cuh"
+#include "df64.cuh"
 
 namespace dd {
 
@@ -42,8 +43,8 @@ __device__ __forceinline__ C<T> tw_const(C<T> v) {
                                       -1, -DD_C8, -DD_R2, -DD_S8, 0, DD_S8, DD_R2, DD_C8};
         constexpr double ang_s[16] = {0, DD_S8, DD_R2, DD_C8, 1, DD_C8, DD_R2, DD_S8,
                                       0, -DD_S8, -DD_R2, -DD_C8, -1, -DD_C8, -DD_R2, -DD_S8};
-        const T c = T(ang_c[m16]);
-        const T s = INV ? T(ang_s[m16]) : T(-ang_s[m16]);
+        constexpr T c = T(ang_c[m16]);
+        constexpr T s = INV ? T(ang_s[m16]) : T(-ang_s[m16]);
         return mk<T>(v.x * c - v.y * s, v.x * s + v.y * c);
     }
 }

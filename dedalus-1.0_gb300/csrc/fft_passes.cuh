@@ -62,7 +62,7 @@ int launch_pass(const Op& op, int npencil, int nslow, int nfield, cudaStream_t s
         return DD_ERR_UNSUPPORTED;
     }
     dim3 grid(cdiv(npencil, P) * nfield, nslow > 65535 ? 65535 : nslow, nslow > 65535 ? nslow / 65535 : 1);
-    static const std::string label = std::string(Op::name) + "_" + std::to_string(L) + (sizeof(T) == 8 ? "_f64" : "_f32");
+    static const std::string label = std::string(Op::name) + "_" + std::to_string(L) + PrecName<T>::s;
     DD_KT(label.c_str(), st, kern<<<grid, NT, smem, st>>>(op, nfield));
     DD_LAUNCH_CHECK();
     return DD_OK;
@@ -74,6 +74,7 @@ template <typename T, typename KT>
 struct OpZInv3 {
     using V = typename Vec2<T>::type;
     static constexpr const char* name = "z_inv";
+    static constexpr int lmin = 8, lmax = 512;
     using KV = typename Vec2<KT>::type;
     Geo3 g; CPtrs in; Ptrs out; const V* tw;
     __device__ int npencil() const { return g.Kx; }
@@ -94,6 +95,7 @@ template <typename T>
 struct OpYInv3 {
     using V = typename Vec2<T>::type;
     static constexpr const char* name = "y_inv";
+    static constexpr int lmin = 8, lmax = 512;
     Geo3 g; CPtrs in; Ptrs out; const V* tw;
     __device__ int npencil() const { return g.Kx; }
     __device__ int nstore() const { return g.Ny; }
@@ -136,6 +138,7 @@ template <typename T, typename XT>
 struct OpXc2r3 {
     using V = typename Vec2<T>::type;
     static constexpr const char* name = "x_c2r";
+    static constexpr int lmin = 8, lmax = 512;
     int nrows, Nx, Kx; CPtrs in; Ptrs out; const V* tw;
     __device__ int npencil() const { return (nrows + 1) / 2; }
     __device__ int nstore() const { return Nx; }
@@ -160,6 +163,7 @@ template <typename T, typename XT>
 struct OpXr2c3 {
     using V = typename Vec2<T>::type;
     static constexpr const char* name = "x_r2c";
+    static constexpr int lmin = 8, lmax = 512;
     int nrows, Nx, Kx; T s; CPtrs in; Ptrs out; const V* tw;
     __device__ int npencil() const { return (nrows + 1) / 2; }
     __device__ int nstore() const { return Kx; }
@@ -183,6 +187,7 @@ template <typename T>
 struct OpYFwd3 {
     using V = typename Vec2<T>::type;
     static constexpr const char* name = "y_fwd";
+    static constexpr int lmin = 8, lmax = 512;
     Geo3 g; CPtrs in; Ptrs out; const V* tw;
     __device__ int npencil() const { return g.Kx; }
     __device__ int nstore() const { return g.Ny; }
@@ -202,6 +207,7 @@ template <typename T, typename KT>
 struct OpZFwd3 {
     using V = typename Vec2<T>::type;
     static constexpr const char* name = "z_fwd";
+    static constexpr int lmin = 8, lmax = 512;
     using KV = typename Vec2<KT>::type;
     Geo3 g; CPtrs in; Ptrs out; const V* tw;
     __device__ int npencil() const { return g.Kx; }
@@ -224,6 +230,7 @@ template <typename T, typename KT>
 struct OpYInv2 {
     using V = typename Vec2<T>::type;
     static constexpr const char* name = "y_inv2d";
+    static constexpr int lmin = 8, lmax = 512;
     using KV = typename Vec2<KT>::type;
     Geo2 g; CPtrs in; Ptrs out; const V* tw;
     __device__ int npencil() const { return g.Kx; }
@@ -243,6 +250,7 @@ template <typename T, typename KT>
 struct OpYFwd2 {
     using V = typename Vec2<T>::type;
     static constexpr const char* name = "y_fwd2d";
+    static constexpr int lmin = 8, lmax = 512;
     using KV = typename Vec2<KT>::type;
     Geo2 g; CPtrs in; Ptrs out; const V* tw;
     __device__ int npencil() const { return g.Kx; }

@@ -16,6 +16,7 @@ struct dd_plan {
     // twiddle tables W_L^m, m < L, per axis length (device), fp64 and fp32
     double2* tw64_x; double2* tw64_y; double2* tw64_z;
     float2* tw32_x;  float2* tw32_y;  float2* tw32_z;
+    float4* twdf_x;  float4* twdf_y;  float4* twdf_z;   // double-float (hi, lo) pairs
     // rounded-down 1/N_total used by the forward transform
     double inv_n;
 };
@@ -33,6 +34,28 @@ template <> struct TwSel<float> {
     static const float2* y(const dd_plan* p) { return p->tw32_y; }
     static const float2* z(const dd_plan* p) { return p->tw32_z; }
 };
+
+template <> struct TwSel<df64> {
+    static const float4* x(const dd_plan* p) { return p->twdf_x; }
+    static const float4* y(const dd_plan* p) { return p->twdf_y; }
+    static const float4* z(const dd_plan* p) { return p->twdf_z; }
+};
+
+// Run `body` with T bound to the arithmetic type of precision code `prec`
+// (DD_FP64 -> double, DD_FP32 -> float, DD_DF64 -> df64).
+#define DD_PREC_DISPATCH(prec, T, ...)                                 \
+    do {                                                               \
+        if ((prec) == DD_FP64) { using T = double; __VA_ARGS__; }       \
+        else if ((prec) == DD_FP32) { using T = float; __VA_ARGS__; }   \
+        else { using T = ::dd::df64; __VA_ARGS__; }                     \
+    } while (0)
+
+// Same for FP64 / FP32 only.
+#define DD_PREC_DISPATCH_2(prec, T, ...)                               \
+    do {                                                               \
+        if ((prec) == DD_FP64) { using T = double; __VA_ARGS__; }       \
+        else { using T = float; __VA_ARGS__; }                          \
+    } while (0)
 
 // Dispatch a pass on a runtime length.
 template <typename T, bool INV, bool LD_E, bool ST_E, class Op>

@@ -1,125 +1,13 @@
-// Fused 3D right-hand sides and RK4 step for incompressible hydro and MHD.
-//
-//   hydro: RHS(u) = P[u x w]^, w = curl u                  (physics.py:527-599)
-//   MHD:   RHS(u) = P[u x w + (J x B) / (4 pi rho0)]^, J = curl B,
-//          RHS(B) = curl (u x B)^                            (physics.py:770-819)
-// The rotational form u x w equals the reference's -(u.grad)u on the kept
-// modes to roundoff: the difference is a gradient, which the projection
-// removes, and products of dealiased fields alias only onto non-kept modes.
-// The Lorentz term is added in x-space before the forward transform (one
-// transform per component instead of two; equal by linearity).
-//
-// Passes (all pruned to the kept modes; T = FP64 or FP32 arithmetic):
-//   1  Z^-1 of each vector field and its curl (formed while loading)
-//   2  Y^-1
-//   3  X c2r -> pointwise products -> X r2c, scaled by 1/N   (k_x_prod)
-//   4  Y forward, kept ky only
-//   5  Z forward, kept kz only, into a compact [kyc][kzc][kx] buffer
-//   6  projection (physics.py:588-599, laplace_solve 407-416) and, for B,
-//      the spectral curl (physics.py:394-396), fused with the RK4 stage.
-#include "launch_len.cuh"
-#include "xprod.cuh"
-#include "etd.cuh"
+// Fused 3D right-hand sides and RK4 step: projection/stage kernels, drivers and
+// the C ABI.  The transform passes and their instantiations are in
+// rhs3d_impl.cuh / rhs3d_<precision>.cu.
+#include "rhs3d_impl.cuh"
 
 namespace dd {
 
-enum { P3_HYDRO = 0, P3_MHD = 1 };
-template <int PH> struct Phys3;
-template <> struct Phys3<P3_HYDRO> { static constexpr int NG = 1, NF = 3, NI = 6, NO = 3; };
-template <> struct Phys3<P3_MHD>   { static constexpr int NG = 2, NF = 6, NI = 12, NO = 6; };
-static_assert(Phys3<P3_MHD>::NI <= DD_MAXF, "too many transform fields for Ptrs");
-
-// a * (1j * k) as numpy computes it (representations.py:423)
-__device__ __forceinline__ double2 ideriv(double2 a, double k) { return make_double2(-(a.y * k), a.x * k); }
-
-// ------------------------------------------------------------------ pass 1
-// Field f: group g = f / 6 (vector field g of the state), j = f % 6:
-// j < 3 -> component j; j >= 3 -> component j - 3 of its curl (curlX,
-// physics.py:394-396: (d_y X_z - d_z X_y, d_z X_x - d_x X_z, d_x X_y - d_y X_x)).
-// The state is read from the full reference layout [ky][kz][kx] or from the
-// compact kept layout [kyc][kzc][kx] used for RK stage states.
-template <typename T, bool COMPACT, int NG>
-struct OpZInvCurl3 {
-    using V = typename Vec2<T>::type;
-    static constexpr const char* name = NG == 1 ? "z_inv_curl" : "z_inv_curl_mhd";
-    Geo3 g; CPtrs u; Ptrs out; const V* tw;
-    const double* kx; const double* ky; const double* kz;
-    __device__ int npencil() const { return g.Kx; }
-    __device__ int nstore() const { return g.Nz; }
-    __device__ double2 get(int c, int kyc, int ky_i, int e, int ix) const {
-        const double2* U = (const double2*)u.p[c];
-        if (COMPACT) return U[((int64_t)kyc * g.Kz + full_to_compact(e, g.Nz, g.Kz)) * g.Kx + ix];
-        return U[((int64_t)ky_i * g.Nz + e) * g.Nh + ix];
-    }
-    __device__ C<T> load(int fld, int kyc, int e, int ix) const {
-        if (!kept_full(e, g.Nz, g.Mz)) return zero<T>();
-        const int ky_i = compact_to_full(kyc, g.Ny, g.Ky);
-        const int grp = fld / 6, j = fld % 6, c0 = 3 * grp;
-        double2 r;
-        if (j < 3) {
-            r = get(c0 + j, kyc, ky_i, e, ix);
-        } else {
-            const double kxv = kx[ix], kyv = ky[ky_i], kzv = kz[e];
-            double2 a, b;
-            if (j == 3) { a = ideriv(get(c0 + 2, kyc, ky_i, e, ix), kyv); b = ideriv(get(c0 + 1, kyc, ky_i, e, ix), kzv); }
-            else if (j == 4) { a = ideriv(get(c0 + 0, kyc, ky_i, e, ix), kzv); b = ideriv(get(c0 + 2, kyc, ky_i, e, ix), kxv); }
-            else { a = ideriv(get(c0 + 1, kyc, ky_i, e, ix), kxv); b = ideriv(get(c0 + 0, kyc, ky_i, e, ix), kyv); }
-            r = make_double2(a.x - b.x, a.y - b.y);
-        }
-        return mk<T>((T)r.x, (T)r.y);
-    }
-    __device__ void store(int fld, int kyc, int e, int ix, const C<T>* col, int PS) const {
-        stc<T>((V*)out.p[fld] + ((int64_t)kyc * g.Nz + e) * g.Kx + ix, col[e * PS]);
-    }
-};
-
-// ------------------------------------------------------------------ pass 3
-template <typename T>
-struct ProdHydro3 {
-    static constexpr int NI = 6, NO = 3;
-    __device__ void operator()(const T* in, T* out, int) const {
-        const T ux = in[0], uy = in[1], uz = in[2], wx = in[3], wy = in[4], wz = in[5];
-        out[0] = uy * wz - uz * wy;
-        out[1] = uz * wx - ux * wz;
-        out[2] = ux * wy - uy * wx;
-    }
-};
-
-// in: u, w, B, J;  out: u x w + (J x B) / (4 pi rho0), u x B  (physics.py:795-815)
-template <typename T>
-struct ProdMHD3 {
-    static constexpr int NI = 12, NO = 6;
-    T inv_fpr;
-    __device__ void operator()(const T* in, T* out, int) const {
-        const T ux = in[0], uy = in[1], uz = in[2], wx = in[3], wy = in[4], wz = in[5];
-        const T bx = in[6], by = in[7], bz = in[8], jx = in[9], jy = in[10], jz = in[11];
-        out[0] = (uy * wz - uz * wy) + (jy * bz - jz * by) * inv_fpr;
-        out[1] = (uz * wx - ux * wz) + (jz * bx - jx * bz) * inv_fpr;
-        out[2] = (ux * wy - uy * wx) + (jx * by - jy * bx) * inv_fpr;
-        out[3] = uy * bz - uz * by;
-        out[4] = uz * bx - ux * bz;
-        out[5] = ux * by - uy * bx;
-    }
-};
-
-// ------------------------------------------------------------------ pass 5
-template <typename T>
-struct OpZFwdCompact3 {
-    using V = typename Vec2<T>::type;
-    static constexpr const char* name = "z_fwd_compact";
-    Geo3 g; CPtrs in; Ptrs out; const V* tw;
-    __device__ int npencil() const { return g.Kx; }
-    __device__ int nstore() const { return g.Nz; }
-    __device__ C<T> load(int fld, int kyc, int e, int kx) const {
-        return ldc<T>((const V*)in.p[fld] + ((int64_t)kyc * g.Nz + e) * g.Kx + kx);
-    }
-    __device__ void store(int fld, int kyc, int e, int kx, const C<T>* col, int PS) const {
-        if (!kept_full(e, g.Nz, g.Mz)) return;
-        const C<T> c = col[e * PS];
-        ((double2*)out.p[fld])[((int64_t)kyc * g.Kz + full_to_compact(e, g.Nz, g.Kz)) * g.Kx + kx] =
-            make_double2((double)c.x, (double)c.y);
-    }
-};
+DD_RHS3D_INSTANTIATE(extern, double)
+DD_RHS3D_INSTANTIATE(extern, float)
+DD_RHS3D_INSTANTIATE_PH(extern, df64, P3_HYDRO)
 
 // ------------------------------------------------------------------ pass 6
 struct ProjArgs {
@@ -324,74 +212,41 @@ static unsigned ew_grid(int64_t n) {
     return (unsigned)(b < 1 ? 1 : b);
 }
 
-// ------------------------------------------------------------ drivers
-// workspace: W1 (NI fields), W2 (NI), NC (NO, complex128), then for the RK4
-// step tot (NF) and the stage state (NF), both compact complex128.
-struct Work3 {
-    size_t w1, w2, kc;
-    int ni, no, nf;
-    char* base;
-    template <typename T> C<T>* W1(int f) const { return (C<T>*)base + f * w1; }
-    template <typename T> C<T>* W2(int f) const { return (C<T>*)base + ni * w1 + f * w2; }
-    // transform intermediates first, then the complex128 regions from a
-    // 256-byte boundary
-    static size_t up256(size_t b) { return (b + 255) & ~(size_t)255; }
-    template <typename T> double2* NC(int f) const {
-        return (double2*)((char*)base + up256(sizeof(C<T>) * ni * (w1 + w2))) + f * kc;
-    }
-    template <typename T> double2* TOT(int f) const { return NC<T>(no) + f * kc; }
-    template <typename T> double2* YS(int f) const { return NC<T>(no + nf) + f * kc; }
-    template <typename T> static size_t bytes(const Geo3& g, int ni, int no, int nf, bool step) {
-        const size_t kc = (size_t)g.Ky * g.Kz * g.Kx;
-        return up256(sizeof(C<T>) * ni * (size_t)(g.w1count() + g.w2count())) +
-               sizeof(double2) * kc * (no + (step ? 2 * nf : 0));
-    }
-};
-
-template <int PH>
-static Work3 make_work(const Geo3& g, void* base) {
-    using P = Phys3<PH>;
-    return Work3{(size_t)g.w1count(), (size_t)g.w2count(), (size_t)g.Ky * g.Kz * g.Kx, P::NI, P::NO, P::NF,
-                 (char*)base};
-}
-
-template <typename T, bool COMPACT, int PH>
-static int nonlinear3(const dd_plan* pl, const void* const* u, double inv_fpr, const Work3& w, cudaStream_t st) {
-    using P = Phys3<PH>;
-    const Geo3& g = pl->g3;
-    CPtrs uin{}; Ptrs w1{}, w2{}, nc{}; CPtrs w1c{}, w2c{};
-    for (int c = 0; c < P::NF; c++) uin.p[c] = u[c];
-    for (int c = 0; c < P::NO; c++) nc.p[c] = w.NC<T>(c);
-    for (int f = 0; f < P::NI; f++) {
-        w1.p[f] = w.W1<T>(f); w1c.p[f] = w1.p[f];
-        w2.p[f] = w.W2<T>(f); w2c.p[f] = w2.p[f];
-    }
-    OpZInvCurl3<T, COMPACT, P::NG> a{g, uin, w1, TwSel<T>::z(pl), pl->kx, pl->ky, pl->kz};
-    DD_TRY((launch_pass_len<T, true, false, false>(g.Nz, a, g.Kx, g.Ky, P::NI, st)));
-    OpYInv3<T> b{g, w1c, w2, TwSel<T>::y(pl)};
-    DD_TRY((launch_pass_len<T, true, false, false>(g.Ny, b, g.Kx, g.Nz, P::NI, st)));
-    // products overwrite fields 0..NO-1 of W2 row by row (each block reads its rows first)
-    if constexpr (PH == P3_HYDRO) {
-        DD_TRY((launch_x_prod_len<T>("x_cross", g.Nx, g.Nz * g.Ny, g.Kx, w2c, w2, 1, 0, 0, TwSel<T>::x(pl),
-                                     (T)pl->inv_n, ProdHydro3<T>{}, st)));
-    } else {
-        DD_TRY((launch_x_prod_len<T>("x_cross_mhd", g.Nx, g.Nz * g.Ny, g.Kx, w2c, w2, 1, 0, 0, TwSel<T>::x(pl),
-                                     (T)pl->inv_n, ProdMHD3<T>{(T)inv_fpr}, st)));
-    }
-    OpYFwd3<T> d{g, w2c, w1, TwSel<T>::y(pl)};
-    DD_TRY((launch_pass_len<T, false, false, false>(g.Ny, d, g.Kx, g.Nz, P::NO, st)));
-    OpZFwdCompact3<T> e{g, w1c, nc, TwSel<T>::z(pl)};
-    DD_TRY((launch_pass_len<T, false, false, false>(g.Nz, e, g.Kx, g.Ky, P::NO, st)));
-    return DD_OK;
-}
-
 template <int PH>
 static int nonlinear3_any(const dd_plan* pl, int prec, bool compact, const void* const* u, double inv_fpr,
                           const Work3& w, cudaStream_t st) {
     if (prec == DD_FP64) return compact ? nonlinear3<double, true, PH>(pl, u, inv_fpr, w, st)
                                         : nonlinear3<double, false, PH>(pl, u, inv_fpr, w, st);
-    return compact ? nonlinear3<float, true, PH>(pl, u, inv_fpr, w, st)
-                   : nonlinear3<float, false, PH>(pl, u, inv_fpr, w, st);
+    if (prec == DD_FP32) return compact ? nonlinear3<float, true, PH>(pl, u, inv_fpr, w, st)
+                                        : nonlinear3<float, false, PH>(pl, u, inv_fpr, w, st);
+    if constexpr (PH == P3_HYDRO) {
+        return compact ? nonlinear3<df64, true, PH>(pl, u, inv_fpr, w, st)
+                       : nonlinear3<df64, false, PH>(pl, u, inv_fpr, w, st);
+    }
+    set_error("double-float arithmetic is implemented for 3D hydro only");
+    return DD_ERR_UNSUPPORTED;
+}
+
+// Workspace bytes and compact-region pointers for precision code prec.
+static size_t work3_bytes(int prec, const Geo3& g, int ni, int no, int nf, bool step) {
+    size_t b = 0;
+    DD_PREC_DISPATCH(prec, T, b = Work3::bytes<T>(g, ni, no, nf, step));
+    return b;
+}
+static void* work3_nc(int prec, const Work3& w, int f) {
+    void* p = nullptr;
+    DD_PREC_DISPATCH(prec, T, p = (void*)w.NC<T>(f));
+    return p;
+}
+static void* work3_tot(int prec, const Work3& w, int f) {
+    void* p = nullptr;
+    DD_PREC_DISPATCH(prec, T, p = (void*)w.TOT<T>(f));
+    return p;
+}
+static void* work3_ys(int prec, const Work3& w, int f) {
+    void* p = nullptr;
+    DD_PREC_DISPATCH(prec, T, p = (void*)w.YS<T>(f));
+    return p;
 }
 
 // 1 / (4 pi rho0): fpr = 4 * np.pi * rho0 (physics.py:791); numpy divides a
@@ -403,15 +258,14 @@ static int rhs3(const dd_plan* p, const double* params, const void* const* u, vo
                 const double* inv_k2, int prec, int zero_nonkept, void* work, size_t wb, cudaStream_t st) {
     using P = Phys3<PH>;
     const Geo3& g = p->g3;
-    const size_t need = prec == DD_FP32 ? Work3::bytes<float>(g, P::NI, P::NO, P::NF, false)
-                                        : Work3::bytes<double>(g, P::NI, P::NO, P::NF, false);
+    const size_t need = work3_bytes(prec, g, P::NI, P::NO, P::NF, false);
     DD_CHECK_ARG(wb >= need, "workspace too small: %zu < %zu", wb, need);
     const double inv_fpr = PH == P3_MHD ? inv_fpr_of(params) : 0.;
     Work3 w = make_work<PH>(g, work);
     DD_TRY(nonlinear3_any<PH>(p, prec, false, u, inv_fpr, w, st));
     ProjArgs pa{g, p->kx, p->ky, p->kz, inv_k2, inv_k2 != nullptr};
     CPtrs nc{}; Ptrs d{};
-    for (int c = 0; c < P::NO; c++) nc.p[c] = prec == DD_FP64 ? (void*)w.NC<double>(c) : (void*)w.NC<float>(c);
+    for (int c = 0; c < P::NO; c++) nc.p[c] = work3_nc(prec, w, c);
     for (int c = 0; c < P::NF; c++) d.p[c] = deriv[c];
     if (zero_nonkept) {
         DD_KT("zero_nonkept3", st, k_dealias3_all<<<dim3(ew_grid(g.kcount()), P::NF), 256, 0, st>>>(g, d));
@@ -428,8 +282,7 @@ static int rk4_3(const dd_plan* p, const double* params, void* const* u, const d
                  int prec, const int* nonkept_flag, void* work, size_t wb, cudaStream_t st) {
     using P = Phys3<PH>;
     const Geo3& g = p->g3;
-    const size_t need = prec == DD_FP32 ? Work3::bytes<float>(g, P::NI, P::NO, P::NF, true)
-                                        : Work3::bytes<double>(g, P::NI, P::NO, P::NF, true);
+    const size_t need = work3_bytes(prec, g, P::NI, P::NO, P::NF, true);
     DD_CHECK_ARG(wb >= need, "workspace too small: %zu < %zu", wb, need);
     const bool intk = inv_k2 != nullptr;
     DD_CHECK_ARG(!intk || (tab_half && tab_full), "phi tables required with integer wavenumbers");
@@ -440,11 +293,11 @@ static int rk4_3(const dd_plan* p, const double* params, void* const* u, const d
     a.vo = vo;
     for (int grp = 0; grp < P::NG; grp++) a.coeff[grp] = coeff[grp];
     const void* ysc[6] = {};
-    for (int c = 0; c < P::NO; c++) a.nc.p[c] = prec == DD_FP64 ? (void*)w.NC<double>(c) : (void*)w.NC<float>(c);
+    for (int c = 0; c < P::NO; c++) a.nc.p[c] = work3_nc(prec, w, c);
     for (int c = 0; c < P::NF; c++) {
         a.y.p[c] = u[c];
-        a.ys.p[c] = prec == DD_FP64 ? (void*)w.YS<double>(c) : (void*)w.YS<float>(c);
-        a.tot.p[c] = prec == DD_FP64 ? (void*)w.TOT<double>(c) : (void*)w.TOT<float>(c);
+        a.ys.p[c] = work3_ys(prec, w, c);
+        a.tot.p[c] = work3_tot(prec, w, c);
         ysc[c] = a.ys.p[c];
     }
     const double hs[4] = {dt / 2., dt / 2., dt, dt};
@@ -489,8 +342,8 @@ int dd_rhs3d_workspace_size(const dd_plan* p, int physics, int precision, size_t
     DD_CHECK_ARG(p && bytes && p->ndim == 3, "dd_rhs3d_workspace_size: bad arguments");
     DD_CHECK_ARG(physics == P3_HYDRO || physics == P3_MHD, "physics must be 0 (hydro) or 1 (MHD)");
     const int ni = physics == P3_HYDRO ? 6 : 12, no = ni / 2, nf = no;
-    *bytes = precision == DD_FP32 ? Work3::bytes<float>(p->g3, ni, no, nf, true)
-                                  : Work3::bytes<double>(p->g3, ni, no, nf, true);
+    DD_CHECK_ARG(precision >= DD_FP64 && precision <= DD_DF64, "bad precision");
+    *bytes = work3_bytes(precision, p->g3, ni, no, nf, true);
     return DD_OK;
 }
 
@@ -498,7 +351,7 @@ int dd_rhs3d(const dd_plan* p, int physics, const double* params, const void* co
              const double* inv_k2, int precision, int zero_nonkept, void* work, size_t work_bytes, void* stream) {
     DD_TRY(check3(p, physics, params, state, (const void* const*)deriv));
     DD_CHECK_ARG(work, "null workspace");
-    DD_CHECK_ARG(precision == DD_FP64 || precision == DD_FP32, "bad precision");
+    DD_CHECK_ARG(precision >= DD_FP64 && precision <= DD_DF64, "bad precision");
     cudaStream_t st = (cudaStream_t)stream;
     if (physics == P3_HYDRO)
         return rhs3<P3_HYDRO>(p, params, state, deriv, inv_k2, precision, zero_nonkept, work, work_bytes, st);
@@ -511,7 +364,7 @@ int dd_rk4_step3d(const dd_plan* p, int physics, const double* params, void* con
                   size_t work_bytes, void* stream) {
     DD_TRY(check3(p, physics, params, (const void* const*)state, nullptr));
     DD_CHECK_ARG(work && coeff, "null workspace or coefficients");
-    DD_CHECK_ARG(precision == DD_FP64 || precision == DD_FP32, "bad precision");
+    DD_CHECK_ARG(precision >= DD_FP64 && precision <= DD_DF64, "bad precision");
     DD_CHECK_ARG(viscosity_order >= 1, "viscosity_order must be >= 1");
     cudaStream_t st = (cudaStream_t)stream;
     if (physics == P3_HYDRO)

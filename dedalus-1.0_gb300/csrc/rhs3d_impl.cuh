@@ -1,0 +1,199 @@
+#pragma once
+// Fused 3D right-hand sides and RK4 step for incompressible hydro and MHD.
+//
+//   hydro: RHS(u) = P[u x w]^, w = curl u                  (physics.py:527-599)
+//   MHD:   RHS(u) = P[u x w + (J x B) / (4 pi rho0)]^, J = curl B,
+//          RHS(B) = curl (u x B)^                            (physics.py:770-819)
+// The rotational form u x w equals the reference's -(u.grad)u on the kept
+// modes to roundoff: the difference is a gradient, which the projection
+// removes, and products of dealiased fields alias only onto non-kept modes.
+// The Lorentz term is added in x-space before the forward transform (one
+// transform per component instead of two; equal by linearity).
+//
+// Passes (all pruned to the kept modes; T = FP64 or FP32 arithmetic):
+//   1  Z^-1 of each vector field and its curl (formed while loading)
+//   2  Y^-1
+//   3  X c2r -> pointwise products -> X r2c, scaled by 1/N   (k_x_prod)
+//   4  Y forward, kept ky only
+//   5  Z forward, kept kz only, into a compact [kyc][kzc][kx] buffer
+//   6  projection (physics.py:588-599, laplace_solve 407-416) and, for B,
+//      the spectral curl (physics.py:394-396), fused with the RK4 stage.
+#include "launch_len.cuh"
+#include "xprod.cuh"
+#include "etd.cuh"
+
+namespace dd {
+
+enum { P3_HYDRO = 0, P3_MHD = 1 };
+template <int PH> struct Phys3;
+template <> struct Phys3<P3_HYDRO> { static constexpr int NG = 1, NF = 3, NI = 6, NO = 3; };
+template <> struct Phys3<P3_MHD>   { static constexpr int NG = 2, NF = 6, NI = 12, NO = 6; };
+static_assert(Phys3<P3_MHD>::NI <= DD_MAXF, "too many transform fields for Ptrs");
+
+// a * (1j * k) as numpy computes it (representations.py:423)
+__device__ __forceinline__ double2 ideriv(double2 a, double k) { return make_double2(-(a.y * k), a.x * k); }
+
+// ------------------------------------------------------------------ pass 1
+// Field f: group g = f / 6 (vector field g of the state), j = f % 6:
+// j < 3 -> component j; j >= 3 -> component j - 3 of its curl (curlX,
+// physics.py:394-396: (d_y X_z - d_z X_y, d_z X_x - d_x X_z, d_x X_y - d_y X_x)).
+// The state is read from the full reference layout [ky][kz][kx] or from the
+// compact kept layout [kyc][kzc][kx] used for RK stage states.
+template <typename T, bool COMPACT, int NG>
+struct OpZInvCurl3 {
+    using V = typename Vec2<T>::type;
+    static constexpr const char* name = NG == 1 ? "z_inv_curl" : "z_inv_curl_mhd";
+    static constexpr int lmin = 16, lmax = 256;
+    Geo3 g; CPtrs u; Ptrs out; const V* tw;
+    const double* kx; const double* ky; const double* kz;
+    __device__ int npencil() const { return g.Kx; }
+    __device__ int nstore() const { return g.Nz; }
+    __device__ double2 get(int c, int kyc, int ky_i, int e, int ix) const {
+        const double2* U = (const double2*)u.p[c];
+        if (COMPACT) return U[((int64_t)kyc * g.Kz + full_to_compact(e, g.Nz, g.Kz)) * g.Kx + ix];
+        return U[((int64_t)ky_i * g.Nz + e) * g.Nh + ix];
+    }
+    __device__ C<T> load(int fld, int kyc, int e, int ix) const {
+        if (!kept_full(e, g.Nz, g.Mz)) return zero<T>();
+        const int ky_i = compact_to_full(kyc, g.Ny, g.Ky);
+        const int grp = fld / 6, j = fld % 6, c0 = 3 * grp;
+        double2 r;
+        if (j < 3) {
+            r = get(c0 + j, kyc, ky_i, e, ix);
+        } else {
+            const double kxv = kx[ix], kyv = ky[ky_i], kzv = kz[e];
+            double2 a, b;
+            if (j == 3) { a = ideriv(get(c0 + 2, kyc, ky_i, e, ix), kyv); b = ideriv(get(c0 + 1, kyc, ky_i, e, ix), kzv); }
+            else if (j == 4) { a = ideriv(get(c0 + 0, kyc, ky_i, e, ix), kzv); b = ideriv(get(c0 + 2, kyc, ky_i, e, ix), kxv); }
+            else { a = ideriv(get(c0 + 1, kyc, ky_i, e, ix), kxv); b = ideriv(get(c0 + 0, kyc, ky_i, e, ix), kyv); }
+            r = make_double2(a.x - b.x, a.y - b.y);
+        }
+        return mk<T>((T)r.x, (T)r.y);
+    }
+    __device__ void store(int fld, int kyc, int e, int ix, const C<T>* col, int PS) const {
+        stc<T>((V*)out.p[fld] + ((int64_t)kyc * g.Nz + e) * g.Kx + ix, col[e * PS]);
+    }
+};
+
+// ------------------------------------------------------------------ pass 3
+template <typename T>
+struct ProdHydro3 {
+    static constexpr int NI = 6, NO = 3;
+    static constexpr int lmin = 16, lmax = 256;
+    __device__ void operator()(const T* in, T* out, int) const {
+        const T ux = in[0], uy = in[1], uz = in[2], wx = in[3], wy = in[4], wz = in[5];
+        out[0] = uy * wz - uz * wy;
+        out[1] = uz * wx - ux * wz;
+        out[2] = ux * wy - uy * wx;
+    }
+};
+
+// in: u, w, B, J;  out: u x w + (J x B) / (4 pi rho0), u x B  (physics.py:795-815)
+template <typename T>
+struct ProdMHD3 {
+    static constexpr int NI = 12, NO = 6;
+    static constexpr int lmin = 16, lmax = 256;
+    T inv_fpr;
+    __device__ void operator()(const T* in, T* out, int) const {
+        const T ux = in[0], uy = in[1], uz = in[2], wx = in[3], wy = in[4], wz = in[5];
+        const T bx = in[6], by = in[7], bz = in[8], jx = in[9], jy = in[10], jz = in[11];
+        out[0] = (uy * wz - uz * wy) + (jy * bz - jz * by) * inv_fpr;
+        out[1] = (uz * wx - ux * wz) + (jz * bx - jx * bz) * inv_fpr;
+        out[2] = (ux * wy - uy * wx) + (jx * by - jy * bx) * inv_fpr;
+        out[3] = uy * bz - uz * by;
+        out[4] = uz * bx - ux * bz;
+        out[5] = ux * by - uy * bx;
+    }
+};
+
+// ------------------------------------------------------------------ pass 5
+template <typename T>
+struct OpZFwdCompact3 {
+    using V = typename Vec2<T>::type;
+    static constexpr const char* name = "z_fwd_compact";
+    static constexpr int lmin = 16, lmax = 256;
+    Geo3 g; CPtrs in; Ptrs out; const V* tw;
+    __device__ int npencil() const { return g.Kx; }
+    __device__ int nstore() const { return g.Nz; }
+    __device__ C<T> load(int fld, int kyc, int e, int kx) const {
+        return ldc<T>((const V*)in.p[fld] + ((int64_t)kyc * g.Nz + e) * g.Kx + kx);
+    }
+    __device__ void store(int fld, int kyc, int e, int kx, const C<T>* col, int PS) const {
+        if (!kept_full(e, g.Nz, g.Mz)) return;
+        const C<T> c = col[e * PS];
+        ((double2*)out.p[fld])[((int64_t)kyc * g.Kz + full_to_compact(e, g.Nz, g.Kz)) * g.Kx + kx] =
+            make_double2((double)c.x, (double)c.y);
+    }
+};
+
+// ------------------------------------------------------------ drivers
+// workspace: W1 (NI fields), W2 (NI), NC (NO, complex128), then for the RK4
+// step tot (NF) and the stage state (NF), both compact complex128.
+struct Work3 {
+    size_t w1, w2, kc;
+    int ni, no, nf;
+    char* base;
+    template <typename T> C<T>* W1(int f) const { return (C<T>*)base + f * w1; }
+    template <typename T> C<T>* W2(int f) const { return (C<T>*)base + ni * w1 + f * w2; }
+    // transform intermediates first, then the complex128 regions from a
+    // 256-byte boundary
+    static size_t up256(size_t b) { return (b + 255) & ~(size_t)255; }
+    template <typename T> double2* NC(int f) const {
+        return (double2*)((char*)base + up256(sizeof(C<T>) * ni * (w1 + w2))) + f * kc;
+    }
+    template <typename T> double2* TOT(int f) const { return NC<T>(no) + f * kc; }
+    template <typename T> double2* YS(int f) const { return NC<T>(no + nf) + f * kc; }
+    template <typename T> static size_t bytes(const Geo3& g, int ni, int no, int nf, bool step) {
+        const size_t kc = (size_t)g.Ky * g.Kz * g.Kx;
+        return up256(sizeof(C<T>) * ni * (size_t)(g.w1count() + g.w2count())) +
+               sizeof(double2) * kc * (no + (step ? 2 * nf : 0));
+    }
+};
+
+template <int PH>
+static Work3 make_work(const Geo3& g, void* base) {
+    using P = Phys3<PH>;
+    return Work3{(size_t)g.w1count(), (size_t)g.w2count(), (size_t)g.Ky * g.Kz * g.Kx, P::NI, P::NO, P::NF,
+                 (char*)base};
+}
+
+template <typename T, bool COMPACT, int PH>
+int nonlinear3(const dd_plan* pl, const void* const* u, double inv_fpr, const Work3& w, cudaStream_t st) {
+    using P = Phys3<PH>;
+    const Geo3& g = pl->g3;
+    CPtrs uin{}; Ptrs w1{}, w2{}, nc{}; CPtrs w1c{}, w2c{};
+    for (int c = 0; c < P::NF; c++) uin.p[c] = u[c];
+    for (int c = 0; c < P::NO; c++) nc.p[c] = w.NC<T>(c);
+    for (int f = 0; f < P::NI; f++) {
+        w1.p[f] = w.W1<T>(f); w1c.p[f] = w1.p[f];
+        w2.p[f] = w.W2<T>(f); w2c.p[f] = w2.p[f];
+    }
+    OpZInvCurl3<T, COMPACT, P::NG> a{g, uin, w1, TwSel<T>::z(pl), pl->kx, pl->ky, pl->kz};
+    DD_TRY((launch_pass_len<T, true, false, false>(g.Nz, a, g.Kx, g.Ky, P::NI, st)));
+    OpYInv3<T> b{g, w1c, w2, TwSel<T>::y(pl)};
+    DD_TRY((launch_pass_len<T, true, false, false>(g.Ny, b, g.Kx, g.Nz, P::NI, st)));
+    // products overwrite fields 0..NO-1 of W2 row by row (each block reads its rows first)
+    if constexpr (PH == P3_HYDRO) {
+        DD_TRY((launch_x_prod_len<T>("x_cross", g.Nx, g.Nz * g.Ny, g.Kx, w2c, w2, 1, 0, 0, TwSel<T>::x(pl),
+                                     (T)pl->inv_n, ProdHydro3<T>{}, st)));
+    } else {
+        DD_TRY((launch_x_prod_len<T>("x_cross_mhd", g.Nx, g.Nz * g.Ny, g.Kx, w2c, w2, 1, 0, 0, TwSel<T>::x(pl),
+                                     (T)pl->inv_n, ProdMHD3<T>{(T)inv_fpr}, st)));
+    }
+    OpYFwd3<T> d{g, w2c, w1, TwSel<T>::y(pl)};
+    DD_TRY((launch_pass_len<T, false, false, false>(g.Ny, d, g.Kx, g.Nz, P::NO, st)));
+    OpZFwdCompact3<T> e{g, w1c, nc, TwSel<T>::z(pl)};
+    DD_TRY((launch_pass_len<T, false, false, false>(g.Nz, e, g.Kx, g.Ky, P::NO, st)));
+    return DD_OK;
+}
+
+// Explicit instantiations live in rhs3d_<precision>.cu, one translation unit
+// per arithmetic type, so the heavy transform kernels compile in parallel.
+#define DD_RHS3D_INSTANTIATE_PH(EXT, T, PH)                                                            \
+    EXT template int nonlinear3<T, false, PH>(const dd_plan*, const void* const*, double, const Work3&,     \
+                                              cudaStream_t);                                            \
+    EXT template int nonlinear3<T, true, PH>(const dd_plan*, const void* const*, double, const Work3&,      \
+                                             cudaStream_t);
+#define DD_RHS3D_INSTANTIATE(EXT, T) DD_RHS3D_INSTANTIATE_PH(EXT, T, P3_HYDRO) DD_RHS3D_INSTANTIATE_PH(EXT, T, P3_MHD)
+
+}  // namespace dd

@@ -12,7 +12,7 @@
 // are (row block, run): run b's fields start at win.p[f] + b * in_rs and
 // wout.p[g] + b * out_rs (complex entries).
 #pragma once
-#include "fft_passes.cuh"
+#include "launch_len.cuh"
 
 namespace dd {
 
@@ -165,7 +165,7 @@ int launch_x_prod(const char* name, int nrows, int Kx, const CPtrs& win, const P
         DD_CUDA(cudaFuncSetAttribute(k_x_prod<T, L, Op>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         configured = true;
     }
-    static const std::string label = std::string(name) + "_" + std::to_string(L) + (sizeof(T) == 8 ? "_f64" : "_f32");
+    static const std::string label = std::string(name) + "_" + std::to_string(L) + PrecName<T>::s;
     DD_KT(label.c_str(), st,
           k_x_prod<T, L, Op><<<dim3(cdiv(nrows, CC::Q), nrun), CC::NT, smem, st>>>(nrows, Kx, win, wout, in_rs, out_rs,
                                                                                   tw, scale, op));
@@ -178,16 +178,20 @@ int launch_x_prod_len(const char* name, int L, int nrows, int Kx, const CPtrs& w
                       int64_t in_rs, int64_t out_rs, const typename Vec2<T>::type* tw, T scale, const Op& op,
                       cudaStream_t st) {
     DD_CHECK_SUPPORTED(nrun >= 1 && nrun <= 65535, "run batch of %d not supported", nrun);
+#define DD_XP(N) (launch_x_prod<T, N>(name, nrows, Kx, win, wout, nrun, in_rs, out_rs, tw, scale, op, st))
     switch (L) {
-        case 8: return launch_x_prod<T, 8>(name, nrows, Kx, win, wout, nrun, in_rs, out_rs, tw, scale, op, st);
-        case 16: return launch_x_prod<T, 16>(name, nrows, Kx, win, wout, nrun, in_rs, out_rs, tw, scale, op, st);
-        case 32: return launch_x_prod<T, 32>(name, nrows, Kx, win, wout, nrun, in_rs, out_rs, tw, scale, op, st);
-        case 64: return launch_x_prod<T, 64>(name, nrows, Kx, win, wout, nrun, in_rs, out_rs, tw, scale, op, st);
-        case 128: return launch_x_prod<T, 128>(name, nrows, Kx, win, wout, nrun, in_rs, out_rs, tw, scale, op, st);
-        case 256: return launch_x_prod<T, 256>(name, nrows, Kx, win, wout, nrun, in_rs, out_rs, tw, scale, op, st);
-        case 512: return launch_x_prod<T, 512>(name, nrows, Kx, win, wout, nrun, in_rs, out_rs, tw, scale, op, st);
-        default: set_error("unsupported x length %d", L); return DD_ERR_UNSUPPORTED;
+        DD_LEN_CASE(8, DD_XP(8))
+        DD_LEN_CASE(16, DD_XP(16))
+        DD_LEN_CASE(32, DD_XP(32))
+        DD_LEN_CASE(64, DD_XP(64))
+        DD_LEN_CASE(128, DD_XP(128))
+        DD_LEN_CASE(256, DD_XP(256))
+        DD_LEN_CASE(512, DD_XP(512))
+        default: break;
     }
+#undef DD_XP
+    set_error("x length %d is not supported for %s%s", L, name, PrecName<T>::s);
+    return DD_ERR_UNSUPPORTED;
 }
 
 }  // namespace dd

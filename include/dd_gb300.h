@@ -37,6 +37,7 @@ extern "C" {
 
 #define DD_FP64 0
 #define DD_FP32 1
+#define DD_DF64 2  /* double-float: transforms on FP32 pipes, ~48-bit significands */
 
 typedef struct dd_plan dd_plan;
 

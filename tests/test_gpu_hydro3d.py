@@ -138,3 +138,46 @@ def test_fp32_path_error(dd, cuda):
         dd.config.decfg.set('FFT', 'precision', 'fp64')
     err = rel_l2(host_u(dg), [do['u'][i]['kspace'] for i in range(3)])
     assert err < 1e-5, err
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape", [(16, 16, 16), (32, 32, 32), (64, 64, 64)])
+def test_df64_rhs_and_rk4_match_oracle(dd, cuda, shape):
+    """Double-float transform arithmetic (FP32 pipes, ~48-bit significands)
+    meets the FP64 bar: <= 1e-12 relative L2 per RHS and per step."""
+    u0 = dd.init_cond.turbulence_3d(shape, seed=7)
+    ro, do = oracle_hydro(shape, 5e-3, u0)
+    dero = ro.create_fields(0.)
+    ro.RHS(do, dero)
+    ref_rhs = [dero['u'][i]['kspace'].copy() for i in range(3)]
+    ro2, do2 = oracle_hydro(shape, 5e-3, u0)
+    OT.RK4(ro2).do_advance(do2, 2e-3)
+    dd.config.decfg.set('FFT', 'precision', 'df64')
+    try:
+        rg, dg = gpu_hydro(dd, shape, 5e-3, u0)
+        derg = rg.create_fields(0.)
+        rg.RHS(dg, derg)
+        e_rhs = rel_l2(host_u(derg), ref_rhs)
+        rg2, dg2 = gpu_hydro(dd, shape, 5e-3, u0)
+        dd.mods.RK4(rg2).do_advance(dg2, 2e-3)
+        e_step = rel_l2(host_u(dg2), [do2['u'][i]['kspace'] for i in range(3)])
+    finally:
+        dd.config.decfg.set('FFT', 'precision', 'fp64')
+    assert e_rhs < 1e-12, e_rhs
+    assert e_step < 1e-12, e_step
+
+
+@pytest.mark.gpu
+def test_df64_not_offered_for_2d(dd, cuda):
+    shape = (32, 32)
+    M = dd.mods
+    rhs = M.IncompressibleHydro(shape, M.FourierRepresentation)
+    data = rhs.create_fields(0.)
+    for i, c in enumerate(dd.init_cond.turbulence_2d(shape, seed=1)):
+        data['u'][i]['kspace'] = c
+    dd.config.decfg.set('FFT', 'precision', 'df64')
+    try:
+        with pytest.raises(NotImplementedError):
+            rhs.RHS(data, rhs.create_fields(0.))
+    finally:
+        dd.config.decfg.set('FFT', 'precision', 'fp64')
