@@ -1,19 +1,27 @@
 #!/usr/bin/env python
-"""Benchmark: 3D incompressible hydro, 256^3, FP64, RK4 (dt = 2e-3, nu = 5e-3),
-2/3 dealiasing, on one GB300 per rank.
+"""Benchmarks of the pseudospectral RHS / timestepping path on one GB300 per rank.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload hydro3d-256-fp64|hydro3d-256-fp32|hydro3d-128-fp64]
+                    [--workload NAME]
 
-A step is one RK4 step (4 fused right-hand sides + stage updates) of the
-whole 256^3 state.  The state (3 x 135 MB complex128) and the transform
-intermediates are larger than L2 (129 MB), so no L2 flush is needed between
-steps.  Prints one JSON line (rank 0).  Multi-GPU runs are independent
-replicas (weak scaling, no collective on the data path).
+Default workload (the headline): 3D incompressible hydro, 256^3, FP64, RK4,
+dt = 2e-3, nu = 5e-3, 2/3 dealiasing.  A step is one RK4 step (4 fused
+right-hand sides and stage updates) of the whole state.  The state
+(3 x 135 MB complex128) and the transform intermediates exceed L2 (129 MB),
+so no L2 flush is needed between steps.  Other workloads (one per benchmark
+configuration of the project):
 
-``--impl reference`` times the reference's CPU path (the oracle: the
-reference's numpy-FFT algorithm with the C restatement of its Cython stage
-kernels) on the host cores, on the same workload.
+    hydro3d-256-{fp64,df64,fp32}  3D hydro 256^3 RK4 with FP64 / double-float / FP32 transforms
+    hydro3d-128-fp64              the same at 128^3
+    mhd3d-256-{fp32,fp64}         3D MHD 256^3 RK4, nu = eta = 5e-3, dt = 1e-3
+    hydro2d-128                   2D hydro 128^2 RK2mid, nu = 1e-3, dt = 1e-3
+    bouss2d-ensemble-512          512 2D Boussinesq runs, sizes uniform in {64,128,256,512}^2,
+                                  nu = kappa = 2e-3, N^2 = 1, RK2mid, dt = 1e-2, one CUDA graph per step
+
+Prints one JSON line (rank 0).  Multi-GPU runs are independent replicas (weak
+scaling, no collective on the data path).  ``--impl reference`` times the
+reference's CPU algorithm (the oracle: numpy-FFT path with the C restatement of
+the Cython stage kernels) on the host cores for the same workload.
 """
 import argparse
 import json
@@ -28,48 +36,311 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "256³ hydro steps/s: plain FP64 vs FP32 vs 64³+closure at matched E(k) error"
+HEADLINE = "256³ hydro steps/s: plain FP64 vs FP32 vs 64³+closure at matched E(k) error"
+DATA3 = "synthetic (seeded random-phase solenoidal field, E(k)~k^4 exp(-2(k/4)^2), unit energy)"
 WORKLOADS = {
-    "hydro3d-256-fp64": dict(shape=(256, 256, 256), nu=5e-3, dt=2e-3, precision="fp64"),
-    "hydro3d-256-fp32": dict(shape=(256, 256, 256), nu=5e-3, dt=2e-3, precision="fp32"),
-    "hydro3d-128-fp64": dict(shape=(128, 128, 128), nu=5e-3, dt=2e-3, precision="fp64"),
-    "hydro3d-256-df64": dict(shape=(256, 256, 256), nu=5e-3, dt=2e-3, precision="df64"),
+    "hydro3d-256-fp64": dict(kind="hydro3d", shape=(256,) * 3, nu=5e-3, dt=2e-3, precision="fp64"),
+    "hydro3d-256-df64": dict(kind="hydro3d", shape=(256,) * 3, nu=5e-3, dt=2e-3, precision="df64"),
+    "hydro3d-256-fp32": dict(kind="hydro3d", shape=(256,) * 3, nu=5e-3, dt=2e-3, precision="fp32"),
+    "hydro3d-128-fp64": dict(kind="hydro3d", shape=(128,) * 3, nu=5e-3, dt=2e-3, precision="fp64"),
+    "mhd3d-256-fp32": dict(kind="mhd3d", shape=(256,) * 3, nu=5e-3, dt=1e-3, precision="fp32"),
+    "mhd3d-256-fp64": dict(kind="mhd3d", shape=(256,) * 3, nu=5e-3, dt=1e-3, precision="fp64"),
+    "hydro2d-128": dict(kind="hydro2d", shape=(128, 128), nu=1e-3, dt=1e-3, precision="fp64"),
+    "bouss2d-ensemble-512": dict(kind="ensemble", nrun=512, sizes=(64, 128, 256, 512), nu=2e-3, dt=1e-2,
+                                 precision="fp64"),
 }
 
 
-def algorithmic_bytes_per_step(N):
-    """Canonical bytes of one 3D RK4 step: 4 RHS x 9 FFTs x (1 real + 1 complex
-    field pass) + 4 stages x 3 components x 3 complex-array passes."""
-    B3 = 8 * N ** 3 + 16 * N ** 2 * (N // 2 + 1)
-    C3 = 16 * N ** 2 * (N // 2 + 1)
-    return 4 * 9 * B3 + 4 * 3 * 3 * C3
+def B3(N):
+    return 8 * N ** 3 + 16 * N ** 2 * (N // 2 + 1)
 
 
-def kernel_bytes(label, shape, precision):
-    """Algorithmic bytes of one launch of a fused-hydro kernel (reads + writes
-    of the pruned data it must move), keyed by the library's timing label."""
-    Nz, Ny, Nx = shape
-    Mx, My, Mz = (Nx - 1) // 3, (Ny - 1) // 3, (Nz - 1) // 3
-    Kx, Ky, Kz = Mx + 1, 2 * My + 1, 2 * Mz + 1
-    cs = 8 if precision == "fp32" else 16           # intermediate complex entry
-    kc = Ky * Kz * Kx * 16                          # compact kept complex128 array
-    w1 = Ky * Nz * Kx * cs
-    w2 = Nz * Ny * Kx * cs
-    if label.startswith("z_inv_curl"):
-        return 3 * kc + 6 * w1
-    if label.startswith("y_inv"):
-        return 6 * w1 + 6 * w2
-    if label.startswith("x_cross"):
-        return 6 * w2 + 3 * w2
-    if label.startswith("y_fwd"):
-        return 3 * w2 + 3 * w1
-    if label.startswith("z_fwd_compact"):
-        return 3 * w1 + 3 * kc
-    if label.startswith("rk4_stage3"):
-        return 3 * kc * 5          # N, y, tot (read) + tot/ys (write), average stage
-    return None
+def C3(N):
+    return 16 * N ** 2 * (N // 2 + 1)
 
 
+def B2(N):
+    return 8 * N * N + 16 * N * (N // 2 + 1)
+
+
+def C2(N):
+    return 16 * N * (N // 2 + 1)
+
+
+# ---------------------------------------------------------------- runners
+class Hydro3Runner:
+    """3D hydro (kind hydro3d) or MHD (kind mhd3d) with the fused RK4 step."""
+
+    def __init__(self, dd, wl, rank):
+        import torch
+        self.torch, self.dd, self.wl = torch, dd, wl
+        self.mhd = wl["kind"] == "mhd3d"
+        shape = wl["shape"]
+        dd.config.decfg.set("FFT", "precision", wl["precision"])
+        M = dd.mods
+        if self.mhd:
+            u = dd.init_cond.turbulence_3d(shape, seed=rank, k0=3.0)
+            b = dd.init_cond.turbulence_3d(shape, seed=rank + 1000, k0=3.0)
+            self.host = u + b
+            self.rhs = M.IncompressibleMHD(shape, M.FourierRepresentation)
+            self.rhs.parameters.update({"nu": wl["nu"], "eta": wl["nu"]})
+            self.names = [("u", 0), ("u", 1), ("u", 2), ("B", 0), ("B", 1), ("B", 2)]
+        else:
+            self.host = dd.init_cond.turbulence_3d(shape, seed=rank)
+            self.rhs = M.IncompressibleHydro(shape, M.FourierRepresentation)
+            self.rhs.parameters["nu"] = wl["nu"]
+            self.names = [("u", 0), ("u", 1), ("u", 2)]
+        self.data = self.rhs.create_fields(0.)
+        for (f, c), a in zip(self.names, self.host):
+            self.data[f][c]["kspace"] = a
+        self.ti = M.RK4(self.rhs)
+        self.launches_per_step = None
+
+    def step(self):
+        self.ti.do_advance(self.data, self.wl["dt"])
+
+    def state(self):
+        return [self.data[f][c].kdata for f, c in self.names]
+
+    def bytes_per_step(self):
+        N = self.wl["shape"][0]
+        if self.mhd:
+            return 4 * 18 * B3(N) + 4 * 6 * 3 * C3(N)
+        return 4 * 9 * B3(N) + 4 * 3 * 3 * C3(N)
+
+    def point_stages(self):
+        return float(np.prod(self.wl["shape"])) * 4
+
+    def kernel_bytes(self, label):
+        Nz, Ny, Nx = self.wl["shape"]
+        Mx, My, Mz = (Nx - 1) // 3, (Ny - 1) // 3, (Nz - 1) // 3
+        Kx, Ky, Kz = Mx + 1, 2 * My + 1, 2 * Mz + 1
+        cs = 8 if self.wl["precision"] == "fp32" else 16
+        kc = Ky * Kz * Kx * 16
+        w1, w2 = Ky * Nz * Kx * cs, Nz * Ny * Kx * cs
+        g = 2 if self.mhd else 1           # vector fields in the state
+        ni, no = 6 * g, 3 * g
+        if label.startswith("z_inv_curl"):
+            return 3 * g * kc + ni * w1
+        if label.startswith("y_inv"):
+            return ni * (w1 + w2)
+        if label.startswith("x_cross"):
+            return (ni + no) * w2
+        if label.startswith("y_fwd"):
+            return no * (w2 + w1)
+        if label.startswith("z_fwd_compact"):
+            return no * (w1 + kc)
+        if label.startswith("rk4_stage3"):
+            return 3 * g * kc * 5
+        return None
+
+    def config(self, ws):
+        w = self.wl
+        return {"workload": "%s %dx%dx%d, RK4 (ETD stages), dt=%g, nu=%g%s, 2/3 dealiasing, %s transforms"
+                            % ("3D incompressible MHD" if self.mhd else "3D incompressible hydro", *w["shape"], w["dt"],
+                               w["nu"], ", eta=%g" % w["nu"] if self.mhd else "", w["precision"]),
+                "grid": list(w["shape"]), "integrator": "RK4", "dt": w["dt"], "precision": w["precision"],
+                "parallelism": "replicas x%d" % ws, "l2": "inputs larger than L2 (state + intermediates), no flush"}
+
+    def metric(self):
+        if self.mhd:
+            return "256³ MHD steps/s", "steps/s"
+        return HEADLINE, "steps/s"
+
+
+class Hydro2Runner:
+    """2D hydro 128^2 with the fused RK2mid step."""
+
+    def __init__(self, dd, wl, rank):
+        import torch
+        self.torch, self.dd, self.wl = torch, dd, wl
+        dd.config.decfg.set("FFT", "precision", wl["precision"])
+        M = dd.mods
+        self.host = dd.init_cond.turbulence_2d(wl["shape"], seed=rank)
+        self.rhs = M.IncompressibleHydro(wl["shape"], M.FourierRepresentation)
+        self.rhs.parameters["nu"] = wl["nu"]
+        self.data = self.rhs.create_fields(0.)
+        for i in range(2):
+            self.data["u"][i]["kspace"] = self.host[i]
+        self.ti = M.RK2mid(self.rhs)
+        self.launches_per_step = None
+
+    def step(self):
+        self.ti.do_advance(self.data, self.wl["dt"])
+
+    def state(self):
+        return [self.data["u"][i].kdata for i in range(2)]
+
+    def bytes_per_step(self):
+        N = self.wl["shape"][0]
+        return 2 * 5 * B2(N) + 2 * 2 * 3 * C2(N)
+
+    def point_stages(self):
+        return float(np.prod(self.wl["shape"])) * 2
+
+    def kernel_bytes(self, label):
+        return None
+
+    def config(self, ws):
+        w = self.wl
+        return {"workload": "2D incompressible hydro %dx%d, RK2mid, dt=%g, nu=%g, 2/3 dealiasing" % (*w["shape"], w["dt"],
+                                                                                                  w["nu"]),
+                "grid": list(w["shape"]), "integrator": "RK2mid", "dt": w["dt"], "precision": w["precision"],
+                "parallelism": "replicas x%d" % ws, "l2": "state fits in L2 (launch-bound workload)"}
+
+    def metric(self):
+        return "128² 2D hydro steps/s", "steps/s"
+
+
+class EnsembleRunner:
+    """512 uneven-size 2D Boussinesq runs advanced together (CUDA graph per step)."""
+
+    def __init__(self, dd, wl, rank):
+        import torch
+        self.torch, self.dd, self.wl = torch, dd, wl
+        rng = np.random.Generator(np.random.PCG64(1234 + rank))
+        self.sizes = [int(s) for s in rng.choice(wl["sizes"], wl["nrun"])]
+        self.ens = dd.ensemble.BoussinesqEnsemble2D(self.sizes, nu=wl["nu"], kappa=wl["nu"],
+                                                    precision=wl["precision"])
+        self.ens.load_initial_conditions(seed=rank * 100000)
+        self.sched = self.ens.autotune(wl["dt"])
+        n0 = dd._lib.launch_count()
+        self.ens.capture(wl["dt"])
+        self.launches_per_step = (dd._lib.launch_count() - n0) // 2   # the eager warm-up + the captured step
+        self.host = [c.slab.cpu() for c in self.ens.classes]
+
+    def step(self):
+        self.ens.step(self.wl["dt"])
+
+    def state(self):
+        return [c.slab for c in self.ens.classes]
+
+    def bytes_per_step(self):
+        return self.ens.algorithmic_bytes_per_step()
+
+    def point_stages(self):
+        return float(self.ens.grid_point_stages())
+
+    def kernel_bytes(self, label):
+        return None
+
+    def config(self, ws):
+        w = self.wl
+        counts = {n: self.sizes.count(n) for n in w["sizes"]}
+        return {"workload": "%d independent 2D Boussinesq runs, sizes uniform (seeded) in %s^2 %s, nu=kappa=%g, "
+                            "N^2=1, RK2mid, dt=%g, %s, one CUDA graph per ensemble step"
+                            % (w["nrun"], list(w["sizes"]), counts, w["nu"], w["dt"], w["precision"]),
+                "runs_per_size": counts, "schedule": self.sched, "dt": w["dt"], "precision": w["precision"],
+                "parallelism": "replicas x%d" % ws, "l2": "ensemble state (> 1 GB) larger than L2, no flush"}
+
+    def metric(self):
+        return "512-run 2D Boussinesq ensemble steps/s", "ensemble steps/s"
+
+
+RUNNERS = {"hydro3d": Hydro3Runner, "mhd3d": Hydro3Runner, "hydro2d": Hydro2Runner, "ensemble": EnsembleRunner}
+
+
+# ---------------------------------------------------------------- CPU side
+def cpu_reference_steps(wl, nsteps, workers, time_budget, seed=0):
+    """Wall time of RK steps of the oracle (the reference's CPU algorithm)."""
+    import __graft_entry__
+    dd = __graft_entry__.load_package()
+    from oracle import physics as OP, time_step as OT, representation as OR
+    OR.FFT_WORKERS = workers
+    kind = wl["kind"]
+    if kind == "ensemble":
+        return cpu_ensemble_times(wl, dd, OP, OT, OR, nsteps, time_budget)
+    shape = wl["shape"]
+    if kind == "mhd3d":
+        rhs = OP.IncompressibleMHD(shape, OR.FourierRepresentation)
+        rhs.parameters.update({"nu": wl["nu"], "eta": wl["nu"]})
+        u = dd.init_cond.turbulence_3d(shape, seed=seed, k0=3.0)
+        b = dd.init_cond.turbulence_3d(shape, seed=seed + 1000, k0=3.0)
+        fields = list(zip([("u", 0), ("u", 1), ("u", 2), ("B", 0), ("B", 1), ("B", 2)], u + b))
+        ti_cls = OT.RK4
+    elif kind == "hydro3d":
+        rhs = OP.IncompressibleHydro(shape, OR.FourierRepresentation)
+        rhs.parameters["nu"] = wl["nu"]
+        fields = list(zip([("u", 0), ("u", 1), ("u", 2)], dd.init_cond.turbulence_3d(shape, seed=seed)))
+        ti_cls = OT.RK4
+    else:
+        rhs = OP.IncompressibleHydro(shape, OR.FourierRepresentation)
+        rhs.parameters["nu"] = wl["nu"]
+        fields = list(zip([("u", 0), ("u", 1)], dd.init_cond.turbulence_2d(shape, seed=seed)))
+        ti_cls = OT.RK2mid
+    data = rhs.create_fields(0.)
+    for (f, c), a in fields:
+        data[f][c]["kspace"] = a
+    ti = ti_cls(rhs)
+    times = []
+    t_start = time.perf_counter()
+    for _ in range(nsteps):
+        t0 = time.perf_counter()
+        ti.do_advance(data, wl["dt"])
+        times.append(time.perf_counter() - t0)
+        if time.perf_counter() - t_start + times[-1] > time_budget:
+            break
+    return times
+
+
+def cpu_ensemble_times(wl, dd, OP, OT, OR, nsteps, budget):
+    """One oracle run per size class, a few steps each; the ensemble-step time
+    is sum over classes of (runs in class) x (time per run-step)."""
+    rng = np.random.Generator(np.random.PCG64(1234))
+    sizes = [int(s) for s in rng.choice(wl["sizes"], wl["nrun"])]
+    per = {}
+    for n in wl["sizes"]:
+        rhs = OP.BoussinesqHydro((n, n), OR.FourierRepresentation)
+        rhs.parameters.update({"nu": wl["nu"], "kappa": wl["nu"], "boussinesq_direction": "y"})
+        d = rhs.create_fields(0.)
+        d["T"]["kspace"] = dd.init_cond.band_limited_noise_2d((n, n), seed=n)
+        ti = OT.RK2mid(rhs)
+        ti.do_advance(d, wl["dt"])
+        k = 3 if n < 512 else 2
+        t0 = time.perf_counter()
+        for _ in range(k):
+            ti.do_advance(d, wl["dt"])
+        per[n] = (time.perf_counter() - t0) / k
+    t_step = sum(per[n] for n in sizes)
+    return [t_step] * max(1, nsteps)
+
+
+def run_reference(args, wl, ws, rank):
+    if rank != 0:
+        return 0
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    budget = 150.0
+    times = cpu_reference_steps(wl, args.warmup + args.steps, cores, budget)
+    timed = times[min(args.warmup, len(times) - 1):] if len(times) > 1 else times
+    v = len(timed) / sum(timed)
+    if wl["kind"] == "ensemble":
+        # independent runs spread over all cores
+        v = v * cores
+        sample = ("one oracle run per size class timed for 2-3 RK2mid steps on one core, summed over the 512 runs "
+                  "and divided over %d cores (independent runs)" % cores)
+    else:
+        sample = ("%d step(s) of the %s workload on the host (of %d requested; %.0f s budget), the reference's "
+                  "numpy-FFT algorithm with pocketfft on %d threads" % (len(timed), args.workload,
+                                                                       args.warmup + args.steps, budget, cores))
+    metric, unit = metric_of(wl)
+    line = {"impl": "reference", "metric": metric, "value": v, "unit": unit, "n_gpus": ws,
+            "steps": len(timed), "warmup": len(times) - len(timed), "ms_per_step": 1e3 / v,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": DATA3 if "3d" in wl["kind"] else "synthetic (seeded)",
+            "config": {"workload": args.workload},
+            "cpu_baseline": {"value": v, "unit": unit, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def metric_of(wl):
+    return {"hydro3d": (HEADLINE, "steps/s"), "mhd3d": ("256³ MHD steps/s", "steps/s"),
+            "hydro2d": ("128² 2D hydro steps/s", "steps/s"),
+            "ensemble": ("512-run 2D Boussinesq ensemble steps/s", "ensemble steps/s")}[wl["kind"]]
+
+
+# ---------------------------------------------------------------- clocks
 class ClockSampler:
     """nvidia-smi clocks/throttle reasons sampled every 200 ms in the background."""
 
@@ -129,73 +400,17 @@ class ClockSampler:
 
 def gpu_uuid(torch, dev):
     try:
-        u = torch.cuda.get_device_properties(dev).uuid
-        return "GPU-" + str(u)
+        return "GPU-" + str(torch.cuda.get_device_properties(dev).uuid)
     except Exception:
         return None
 
 
 def setup_dist():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+    return (int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")),
+            int(os.environ.get("LOCAL_RANK", "0")))
 
 
-def cpu_reference_steps(wl, seed, nsteps, workers, time_budget):
-    """Time RK4 steps of the oracle (the reference's CPU algorithm) on the host."""
-    import __graft_entry__
-    dd = __graft_entry__.load_package()
-    from oracle import physics as OP, time_step as OT, representation as OR
-    OR.FFT_WORKERS = workers
-    u0 = dd.init_cond.turbulence_3d(wl["shape"], seed=seed)
-    rhs = OP.IncompressibleHydro(wl["shape"], OR.FourierRepresentation)
-    rhs.parameters["nu"] = wl["nu"]
-    data = rhs.create_fields(0.)
-    for i in range(3):
-        data["u"][i]["kspace"] = u0[i]
-    ti = OT.RK4(rhs)
-    times = []
-    t_start = time.perf_counter()
-    for s in range(nsteps):
-        t0 = time.perf_counter()
-        ti.do_advance(data, wl["dt"])
-        times.append(time.perf_counter() - t0)
-        if time.perf_counter() - t_start + times[-1] > time_budget:
-            break
-    return times
-
-
-def run_reference(args, wl, ws, rank):
-    if rank != 0:
-        return 0
-    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
-    budget = 150.0
-    times = cpu_reference_steps(wl, 0, args.warmup + args.steps, cores, budget)
-    timed = times[min(args.warmup, len(times) - 1):] if len(times) > 1 else times
-    v = len(timed) / sum(timed)
-    sample = ("%d RK4 step(s) of the %s workload on the host (warm-up %d of %d requested; stopped at a %.0f s "
-              "budget), numpy-FFT algorithm of the reference with pocketfft on %d threads"
-              % (len(timed), args.workload, len(times) - len(timed), args.warmup, budget, cores))
-    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": ws,
-            "steps": len(timed), "warmup": len(times) - len(timed), "ms_per_step": 1e3 / v,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded random-phase solenoidal field, E(k)~k^4 exp(-2(k/4)^2), unit energy)",
-            "config": config_of(args, wl, ws),
-            "cpu_baseline": {"value": v, "unit": "steps/s", "cores": cores, "kind": "port", "sample": sample},
-            "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line))
-    return 0
-
-
-def config_of(args, wl, ws):
-    return {"workload": "%s: 3D incompressible hydro %dx%dx%d, RK4, dt=%g, nu=%g, 2/3 dealiasing, %s"
-                        % (args.workload, *wl["shape"], wl["dt"], wl["nu"], wl["precision"]),
-            "grid": list(wl["shape"]), "integrator": "RK4 (ETD stages)", "dt": wl["dt"], "nu": wl["nu"],
-            "precision": wl["precision"], "parallelism": "replicas x%d" % ws,
-            "l2": "inputs larger than L2 (state 406 MB + intermediates), no flush"}
-
-
+# ---------------------------------------------------------------- main
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -221,29 +436,27 @@ def main():
     if ws > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=dev)
-    dd.config.decfg.set("FFT", "precision", wl["precision"])
-    M = dd.mods
-    shape = wl["shape"]
-    u0 = dd.init_cond.turbulence_3d(shape, seed=rank)
-    rhs = M.IncompressibleHydro(shape, M.FourierRepresentation)
-    rhs.parameters["nu"] = wl["nu"]
-    data = rhs.create_fields(0.)
-    for i in range(3):
-        data["u"][i]["kspace"] = u0[i]
-    ti = M.RK4(rhs)
-    dt = wl["dt"]
-    stream = torch.cuda.current_stream()
-    for _ in range(max(args.warmup, 0)):
-        ti.do_advance(data, dt)
-    torch.cuda.synchronize()
 
     def barrier():
         if dist is not None:
             dist.barrier()
 
+    def max_over_ranks(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    run = RUNNERS[wl["kind"]](dd, wl, rank)
+    stream = torch.cuda.current_stream()
+    for _ in range(max(args.warmup, 0)):
+        run.step()
+    torch.cuda.synchronize()
+
     sampler = ClockSampler(gpu_uuid(torch, local))
     sampler.start()
-    dd._lib.timing_enable(True)
+    dd._lib.timing_enable(run.launches_per_step is None)   # per-launch events only for non-graph workloads
     dd._lib.timing_reset()
     n0 = dd._lib.launch_count()
     barrier()
@@ -251,111 +464,98 @@ def main():
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for _ in range(args.steps):
-        ti.do_advance(data, dt)
+        run.step()
     e1.record(stream)
     torch.cuda.synchronize()
     barrier()
     launches = dd._lib.launch_count() - n0
-    ms = e0.elapsed_time(e1)
+    if run.launches_per_step is not None:
+        launches = run.launches_per_step * args.steps      # graph replays launch the captured kernels
+    ms = max_over_ranks(e0.elapsed_time(e1))
     kt = dd._lib.timing_report()
     dd._lib.timing_enable(False)
     clocks = sampler.stop()
-    if dist is not None:
-        t = torch.tensor([ms], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
     ms_per_step = ms / args.steps
     value = ws * args.steps / (ms / 1e3)
 
-    # dominant kernel roofline (device time from the events around each launch)
     peaks = {}
     pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.isfile(pk):
         peaks = json.load(open(pk))
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
-    top = max(kt.items(), key=lambda kv: kv[1][1]) if kt else None
-    roofline = None
-    kernels = {}
+    kernels, roofline = {}, None
+    total_kt = sum(v[1] for v in kt.values()) or 1.0
     for name, (cnt, tot) in sorted(kt.items(), key=lambda kv: -kv[1][1]):
-        b = kernel_bytes(name, shape, wl["precision"])
-        kernels[name] = {"launches": cnt, "ms_total": round(tot, 4), "share": round(tot / sum(v[1] for v in kt.values()), 4),
+        b = run.kernel_bytes(name)
+        kernels[name] = {"launches": cnt, "ms_total": round(tot, 4), "share": round(tot / total_kt, 4),
                          "gbs": (round(b / (tot / cnt / 1e3) / 1e9, 1) if b else None)}
-    if top:
-        name, (cnt, tot) = top
-        b = kernel_bytes(name, shape, wl["precision"])
+    B = run.bytes_per_step()
+    if kt:
+        name, (cnt, tot) = max(kt.items(), key=lambda kv: kv[1][1])
+        b = run.kernel_bytes(name)
         avg = tot / cnt / 1e3
         ach = b / avg / 1e9 if b else None
         roofline = {"bound": "hbm", "kernel": name, "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
-                    "frac": (ach / hbm_peak) if ach else None, "traffic": None,
-                    "peak_source": peak_src, "algorithmic_bytes_per_launch": b, "avg_launch_ms": avg * 1e3}
-    B = algorithmic_bytes_per_step(shape[0])
+                    "frac": (ach / hbm_peak) if ach else None, "traffic": None, "peak_source": peak_src,
+                    "algorithmic_bytes_per_launch": b, "avg_launch_ms": avg * 1e3}
+    else:
+        ach = B / (ms_per_step / 1e3) / 1e9
+        roofline = {"bound": "hbm", "kernel": "whole step (CUDA graph)", "achieved": ach, "peak": hbm_peak,
+                    "unit": "GB/s", "frac": ach / hbm_peak, "traffic": None, "peak_source": peak_src,
+                    "algorithmic_bytes_per_launch": B, "avg_launch_ms": ms_per_step}
     step_hbm = {"algorithmic_bytes_per_step": B, "t_roofline_ms": B / (hbm_peak * 1e9) * 1e3,
                 "hbm_frac": (B / (hbm_peak * 1e9)) / (ms_per_step / 1e3),
-                "grid_point_stages_per_s": float(np.prod(shape)) * 4 * value}
+                "grid_point_stages_per_s": run.point_stages() * value}
 
-    # end to end through the public API with host buffers
+    # end to end through the public API: the state in from pinned host memory,
+    # one step, the state back out, every step
     e2e = None
     if not args.no_e2e:
-        host_in = [torch.from_numpy(c).pin_memory() for c in u0]
+        host_in = [torch.as_tensor(h).pin_memory() for h in
+                   (run.host if isinstance(run.host[0], torch.Tensor) else [torch.from_numpy(h) for h in run.host])]
         host_out = [torch.empty_like(h).pin_memory() for h in host_in]
+        dev_state = run.state()
         ke = max(3, min(args.steps, 10))
         barrier()
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
         f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         f0.record(stream)
         for _ in range(ke):
-            for i in range(3):
-                data["u"][i].kdata.copy_(host_in[i], non_blocking=True)
-                data["u"][i]._curr_space = "kspace"
-                data["u"][i].data = data["u"][i].kdata
-            ti.do_advance(data, dt)
-            for i in range(3):
-                host_out[i].copy_(data["u"][i].kdata, non_blocking=True)
+            for d, h in zip(dev_state, host_in):
+                d.copy_(h, non_blocking=True)
+            run.step()
+            for d, h in zip(dev_state, host_out):
+                h.copy_(d, non_blocking=True)
         f1.record(stream)
         torch.cuda.synchronize()
-        wall = time.perf_counter() - t0
-        me = f0.elapsed_time(f1)
-        if dist is not None:
-            t = torch.tensor([me], dtype=torch.float64, device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            me = float(t.item())
+        me = max_over_ranks(f0.elapsed_time(f1))
         nb = sum(h.numel() * h.element_size() for h in host_in)
-        e2e = {"value": ws * ke / (me / 1e3), "unit": "steps/s", "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb,
-               "steps": ke, "host_wall_s": wall}
+        e2e = {"value": ws * ke / (me / 1e3), "unit": run.metric()[1], "h2d_bytes_per_step": nb,
+               "d2h_bytes_per_step": nb, "steps": ke}
 
-    # the same workload with the other transform arithmetics, from the same
-    # initial state, with their difference from the FP64 state after the
-    # same steps (FP64 native is the reference; it is the headline value)
+    # the headline workload with the other transform arithmetics, each with its
+    # difference from the FP64 state after the same steps
     variants = None
-    if not args.no_variants and wl["precision"] == "fp64":
+    if not args.no_variants and args.workload == "hydro3d-256-fp64":
         variants = {}
         kv = max(3, min(args.steps, 10))
-        ref = None
 
         def run_prec(prec):
-            dd.config.decfg.set("FFT", "precision", prec)
+            w2 = dict(wl, precision=prec)
+            r = Hydro3Runner(dd, w2, rank)
             try:
-                r = M.IncompressibleHydro(shape, M.FourierRepresentation)
-                r.parameters["nu"] = wl["nu"]
-                d = r.create_fields(0.)
-                for i in range(3):
-                    d["u"][i]["kspace"] = u0[i]
-                t = M.RK4(r)
-                t.do_advance(d, dt)  # warm-up step, part of the compared trajectory
+                r.step()
                 torch.cuda.synchronize()
                 a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                 a.record(stream)
                 for _ in range(kv):
-                    t.do_advance(d, dt)
+                    r.step()
                 b.record(stream)
                 torch.cuda.synchronize()
-                out = [d["u"][i].kdata.clone() for i in range(3)]
-                del r, d, t
-                return a.elapsed_time(b) / kv, out
+                return a.elapsed_time(b) / kv, [x.clone() for x in r.state()]
             finally:
-                dd.config.decfg.set("FFT", "precision", "fp64")
+                dd.config.decfg.set("FFT", "precision", wl["precision"])
 
         ms64, ref = run_prec("fp64")
         den = sum(float(torch.sum(torch.abs(x) ** 2)) for x in ref)
@@ -368,24 +568,24 @@ def main():
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        times = cpu_reference_steps(wl, 0, 1, 1, 60.0)
-        cpu = {"value": 1.0 / times[0], "unit": "steps/s", "cores": 1, "kind": "port",
-               "sample": "1 RK4 step of the %s workload, oracle (reference numpy-FFT algorithm + C restatement "
-                         "of its Cython stage kernels), single thread" % args.workload}
+        times = cpu_reference_steps(wl, 1, 1, 60.0)
+        cpu = {"value": 1.0 / times[0], "unit": run.metric()[1], "cores": 1, "kind": "port",
+               "sample": ("one step of the %s workload, oracle (the reference's numpy-FFT algorithm + C restatement "
+                          "of its Cython stage kernels), single thread" % args.workload) if wl["kind"] != "ensemble"
+               else "one oracle run per size class timed for 2-3 steps on one core, summed over the 512 runs"}
 
     if dist is not None:
         dist.barrier()
         dist.destroy_process_group()
     if rank != 0:
         return 0
-    vs = None
-    line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
+    metric, unit = run.metric()
+    line = {"metric": metric, "value": value, "unit": unit, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": vs, "dtype": {"fp64": "f64", "df64": "df64", "fp32": "f32"}[wl["precision"]],
-            "data": "synthetic (seeded random-phase solenoidal field, E(k)~k^4 exp(-2(k/4)^2), unit energy)",
-            "config": config_of(args, wl, ws), "clocks": clocks, "e2e": e2e, "gpu_launches": launches,
-            "roofline": roofline, "step_roofline": step_hbm, "kernels": kernels, "variants": variants,
-            "cpu_baseline": cpu}
+            "vs_baseline": None, "dtype": {"fp64": "f64", "df64": "df64", "fp32": "f32"}[wl["precision"]],
+            "data": DATA3 if "3d" in wl["kind"] else "synthetic (seeded)", "config": run.config(ws),
+            "clocks": clocks, "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
+            "step_roofline": step_hbm, "kernels": kernels, "variants": variants, "cpu_baseline": cpu}
     print(json.dumps(line))
     return 0
 

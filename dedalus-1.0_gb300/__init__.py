@@ -19,9 +19,11 @@ try:  # the device layers need torch; host helpers (kgrid, init_cond) do not
     from . import physics
     from . import time_step
     from . import mods
+    from . import diagnostics
+    from . import ensemble
 except ImportError as e:  # pragma: no cover
     if "torch" not in str(e):
         raise
 
 __all__ = ["_lib", "kgrid", "config", "init_cond", "engine", "representations", "fields", "physics",
-           "time_step", "mods"]
+           "time_step", "mods", "diagnostics", "ensemble"]

@@ -55,6 +55,9 @@ SIGNATURES = {
     "dd_hydro3d_rhs": [P, PP, PP, P, I, I, P, SZ, P],
     "dd_hydro3d_rk4_step": [P, PP, P, P, P, D, I, D, I, ctypes.POINTER(I), P, SZ, P],
     "dd_any_nonkept": [P, I, PP, P, P],
+    "dd_diag_workspace_size": [P, I, ctypes.POINTER(SZ)],
+    "dd_volume_average": [P, I, I, PP, P, P, SZ, P],
+    "dd_spectrum": [P, I, PP, D, I, P, P, D, P, P, P, SZ, P],
     "dd_rhs3d_workspace_size": [P, I, I, ctypes.POINTER(SZ)],
     "dd_rhs3d": [P, I, P, PP, PP, P, I, I, P, SZ, P],
     "dd_rk4_step3d": [P, I, P, PP, P, PP, PP, P, I, D, I, ctypes.POINTER(I), P, SZ, P],

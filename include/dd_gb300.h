@@ -203,6 +203,28 @@ int dd_rk4_step3d(const dd_plan* plan, int physics, const double* params, void* 
                   int viscosity_order, double dt, int precision, const int* nonkept_flag, void* work,
                   size_t work_bytes, void* stream);
 
+/* ---------------------------------------------------------- diagnostics
+ * Volume averages in k-space with the reference's Hermitian weights (entries
+ * with kx > 0 count twice; dedalus/analysis/volume_average.py:71-98), summed
+ * in FP64 with compensated, deterministic reductions.  kind:
+ *   0 energy 1/2 sum|u_c|^2 (ekin/emag, volume_average.py:109-118, 180-188)
+ *   1 1/2 |curl u|^2, 3D (energy_dissipation = 2 nu x this, 254-265)
+ *   2 2D enstrophy 1/2 |d_x u_y - d_y u_x|^2 (191-200)
+ *   3 helicity Re(u . conj(curl u)), 3D
+ *   4 mean square divergence |sum_i i k_i u_i|^2
+ *   5 divergence_sum: unweighted sum |sum_i i k_i u_i| (288-295)
+ *   6 |u|^2 of one component (ux2, uy2, temp2, ...)
+ * out is a device double.  dd_spectrum bins power1d = norm sum_c |u_c|^2 x
+ * 4 pi k^2 (3D) or 2 pi k (2D) by kbottom[i] <= |k| < ktop[i], skipping zero
+ * power (analysis_set.py:778-815); bin sums and counts are device arrays and
+ * dk = kbottom[1]. */
+int dd_diag_workspace_size(const dd_plan* plan, int nbins, size_t* bytes);
+int dd_volume_average(const dd_plan* plan, int kind, int ncomp, const void* const* comps, double* out, void* work,
+                      size_t work_bytes, void* stream);
+int dd_spectrum(const dd_plan* plan, int ncomp, const void* const* comps, double norm, int nbins, const double* kbottom,
+                const double* ktop, double dk, double* out_sum, double* out_count, void* work, size_t work_bytes,
+                void* stream);
+
 /* Sets *dflag (device int) to 1 if any of the ncomp k arrays has a non-zero
  * entry outside the kept (dealiased) modes; does not clear it. */
 int dd_any_nonkept(const dd_plan* plan, int ncomp, const void* const* k, int* dflag, void* stream);
