@@ -1,6 +1,7 @@
 """GB300-native drop-in for the pseudospectral RHS / timestepping hot path of
 dedalus-1.0 (Fourier representation, IncompressibleHydro / BoussinesqHydro /
-IncompressibleMHD physics, RK2mid / RK2trap / RK4 integrators).
+IncompressibleMHD physics, RK2mid / RK2trap / RK4 integrators), plus a learned
+subgrid closure for 64^3 LES (``closure``, ``physics.LESHydro``).
 
 Import name ``dedalus_gb300`` (the directory name is not a Python identifier;
 ``__graft_entry__.load_package()`` registers it).  All compute runs in
@@ -21,9 +22,10 @@ try:  # the device layers need torch; host helpers (kgrid, init_cond) do not
     from . import mods
     from . import diagnostics
     from . import ensemble
+    from . import closure
 except ImportError as e:  # pragma: no cover
     if "torch" not in str(e):
         raise
 
 __all__ = ["_lib", "kgrid", "config", "init_cond", "engine", "representations", "fields", "physics",
-           "time_step", "mods", "diagnostics", "ensemble"]
+           "time_step", "mods", "diagnostics", "ensemble", "closure"]

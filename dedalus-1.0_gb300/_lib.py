@@ -64,7 +64,29 @@ SIGNATURES = {
     "dd_rhs2d_workspace_size": [P, I, I, ctypes.POINTER(SZ)],
     "dd_rhs2d": [P, I, P, I, PP, I64, PP, I64, P, I, I, P, SZ, P],
     "dd_rk2mid_step2d": [P, I, P, I, PP, I64, P, PP, PP, P, I, D, I, P, SZ, P],
+    "dd_mlp_sizes": [ctypes.POINTER(I)] * 5,
+    "dd_mlp_workspace_size": [I64, ctypes.POINTER(SZ)],
+    "dd_mlp_pack": [P, P, P],
+    "dd_mlp_infer": [P, P, I64, P, P, P],
+    "dd_mlp_grad": [P, P, P, I64, I64, P, P, P, P, P, SZ, P],
+    "dd_mlp_adam": [P, P, P, P, I, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, P, P],
+    "dd_mlp_normalize": [P, I64, P, P, P, P],
+    "dd_les_products": [I64, PP, PP, P],
+    "dd_les_truncate3": [P, P, I, PP, PP, P],
+    "dd_les_gradients": [P, PP, PP, I, P, SZ, P],
+    "dd_les_samples": [I64, PP, PP, PP, D, P, P],
+    "dd_les_stress": [P, PP, PP, P, I, P, SZ, P],
+    "dd_les_workspace_size": [P, I, ctypes.POINTER(SZ)],
+    "dd_les_rhs3d": [P, PP, PP, P, I, I, P, P, SZ, P],
+    "dd_les_rk4_step3d": [P, PP, P, PP, PP, P, I, D, I, ctypes.POINTER(I), P, P, SZ, P],
 }
+
+
+class Closure(ctypes.Structure):
+    """dd_closure: device pointers of the BF16 weights, FP32 parameters and
+    normalisation vector, and the filter width."""
+    _fields_ = [("wbf16", ctypes.c_void_p), ("params", ctypes.c_void_p), ("norm", ctypes.c_void_p),
+                ("delta", ctypes.c_double)]
 _RESTYPE = {"dd_last_error": ctypes.c_char_p, "dd_launch_count": ctypes.c_longlong}
 
 

@@ -1,0 +1,340 @@
+// Learned subgrid closure of the 3D LES (les.cuh): velocity gradients at the
+// grid points, the fused normalise -> MLP -> stress kernel, the closure term
+// added to the unprojected nonlinear products, and the kernels that make the
+// training data from a DNS (products, sharp spectral truncation, samples).
+#include "fft_impl.cuh"
+#include "les.cuh"
+#include "mlp.cuh"
+
+namespace dd {
+
+DD_FFT_INSTANTIATE(extern, double)
+DD_FFT_INSTANTIATE(extern, float)
+
+static inline size_t up256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+static inline unsigned les_grid(int64_t n, int per = 256) {
+    int64_t b = (n + per - 1) / per;
+    if (b > 152 * 16) b = 152 * 16;
+    return (unsigned)(b < 1 ? 1 : b);
+}
+
+// kept entry i of the compact order [kyc][kzc][kx] -> full-layout indices
+__device__ __forceinline__ void les_kept(const Geo3& g, int64_t i, int& ky_i, int& kz_i, int& ix, int64_t& o) {
+    ix = (int)(i % g.Kx);
+    const int64_t r = i / g.Kx;
+    const int kzc = (int)(r % g.Kz), kyc = (int)(r / g.Kz);
+    ky_i = compact_to_full(kyc, g.Ny, g.Ky);
+    kz_i = compact_to_full(kzc, g.Nz, g.Kz);
+    o = ((int64_t)ky_i * g.Nz + kz_i) * g.Nh + ix;
+}
+
+// (i k) a
+__device__ __forceinline__ double2 les_ik(double2 a, double k) { return make_double2(-(k * a.y), k * a.x); }
+
+// gk[3 a + j] = i k_j y_a on the kept modes (full layout out).
+template <bool COMPACT>
+__global__ void k_les_grad9(Geo3 g, const double* kx, const double* ky, const double* kz, CPtrs y, Ptrs gk) {
+    const int64_t n = (int64_t)g.Ky * g.Kz * g.Kx;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int ky_i, kz_i, ix;
+        int64_t o;
+        les_kept(g, i, ky_i, kz_i, ix, o);
+        const double kv[3] = {kx[ix], ky[ky_i], kz[kz_i]};
+        const int64_t src = COMPACT ? i : o;
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            const double2 u = ((const double2*)y.p[a])[src];
+#pragma unroll
+            for (int j = 0; j < 3; j++) ((double2*)gk.p[3 * a + j])[o] = les_ik(u, kv[j]);
+        }
+    }
+}
+
+// Per tile of 64 grid points: the 9 gradients and the width are normalised to
+// BF16 network inputs, the MLP runs on the tensor cores and the 6 stresses are
+// written.  tau may alias gx[0..5]: a block reads all inputs of a tile before
+// it writes that tile's outputs, and tiles are disjoint.
+__global__ void __launch_bounds__(MLP_THREADS) k_les_mlp(CPtrs gx, Ptrs tau, int64_t npts, const bf16* wb,
+                                                         const float* p, const float* norm, double delta) {
+    extern __shared__ __align__(16) unsigned char les_smem[];
+    MlpFwdSmem& s = *reinterpret_cast<MlpFwdSmem*>(les_smem);
+    mlp_load_weights(s, wb, p);
+    const int r0 = 16 * (threadIdx.x >> 5);
+    for (int64_t base = (int64_t)blockIdx.x * 64; base < npts; base += (int64_t)gridDim.x * 64) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < 64 * MLP_IN; i += blockDim.x) {
+            const int a = i >> 6, r = i & 63;
+            const int64_t pt = base + r;
+            float v = 0.f;
+            if (a < 9) v = pt < npts ? (float)((const double*)gx.p[a])[pt] : 0.f;
+            else if (a == 9) v = (float)delta;
+            if (a < MLP_NIN) v = (v - norm[NORM_IN_MEAN + a]) * norm[NORM_IN_SCALE + a];
+            s.x[r * LDI + a] = __float2bfloat16_rn(v);
+        }
+        __syncthreads();
+        float y[4];
+        mlp_forward_warp(s, r0, y);
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int c = frag_col(q);
+            const int64_t pt = base + r0 + frag_row(q);
+            if (c < MLP_NOUT && pt < npts)
+                ((double*)tau.p[c])[pt] = (double)(y[q] * norm[NORM_OUT_SCALE + c] + norm[NORM_OUT_MEAN + c]);
+        }
+    }
+}
+
+// nc_i -= i k_j tau_ij on the kept modes; tau spectra in full layout, order
+// xx, yy, zz, xy, xz, yz; nc compact complex128.
+__global__ void k_les_add(Geo3 g, const double* kx, const double* ky, const double* kz, CPtrs tk, Ptrs nc) {
+    const int64_t n = (int64_t)g.Ky * g.Kz * g.Kx;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int ky_i, kz_i, ix;
+        int64_t o;
+        les_kept(g, i, ky_i, kz_i, ix, o);
+        const double k0 = kx[ix], k1 = ky[ky_i], k2 = kz[kz_i];
+        double2 t[6];
+#pragma unroll
+        for (int c = 0; c < 6; c++) t[c] = ((const double2*)tk.p[c])[o];
+        // rows of tau: (xx, xy, xz), (xy, yy, yz), (xz, yz, zz)
+        const int row[3][3] = {{0, 3, 4}, {3, 1, 5}, {4, 5, 2}};
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            const double2 d0 = les_ik(t[row[a][0]], k0), d1 = les_ik(t[row[a][1]], k1), d2 = les_ik(t[row[a][2]], k2);
+            double2* N = (double2*)nc.p[a];
+            const double2 v = N[i];
+            N[i] = make_double2(v.x - ((d0.x + d1.x) + d2.x), v.y - ((d0.y + d1.y) + d2.y));
+        }
+    }
+}
+
+__global__ void k_les_products(int64_t npts, CPtrs u, Ptrs out) {
+    const int pa[6] = {0, 1, 2, 0, 0, 1}, pb[6] = {0, 1, 2, 1, 2, 2};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < npts; i += (int64_t)gridDim.x * blockDim.x) {
+        double v[3];
+#pragma unroll
+        for (int a = 0; a < 3; a++) v[a] = ((const double*)u.p[a])[i];
+#pragma unroll
+        for (int c = 0; c < 6; c++) ((double*)out.p[c])[i] = v[pa[c]] * v[pb[c]];
+    }
+}
+
+// Signed wavenumber index m of full index i on an axis of length N, and back.
+__device__ __forceinline__ int les_signed(int i, int N) { return i <= N / 2 ? i : i - N; }
+__device__ __forceinline__ int les_index(int m, int N) { return m >= 0 ? m : m + N; }
+
+__global__ void k_les_truncate3(Geo3 gs, Geo3 gd, CPtrs s, Ptrs d) {
+    const double2* S = (const double2*)s.p[blockIdx.y];
+    double2* D = (double2*)d.p[blockIdx.y];
+    const int64_t n = gd.kcount();
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int ix = (int)(i % gd.Nh);
+        const int64_t r = i / gd.Nh;
+        const int kz_i = (int)(r % gd.Nz), ky_i = (int)(r / gd.Nz);
+        double2 v = make_double2(0., 0.);
+        if (ix <= gd.Mx && kept_full(ky_i, gd.Ny, gd.My) && kept_full(kz_i, gd.Nz, gd.Mz)) {
+            const int sy = les_index(les_signed(ky_i, gd.Ny), gs.Ny), sz = les_index(les_signed(kz_i, gd.Nz), gs.Nz);
+            v = S[((int64_t)sy * gs.Nz + sz) * gs.Nh + ix];
+        }
+        D[i] = v;
+    }
+}
+
+__global__ void k_les_samples(int64_t npts, CPtrs gx, CPtrs f, CPtrs fr, double delta, float* raw) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < npts; i += (int64_t)gridDim.x * blockDim.x) {
+        __align__(16) float r[16];
+#pragma unroll
+        for (int a = 0; a < 9; a++) r[a] = (float)((const double*)gx.p[a])[i];
+        r[9] = (float)delta;
+#pragma unroll
+        for (int c = 0; c < 6; c++) r[10 + c] = (float)(((const double*)f.p[c])[i] - ((const double*)fr.p[c])[i]);
+        float4* dst = reinterpret_cast<float4*>(raw + i * 16);
+#pragma unroll
+        for (int q = 0; q < 4; q++) dst[q] = reinterpret_cast<const float4*>(r)[q];
+    }
+}
+
+// ------------------------------------------------------------- drivers
+struct LesWork {
+    double2* gk[9];   // gradient spectra, later the stress spectra (0..5)
+    double* gx[9];    // gradients at the grid points, later the stresses (0..5)
+    void* fw;
+    size_t fwb;
+};
+
+size_t les_work_bytes(const dd_plan* p) {
+    const Geo3& g = p->g3;
+    return up256(9 * (size_t)g.kcount() * sizeof(double2)) + up256(9 * (size_t)g.xcount() * sizeof(double)) +
+           up256(ws_bytes<double>(p, 9));
+}
+
+static LesWork les_carve(const dd_plan* p, void* work) {
+    const Geo3& g = p->g3;
+    LesWork w;
+    char* b = (char*)work;
+    for (int f = 0; f < 9; f++) w.gk[f] = (double2*)b + f * g.kcount();
+    b += up256(9 * (size_t)g.kcount() * sizeof(double2));
+    for (int f = 0; f < 9; f++) w.gx[f] = (double*)b + f * g.xcount();
+    b += up256(9 * (size_t)g.xcount() * sizeof(double));
+    w.fw = b;
+    w.fwb = up256(ws_bytes<double>(p, 9));
+    return w;
+}
+
+static int les_grads(const dd_plan* p, int prec, bool compact, const void* const* y, const LesWork& w,
+                     cudaStream_t st) {
+    const Geo3& g = p->g3;
+    CPtrs yc{};
+    Ptrs gk{};
+    for (int a = 0; a < 3; a++) yc.p[a] = y[a];
+    for (int f = 0; f < 9; f++) gk.p[f] = w.gk[f];
+    const unsigned nb = les_grid((int64_t)g.Ky * g.Kz * g.Kx);
+    if (compact) DD_KT("les_grad9", st, k_les_grad9<true><<<nb, 256, 0, st>>>(g, p->kx, p->ky, p->kz, yc, gk));
+    else DD_KT("les_grad9", st, k_les_grad9<false><<<nb, 256, 0, st>>>(g, p->kx, p->ky, p->kz, yc, gk));
+    DD_LAUNCH_CHECK();
+    const void* kin[9];
+    double* xo[9];
+    for (int f = 0; f < 9; f++) { kin[f] = w.gk[f]; xo[f] = w.gx[f]; }
+    if (prec == DD_FP32) return fft_c2r<float>(p, 9, kin, xo, w.fw, w.fwb, st);
+    return fft_c2r<double>(p, 9, kin, xo, w.fw, w.fwb, st);
+}
+
+static int les_mlp(const dd_plan* p, const dd_closure* cl, const LesWork& w, double* const* tau, cudaStream_t st) {
+    static bool configured = false;
+    if (!configured) {
+        DD_CUDA(cudaFuncSetAttribute(k_les_mlp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MlpFwdSmem)));
+        configured = true;
+    }
+    const int64_t npts = p->g3.xcount();
+    CPtrs gx{};
+    Ptrs t{};
+    for (int f = 0; f < 9; f++) gx.p[f] = w.gx[f];
+    for (int c = 0; c < 6; c++) t.p[c] = tau[c];
+    unsigned nb = les_grid(npts, 64);
+    if (nb > 152 * 4) nb = 152 * 4;
+    DD_KT("les_mlp", st,
+          k_les_mlp<<<nb, MLP_THREADS, sizeof(MlpFwdSmem), st>>>(gx, t, npts, (const bf16*)cl->wbf16, cl->params,
+                                                                  cl->norm, cl->delta));
+    DD_LAUNCH_CHECK();
+    return DD_OK;
+}
+
+int les_closure_add(const dd_plan* p, const LesHook& h, int prec, bool compact, const void* const* y,
+                    void* const* nc, cudaStream_t st) {
+    DD_CHECK_ARG(h.wb >= les_work_bytes(p), "closure workspace too small");
+    const LesWork w = les_carve(p, h.work);
+    DD_TRY(les_grads(p, prec, compact, y, w, st));
+    DD_TRY(les_mlp(p, h.cl, w, w.gx, st));      // stresses overwrite gradients 0..5
+    const double* xin[6];
+    void* kout[6];
+    for (int c = 0; c < 6; c++) { xin[c] = w.gx[c]; kout[c] = w.gk[c]; }
+    if (prec == DD_FP32) DD_TRY(fft_r2c<float>(p, 6, xin, kout, w.fw, w.fwb, st));
+    else DD_TRY(fft_r2c<double>(p, 6, xin, kout, w.fw, w.fwb, st));
+    const Geo3& g = p->g3;
+    CPtrs tk{};
+    Ptrs n{};
+    for (int c = 0; c < 6; c++) tk.p[c] = w.gk[c];
+    for (int a = 0; a < 3; a++) n.p[a] = nc[a];
+    DD_KT("les_add", st,
+          k_les_add<<<les_grid((int64_t)g.Ky * g.Kz * g.Kx), 256, 0, st>>>(g, p->kx, p->ky, p->kz, tk, n));
+    DD_LAUNCH_CHECK();
+    return DD_OK;
+}
+
+}  // namespace dd
+
+using namespace dd;
+
+static int les_check_plan(const dd_plan* p) {
+    DD_CHECK_ARG(p, "null plan");
+    DD_CHECK_ARG(p->ndim == 3, "the closure is implemented for 3D grids");
+    return DD_OK;
+}
+
+static int les_check_closure(const dd_closure* cl) {
+    DD_CHECK_ARG(cl && cl->wbf16 && cl->params && cl->norm, "closure weights, parameters and norm are required");
+    return DD_OK;
+}
+
+extern "C" {
+
+int dd_les_products(int64_t npts, const double* const* u, double* const* out, void* stream) {
+    DD_CHECK_ARG(u && out && npts >= 0, "dd_les_products: bad arguments");
+    CPtrs uc{};
+    Ptrs o{};
+    for (int a = 0; a < 3; a++) { DD_CHECK_ARG(u[a], "null velocity %d", a); uc.p[a] = u[a]; }
+    for (int c = 0; c < 6; c++) { DD_CHECK_ARG(out[c], "null product %d", c); o.p[c] = out[c]; }
+    if (npts == 0) return DD_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    DD_KT("les_products", st, k_les_products<<<les_grid(npts), 256, 0, st>>>(npts, uc, o));
+    DD_LAUNCH_CHECK();
+    return DD_OK;
+}
+
+int dd_les_truncate3(const dd_plan* src, const dd_plan* dst, int nfield, const void* const* s, void* const* d,
+                     void* stream) {
+    DD_TRY(les_check_plan(src));
+    DD_TRY(les_check_plan(dst));
+    DD_CHECK_ARG(s && d && nfield >= 1 && nfield <= DD_MAXF, "dd_les_truncate3: bad arguments");
+    const Geo3 &gs = src->g3, &gd = dst->g3;
+    DD_CHECK_ARG(gd.Mx <= gs.Mx && gd.My <= gs.My && gd.Mz <= gs.Mz,
+                 "the kept modes of the target grid must be kept modes of the source grid");
+    CPtrs sc{};
+    Ptrs dc{};
+    for (int f = 0; f < nfield; f++) {
+        DD_CHECK_ARG(s[f] && d[f], "null field %d", f);
+        sc.p[f] = s[f];
+        dc.p[f] = d[f];
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    DD_KT("les_truncate3", st, k_les_truncate3<<<dim3(les_grid(gd.kcount()), nfield), 256, 0, st>>>(gs, gd, sc, dc));
+    DD_LAUNCH_CHECK();
+    return DD_OK;
+}
+
+int dd_les_samples(int64_t npts, const double* const* g, const double* const* f, const double* const* fr,
+                   double delta, float* raw, void* stream) {
+    DD_CHECK_ARG(g && f && fr && raw && npts >= 0, "dd_les_samples: bad arguments");
+    CPtrs gc{}, fc{}, rc{};
+    for (int a = 0; a < 9; a++) { DD_CHECK_ARG(g[a], "null gradient %d", a); gc.p[a] = g[a]; }
+    for (int c = 0; c < 6; c++) { DD_CHECK_ARG(f[c], "null product %d", c); fc.p[c] = f[c]; }
+    for (int c = 0; c < 6; c++) { DD_CHECK_ARG(fr[c], "null resolved product %d", c); rc.p[c] = fr[c]; }
+    if (npts == 0) return DD_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    DD_KT("les_samples", st, k_les_samples<<<les_grid(npts), 256, 0, st>>>(npts, gc, fc, rc, delta, raw));
+    DD_LAUNCH_CHECK();
+    return DD_OK;
+}
+
+int dd_les_gradients(const dd_plan* p, const void* const* u, double* const* gx, int precision, void* work,
+                     size_t work_bytes, void* stream) {
+    DD_TRY(les_check_plan(p));
+    DD_CHECK_ARG(u && gx && work, "dd_les_gradients: null pointer");
+    DD_CHECK_ARG(precision == DD_FP64 || precision == DD_FP32, "precision must be DD_FP64 or DD_FP32");
+    DD_CHECK_ARG(work_bytes >= les_work_bytes(p), "workspace too small: %zu < %zu", work_bytes, les_work_bytes(p));
+    for (int a = 0; a < 3; a++) DD_CHECK_ARG(u[a], "null velocity %d", a);
+    for (int f = 0; f < 9; f++) DD_CHECK_ARG(gx[f], "null gradient %d", f);
+    cudaStream_t st = (cudaStream_t)stream;
+    const LesWork w = les_carve(p, work);
+    DD_TRY(les_grads(p, precision, false, u, w, st));
+    const int64_t xb = p->g3.xcount() * (int64_t)sizeof(double);
+    for (int f = 0; f < 9; f++) DD_CUDA(cudaMemcpyAsync(gx[f], w.gx[f], xb, cudaMemcpyDeviceToDevice, st));
+    return DD_OK;
+}
+
+int dd_les_stress(const dd_plan* p, const void* const* u, double* const* tau, const dd_closure* cl, int precision,
+                  void* work, size_t work_bytes, void* stream) {
+    DD_TRY(les_check_plan(p));
+    DD_TRY(les_check_closure(cl));
+    DD_CHECK_ARG(u && tau && work, "dd_les_stress: null pointer");
+    DD_CHECK_ARG(precision == DD_FP64 || precision == DD_FP32, "precision must be DD_FP64 or DD_FP32");
+    DD_CHECK_ARG(work_bytes >= les_work_bytes(p), "workspace too small: %zu < %zu", work_bytes, les_work_bytes(p));
+    for (int c = 0; c < 6; c++) DD_CHECK_ARG(tau[c], "null stress %d", c);
+    cudaStream_t st = (cudaStream_t)stream;
+    const LesWork w = les_carve(p, work);
+    DD_TRY(les_grads(p, precision, false, u, w, st));
+    return les_mlp(p, cl, w, tau, st);
+}
+
+}  // extern "C"

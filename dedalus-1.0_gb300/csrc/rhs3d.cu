@@ -2,6 +2,7 @@
 // the C ABI.  The transform passes and their instantiations are in
 // rhs3d_impl.cuh / rhs3d_<precision>.cu.
 #include "rhs3d_impl.cuh"
+#include "les.cuh"
 
 namespace dd {
 
@@ -255,7 +256,8 @@ static double inv_fpr_of(const double* params) { return 1.0 / ((4.0 * M_PI) * pa
 
 template <int PH>
 static int rhs3(const dd_plan* p, const double* params, const void* const* u, void* const* deriv,
-                const double* inv_k2, int prec, int zero_nonkept, void* work, size_t wb, cudaStream_t st) {
+                const double* inv_k2, int prec, int zero_nonkept, void* work, size_t wb, cudaStream_t st,
+                const LesHook* les = nullptr) {
     using P = Phys3<PH>;
     const Geo3& g = p->g3;
     const size_t need = work3_bytes(prec, g, P::NI, P::NO, P::NF, false);
@@ -267,6 +269,10 @@ static int rhs3(const dd_plan* p, const double* params, const void* const* u, vo
     CPtrs nc{}; Ptrs d{};
     for (int c = 0; c < P::NO; c++) nc.p[c] = work3_nc(prec, w, c);
     for (int c = 0; c < P::NF; c++) d.p[c] = deriv[c];
+    if (les) {
+        void* ncp[3] = {(void*)nc.p[0], (void*)nc.p[1], (void*)nc.p[2]};
+        DD_TRY(les_closure_add(p, *les, prec, false, u, ncp, st));
+    }
     if (zero_nonkept) {
         DD_KT("zero_nonkept3", st, k_dealias3_all<<<dim3(ew_grid(g.kcount()), P::NF), 256, 0, st>>>(g, d));
         DD_LAUNCH_CHECK();
@@ -279,7 +285,8 @@ static int rhs3(const dd_plan* p, const double* params, const void* const* u, vo
 template <int PH>
 static int rk4_3(const dd_plan* p, const double* params, void* const* u, const double* inv_k2,
                  const void* const* tab_half, const void* const* tab_full, const double* coeff, int vo, double dt,
-                 int prec, const int* nonkept_flag, void* work, size_t wb, cudaStream_t st) {
+                 int prec, const int* nonkept_flag, void* work, size_t wb, cudaStream_t st,
+                 const LesHook* les = nullptr) {
     using P = Phys3<PH>;
     const Geo3& g = p->g3;
     const size_t need = work3_bytes(prec, g, P::NI, P::NO, P::NF, true);
@@ -305,6 +312,10 @@ static int rk4_3(const dd_plan* p, const double* params, void* const* u, const d
     const unsigned nb = ew_grid((int64_t)w.kc);
     for (int s = 1; s <= 4; s++) {
         DD_TRY(nonlinear3_any<PH>(p, prec, s > 1, s == 1 ? (const void* const*)u : ysc, inv_fpr, w, st));
+        if (les) {
+            void* ncp[3] = {(void*)a.nc.p[0], (void*)a.nc.p[1], (void*)a.nc.p[2]};
+            DD_TRY(les_closure_add(p, *les, prec, s > 1, s == 1 ? (const void* const*)u : ysc, ncp, st));
+        }
         a.stage = s; a.h = hs[s - 1]; a.w = ws[s - 1];
         for (int grp = 0; grp < P::NG; grp++)
             a.tab[grp] = intk ? (const double4*)(s <= 2 ? tab_half[grp] : tab_full[grp]) : nullptr;
@@ -372,6 +383,54 @@ int dd_rk4_step3d(const dd_plan* p, int physics, const double* params, void* con
                                nonkept_flag, work, work_bytes, st);
     return rk4_3<P3_MHD>(p, params, state, inv_k2, tab_half, tab_full, coeff, viscosity_order, dt, precision,
                          nonkept_flag, work, work_bytes, st);
+}
+
+// Closed LES (hydro with the learned closure term in every RHS evaluation).
+static size_t les_total_bytes(const dd_plan* p, int prec) {
+    return Work3::up256(work3_bytes(prec, p->g3, 6, 3, 3, true)) + les_work_bytes(p);
+}
+
+static LesHook les_hook(const dd_plan* p, int prec, const dd_closure* cl, void* work, size_t wb) {
+    const size_t off = Work3::up256(work3_bytes(prec, p->g3, 6, 3, 3, true));
+    return LesHook{cl, (char*)work + off, wb > off ? wb - off : 0};
+}
+
+static int les_check(const dd_plan* p, const dd_closure* cl, int precision, void* work, size_t wb) {
+    DD_CHECK_ARG(p && p->ndim == 3, "the closed LES needs a 3D plan");
+    DD_CHECK_ARG(cl && cl->wbf16 && cl->params && cl->norm, "closure weights, parameters and norm are required");
+    DD_CHECK_ARG(precision == DD_FP64 || precision == DD_FP32, "precision must be DD_FP64 or DD_FP32");
+    DD_CHECK_ARG(work, "null workspace");
+    DD_CHECK_ARG(wb >= les_total_bytes(p, precision), "workspace too small: %zu < %zu", wb,
+                 les_total_bytes(p, precision));
+    return DD_OK;
+}
+
+int dd_les_workspace_size(const dd_plan* p, int precision, size_t* bytes) {
+    DD_CHECK_ARG(p && bytes && p->ndim == 3, "dd_les_workspace_size: bad arguments");
+    DD_CHECK_ARG(precision == DD_FP64 || precision == DD_FP32, "precision must be DD_FP64 or DD_FP32");
+    *bytes = les_total_bytes(p, precision);
+    return DD_OK;
+}
+
+int dd_les_rhs3d(const dd_plan* p, const void* const* state, void* const* deriv, const double* inv_k2, int precision,
+                 int zero_nonkept, const dd_closure* cl, void* work, size_t work_bytes, void* stream) {
+    DD_TRY(check3(p, P3_HYDRO, nullptr, state, (const void* const*)deriv));
+    DD_TRY(les_check(p, cl, precision, work, work_bytes));
+    const LesHook h = les_hook(p, precision, cl, work, work_bytes);
+    return rhs3<P3_HYDRO>(p, nullptr, state, deriv, inv_k2, precision, zero_nonkept, work, work_bytes,
+                          (cudaStream_t)stream, &h);
+}
+
+int dd_les_rk4_step3d(const dd_plan* p, void* const* state, const double* inv_k2, const void* const* tab_half,
+                      const void* const* tab_full, const double* coeff, int viscosity_order, double dt, int precision,
+                      const int* nonkept_flag, const dd_closure* cl, void* work, size_t work_bytes, void* stream) {
+    DD_TRY(check3(p, P3_HYDRO, nullptr, (const void* const*)state, nullptr));
+    DD_TRY(les_check(p, cl, precision, work, work_bytes));
+    DD_CHECK_ARG(coeff, "null coefficients");
+    DD_CHECK_ARG(viscosity_order >= 1, "viscosity_order must be >= 1");
+    const LesHook h = les_hook(p, precision, cl, work, work_bytes);
+    return rk4_3<P3_HYDRO>(p, nullptr, state, inv_k2, tab_half, tab_full, coeff, viscosity_order, dt, precision,
+                           nonkept_flag, work, work_bytes, (cudaStream_t)stream, &h);
 }
 
 // Hydro-only forms of the first interface.

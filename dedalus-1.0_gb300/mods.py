@@ -10,12 +10,12 @@ run script of the hot path uses:
 """
 from .config import decfg
 from .representations import FourierRepresentation, GpuFourierRepresentation
-from .physics import Physics, IncompressibleHydro, BoussinesqHydro, IncompressibleMHD
+from .physics import Physics, IncompressibleHydro, BoussinesqHydro, IncompressibleMHD, LESHydro
 from .time_step import RK2mid, RK2trap, RK4
 from .fields import StateData, create_field_classes
 from .kgrid import swap_indices
 from . import init_cond
 
 __all__ = ["decfg", "FourierRepresentation", "GpuFourierRepresentation", "Physics", "IncompressibleHydro",
-           "BoussinesqHydro", "IncompressibleMHD", "RK2mid", "RK2trap", "RK4", "StateData",
+           "BoussinesqHydro", "IncompressibleMHD", "LESHydro", "RK2mid", "RK2trap", "RK4", "StateData",
            "create_field_classes", "swap_indices", "init_cond"]

@@ -62,6 +62,10 @@ class Physics:
     def _finalize(self):
         self._is_finalized = True
 
+    def _precision(self):
+        """Transform precision code of this physics (FFT.precision)."""
+        return precision_code()
+
     def compute_dt(self, data):
         self.dtlist = []
         self.set_dtlist(data)
@@ -192,7 +196,7 @@ class IncompressibleHydro(Physics):
         self._rhs3d(data, deriv, plan)
 
     def _rhs3d(self, data, deriv, plan):
-        prec = precision_code()
+        prec = self._precision()
         n = ctypes.c_size_t()
         _lib.call("dd_rhs3d_workspace_size", plan.handle, self._phys3d, prec, ctypes.byref(n))
         ws = self.workspace(n.value)
@@ -206,23 +210,17 @@ class IncompressibleHydro(Physics):
                   dptr(ws), ws.numel(), current_stream())
         self._mark_kspace(deriv)
 
-    def fused_rk4(self, data, dt):
-        """One fused RK4 step on the device (dd_rk4_step3d) for 3D hydro / MHD;
-        returns False when this physics/grid has no fused step."""
-        if self.ndim != 3 or type(self) not in (IncompressibleHydro, IncompressibleMHD):
-            return False
-        if not self._is_finalized:
-            self._finalize()
+    _fused3d = True
+
+    def _rk4_args(self, data, dt):
+        """Plan, precision, viscosity order, coefficients, 1/k^2 table and the
+        phi-table pointer arrays of a fused 3D RK4 step."""
         names = self._state3d()
         for f, c in names:
             data[f][c].require_space('kspace')
         plan = self.plan(data)
-        prec = precision_code()
         vo = int(self.parameters['viscosity_order'])
         coeffs = [float(self._coeff_of(g)) for g in self._groups3d()]
-        n = ctypes.c_size_t()
-        _lib.call("dd_rhs3d_workspace_size", plan.handle, self._phys3d, prec, ctypes.byref(n))
-        ws = self.workspace(n.value)
         ik2 = self.inv_k2_table(plan)
         th = tf = None
         keep = []
@@ -233,9 +231,23 @@ class IncompressibleHydro(Physics):
             tf, _f = _ptrs(tabs_f)
             keep = [tabs_h, tabs_f, _h, _f]
         sp, _a = _ptrs([data[f][c].kdata for f, c in names])
+        keep.append(_a)
+        cf = (ctypes.c_double * len(coeffs))(*coeffs)
+        return plan, self._precision(), vo, cf, ik2, th, tf, sp, keep
+
+    def fused_rk4(self, data, dt):
+        """One fused RK4 step on the device (dd_rk4_step3d) for 3D hydro / MHD;
+        returns False when this physics/grid has no fused step."""
+        if self.ndim != 3 or not self._fused3d:
+            return False
+        if not self._is_finalized:
+            self._finalize()
+        plan, prec, vo, cf, ik2, th, tf, sp, keep = self._rk4_args(data, dt)
+        n = ctypes.c_size_t()
+        _lib.call("dd_rhs3d_workspace_size", plan.handle, self._phys3d, prec, ctypes.byref(n))
+        ws = self.workspace(n.value)
         pp = self._params3d()
         ppa = None if pp is None else (ctypes.c_double * len(pp))(*pp)
-        cf = (ctypes.c_double * len(coeffs))(*coeffs)
         _lib.call("dd_rk4_step3d", plan.handle, self._phys3d, ppa, sp, None if ik2 is None else dptr(ik2), th, tf,
                   cf, vo, float(dt), prec, None, dptr(ws), ws.numel(), current_stream())
         return True
@@ -250,7 +262,7 @@ class IncompressibleHydro(Physics):
         return None
 
     def _rhs2d(self, data, deriv, plan):
-        prec = precision_code()
+        prec = self._precision()
         n = ctypes.c_size_t()
         _lib.call("dd_rhs2d_workspace_size", plan.handle, 1, prec, ctypes.byref(n))
         ws = self.workspace(n.value)
@@ -278,7 +290,7 @@ class IncompressibleHydro(Physics):
         for f, c in names:
             data[f][c].require_space('kspace')
         plan = self.plan(data)
-        prec = precision_code()
+        prec = self._precision()
         vo = int(self.parameters['viscosity_order'])
         coeffs = [float(self._coeff_of(f)) for f, c in names]
         n = ctypes.c_size_t()
@@ -313,6 +325,8 @@ class IncompressibleHydro(Physics):
 
 class BoussinesqHydro(IncompressibleHydro):
     """physics.py:612-721."""
+
+    _fused3d = False
 
     def __init__(self, *args, **kwargs):
         IncompressibleHydro.__init__(self, *args, **kwargs)
@@ -399,3 +413,59 @@ class IncompressibleMHD(IncompressibleHydro):
         IncompressibleHydro.set_dtlist(self, data)
         dx = data['u']['x'].dx().min()
         self.dtlist.append(dx / self.max_alfven_speed(data))
+
+
+class LESHydro(IncompressibleHydro):
+    """IncompressibleHydro on an LES grid with a learned subgrid closure: the
+    RHS is P[-(u.grad)u - div tau], tau predicted pointwise by the closure
+    network (closure.MLPClosure) from the resolved velocity gradients.  With
+    closure=None it is the unclosed (no-model) LES.  No counterpart in the
+    reference; the closed RHS and RK4 step are dd_les_rhs3d /
+    dd_les_rk4_step3d."""
+
+    _PREC = {'fp64': _lib.DD_FP64, 'fp32': _lib.DD_FP32}
+
+    def __init__(self, *args, closure=None, precision=None, **kwargs):
+        IncompressibleHydro.__init__(self, *args, **kwargs)
+        if self.ndim != 3:
+            raise ValueError("the LES closure is three-dimensional")
+        if precision is not None and precision not in self._PREC:
+            raise NotImplementedError("LES precision must be 'fp64' or 'fp32'")
+        self.closure = closure
+        self.precision = precision
+
+    def _precision(self):
+        if self.precision is None:
+            return IncompressibleHydro._precision(self)
+        return self._PREC[self.precision]
+
+    def _les_ws(self, plan, prec):
+        n = ctypes.c_size_t()
+        _lib.call("dd_les_workspace_size", plan.handle, prec, ctypes.byref(n))
+        return self.workspace(n.value)
+
+    def _rhs3d(self, data, deriv, plan):
+        if self.closure is None:
+            return IncompressibleHydro._rhs3d(self, data, deriv, plan)
+        prec = self._precision()
+        ws = self._les_ws(plan, prec)
+        names = self._state3d()
+        sp, _a = _ptrs([data[f][c].kdata for f, c in names])
+        dp, _b = _ptrs([deriv[f][c].kdata for f, c in names])
+        ik2 = self.inv_k2_table(plan)
+        cl = self.closure.struct()
+        _lib.call("dd_les_rhs3d", plan.handle, sp, dp, None if ik2 is None else dptr(ik2), prec, 1,
+                  ctypes.byref(cl), dptr(ws), ws.numel(), current_stream())
+        self._mark_kspace(deriv)
+
+    def fused_rk4(self, data, dt):
+        if self.closure is None:
+            return IncompressibleHydro.fused_rk4(self, data, dt)
+        if not self._is_finalized:
+            self._finalize()
+        plan, prec, vo, cf, ik2, th, tf, sp, keep = self._rk4_args(data, dt)
+        ws = self._les_ws(plan, prec)
+        cl = self.closure.struct()
+        _lib.call("dd_les_rk4_step3d", plan.handle, sp, None if ik2 is None else dptr(ik2), th, tf, cf, vo,
+                  float(dt), prec, None, ctypes.byref(cl), dptr(ws), ws.numel(), current_stream())
+        return True

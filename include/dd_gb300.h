@@ -229,6 +229,80 @@ int dd_spectrum(const dd_plan* plan, int ncomp, const void* const* comps, double
  * entry outside the kept (dealiased) modes; does not clear it. */
 int dd_any_nonkept(const dd_plan* plan, int ncomp, const void* const* k, int* dflag, void* stream);
 
+/* ------------------------------------------------- learned subgrid closure
+ * No counterpart in the reference: a 64^3 LES of IncompressibleHydro whose
+ * RHS gains -P[d_j tau_ij], tau predicted pointwise by an MLP
+ * 10 -> 64 -> 64 -> 6 (tanh) from the resolved velocity gradients
+ * G[3 i + j] = d_j u_i and the filter width.  Weights are BF16 on the tensor
+ * cores with FP32 accumulation, master weights FP32.
+ *   params: FP32 [nparam] = W1[64][16], b1[64], W2[64][64], b2[64], W3[8][64], b3[8]
+ *   wbf16:  BF16 [nbf16]  = W1[64][16], W2[64][64], W3[16][64] (rows 8..15 zero)
+ *   norm:   FP32 [48] = in_mean[16], in_scale[16], out_mean[8], out_scale[8];
+ *           input a = (feature_a - in_mean[a]) * in_scale[a] (features 0..8 =
+ *           G, 9 = filter width), stress c = y_c * out_scale[c] + out_mean[c]
+ *           in the order xx, yy, zz, xy, xz, yz.
+ * Samples: X [n][16] BF16 (columns 10..15 zero), targets T [n][8] FP32
+ * (columns 6, 7 ignored), raw [n][16] FP32 = G (0..8), width (9), tau (10..15).
+ * All arrays are device memory. */
+typedef struct dd_closure {
+    const void* wbf16;
+    const float* params;
+    const float* norm;
+    double delta;          /* filter width fed to input 9 */
+} dd_closure;
+
+int dd_mlp_sizes(int* nparam, int* nbf16, int* nnorm, int* in_dim, int* out_dim);
+/* Workspace of dd_mlp_grad for a batch of n samples. */
+int dd_mlp_workspace_size(int64_t n, size_t* bytes);
+/* wbf16 = BF16(params). */
+int dd_mlp_pack(const float* params, void* wbf16, void* stream);
+/* Y [n][8] = MLP(X). */
+int dd_mlp_infer(const void* X, float* Y, int64_t n, const void* wbf16, const float* params, void* stream);
+/* Gradient of L = sum_s sum_{c<6} (Y_sc - T_sc)^2 / (6 n_total) over samples
+ * s < n (row idx[s] of X and T when idx is not NULL) into grad [nparam]
+ * (overwritten), and the squared-error sum into loss[0] (if not NULL).
+ * Deterministic: per-block partials reduced in a fixed order. */
+int dd_mlp_grad(const void* X, const float* T, const int64_t* idx, int64_t n, int64_t n_total, const void* wbf16,
+                const float* params, float* grad, float* loss, void* work, size_t work_bytes, void* stream);
+/* One Adam step (step counts from 1) on params, then wbf16 = BF16(params). */
+int dd_mlp_adam(float* params, const float* grad, float* m, float* v, int step, float lr, float beta1, float beta2,
+                float eps, void* wbf16, void* stream);
+/* raw -> normalised X, T. */
+int dd_mlp_normalize(const float* raw, int64_t n, const float* norm, void* X, float* T, void* stream);
+
+/* Training data from a DNS: out (6 FP64 grid-point fields) = u_i u_j in the
+ * order xx, yy, zz, xy, xz, yz. */
+int dd_les_products(int64_t npts, const double* const* u, double* const* out, void* stream);
+/* Sharp spectral filter: copy the modes kept on grid dst (|m_i| <= M_i of dst)
+ * from the full-layout complex128 arrays of grid src to those of dst and zero
+ * the rest of dst.  Both grids 3D with the same box; dst's kept set must lie
+ * inside src's. */
+int dd_les_truncate3(const dd_plan* src, const dd_plan* dst, int nfield, const void* const* s, void* const* d,
+                     void* stream);
+/* Grid-point velocity gradients gx[3 i + j] = d_j u_i of the full-layout
+ * velocity u (3 complex128 arrays); work as for dd_les_workspace_size. */
+int dd_les_gradients(const dd_plan* plan, const void* const* u, double* const* gx, int precision, void* work,
+                     size_t work_bytes, void* stream);
+/* raw[p] = (g_0..8, delta, f_c - fr_c for c = xx, yy, zz, xy, xz, yz) per
+ * grid point: g the gradients, f = filt(u_a u_b) the filtered DNS products and
+ * fr = filt(ubar_a ubar_b) the filtered products of the filtered velocity
+ * (all grid-point values on the LES grid). */
+int dd_les_samples(int64_t npts, const double* const* g, const double* const* f, const double* const* fr,
+                   double delta, float* raw, void* stream);
+/* Grid-point subgrid stress predicted by the closure for velocity u. */
+int dd_les_stress(const dd_plan* plan, const void* const* u, double* const* tau, const dd_closure* cl,
+                  int precision, void* work, size_t work_bytes, void* stream);
+/* Workspace of dd_les_gradients, dd_les_stress, dd_les_rhs3d and dd_les_rk4_step3d. */
+int dd_les_workspace_size(const dd_plan* plan, int precision, size_t* bytes);
+/* RHS of the closed LES: dd_rhs3d (physics 0) plus -P[d_j tau_ij]. */
+int dd_les_rhs3d(const dd_plan* plan, const void* const* state, void* const* deriv, const double* inv_k2,
+                 int precision, int zero_nonkept, const dd_closure* cl, void* work, size_t work_bytes, void* stream);
+/* One RK4 step of the closed LES, as dd_rk4_step3d (physics 0) with the
+ * closure term in every stage. */
+int dd_les_rk4_step3d(const dd_plan* plan, void* const* state, const double* inv_k2, const void* const* tab_half,
+                      const void* const* tab_full, const double* coeff, int viscosity_order, double dt, int precision,
+                      const int* nonkept_flag, const dd_closure* cl, void* work, size_t work_bytes, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -42,3 +42,21 @@ def test_version_and_error_string(dd):
     L = dd._lib.lib()
     assert L.dd_version() >= 100
     assert isinstance(L.dd_last_error(), bytes)
+
+
+def _arity():
+    out = {}
+    for fn in os.listdir(os.path.join(ROOT, "include")):
+        if fn.endswith(".h"):
+            txt = open(os.path.join(ROOT, "include", fn)).read()
+            txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+            for m in re.finditer(r"^\s*[A-Za-z_][\w \*]*?\b(dd_\w+)\s*\(([^)]*)\)\s*;", txt, flags=re.M):
+                args = m.group(2).strip()
+                out[m.group(1)] = 0 if args in ("", "void") else args.count(",") + 1
+    return out
+
+
+def test_binding_arity_matches_header(dd):
+    ar = _arity()
+    bad = {n: (ar[n], len(a)) for n, a in dd._lib.SIGNATURES.items() if ar.get(n) != len(a)}
+    assert not bad, bad

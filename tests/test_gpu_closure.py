@@ -1,0 +1,283 @@
+"""Learned subgrid closure on the GPU against the CPU oracle (oracle/closure.py):
+MLP forward and gradients with the kernels' BF16 rounding points, Adam,
+determinism, training, the filtered-DNS samples, and the closure term of the
+LES right-hand side.
+
+Tolerances: the network runs BF16 x BF16 -> FP32 on the tensor cores, the
+oracle the same roundings in FP64; an FP32 value that sits on a BF16 rounding
+boundary can round the other way, so forward outputs are compared to 2e-3 of
+their scale and gradients to 2e-3 relative L2 per tensor.  The sample
+pipeline (FP64 transforms, FP32 output) is compared to 1e-6 of each column's
+scale, the plain part of the LES RHS bitwise."""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+from oracle import closure as OC
+
+
+def _params(seed=0):
+    rng = np.random.Generator(np.random.PCG64(seed + 100))
+    w = OC.unpack(OC.init_params(seed).astype(np.float64))
+    w["b1"][:] = rng.normal(0, 0.1, 64)
+    w["b2"][:] = rng.normal(0, 0.1, 64)
+    w["b3"][:6] = rng.normal(0, 0.1, 6)
+    return OC.pack(w).astype(np.float32)
+
+
+def _data(n, seed=1):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    X = np.zeros((n, 16), dtype=np.float32)
+    X[:, :10] = rng.normal(0, 1, (n, 10))
+    X = OC.bf16(X).astype(np.float32)
+    T = np.zeros((n, 8), dtype=np.float32)
+    T[:, :6] = rng.normal(0, 1, (n, 6))
+    return X, T
+
+
+def _closure(dd, p, delta=0.15):
+    import torch
+    c = dd.closure.MLPClosure(delta)
+    c.params.copy_(torch.from_numpy(p))
+    c.pack()
+    return c
+
+
+def _dev(a, dtype=None):
+    import torch
+    t = torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    return t.to(dtype) if dtype is not None else t
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(np.asarray(a) - b) / max(np.linalg.norm(b), 1e-300))
+
+
+@pytest.mark.gpu
+def test_mlp_forward_matches_oracle(dd, cuda):
+    import torch
+    p = _params(0)
+    X, _ = _data(1000)
+    c = _closure(dd, p)
+    Y = c.predict(_dev(X, torch.bfloat16)).cpu().numpy()
+    Yo, _ = OC.forward(p, X)
+    assert np.max(np.abs(Y[:, :6] - Yo[:, :6])) <= 2e-3 * np.max(np.abs(Yo[:, :6]))
+    assert _rel(Y[:, :6], Yo[:, :6]) < 1e-3
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,gather", [(1000, False), (777, True), (64 * 600 + 5, False)])
+def test_mlp_gradient_matches_oracle(dd, cuda, n, gather):
+    import torch
+    p = _params(1)
+    X, T = _data(n + 50 if gather else n, seed=2)
+    c = _closure(dd, p)
+    Xd, Td = _dev(X, torch.bfloat16), _dev(T)
+    if gather:
+        idx = np.random.Generator(np.random.PCG64(9)).permutation(len(X))[:n]
+        c.gradient(Xd, Td, idx=_dev(idx.astype(np.int64)), n=n)
+        go, sse_o = OC.grad(p, X[idx], T[idx])
+    else:
+        c.gradient(Xd, Td)
+        go, sse_o = OC.grad(p, X, T)
+    g = c.grad_buf.cpu().numpy()
+    sse = float(c.loss_buf.item())
+    assert abs(sse - sse_o) <= 1e-4 * sse_o
+    gu, gou = OC.unpack(g.astype(np.float64)), OC.unpack(go)
+    for name in gu:
+        assert _rel(gu[name], gou[name]) < 2e-3, name
+    assert np.all(gu["W1"][:, 10:] == 0) and np.all(gu["W3"][6:] == 0)
+
+
+@pytest.mark.gpu
+def test_mlp_gradient_is_deterministic(dd, cuda):
+    import torch
+    X, T = _data(50000, seed=3)
+    c = _closure(dd, _params(2))
+    Xd, Td = _dev(X, torch.bfloat16), _dev(T)
+    c.gradient(Xd, Td)
+    a = c.grad_buf.clone()
+    c.gradient(Xd, Td)
+    assert torch.equal(a, c.grad_buf)
+
+
+@pytest.mark.gpu
+def test_adam_step(dd, cuda):
+    import torch
+    p = _params(3)
+    c = _closure(dd, p)
+    rng = np.random.Generator(np.random.PCG64(4))
+    g = rng.normal(0, 1e-2, p.size).astype(np.float32)
+    c.grad_buf.copy_(torch.from_numpy(g))
+    c.adam(1e-3)
+    m = (np.float32(0.1) * g).astype(np.float32)
+    v = (np.float32(0.001) * g * g).astype(np.float32)
+    ref = p - np.float32(1e-3) * (m / np.float32(0.1)) / (np.sqrt(v / np.float32(0.001)) + np.float32(1e-8))
+    assert np.allclose(c.params.cpu().numpy(), ref, rtol=1e-5, atol=1e-9)
+    wb = c.wbf16.float().cpu().numpy()
+    assert np.array_equal(wb[:1024], OC.bf16(c.params.cpu().numpy()[:1024]).astype(np.float32))
+
+
+@pytest.mark.gpu
+def test_training_fits_a_teacher_network(dd, cuda):
+    """Targets from a different network of the same shape: Adam on the GPU
+    kernels reduces the error by more than an order of magnitude."""
+    import torch
+    n = 1 << 17
+    X, _ = _data(n, seed=5)
+    teacher = _params(7)
+    Yt, _ = OC.forward(teacher, X)
+    T = np.zeros((n, 8), dtype=np.float32)
+    T[:, :6] = Yt[:, :6]
+    c = _closure(dd, _params(8))
+    Xd, Td = _dev(X, torch.bfloat16), _dev(T)
+    idx = torch.arange(n, device="cuda", dtype=torch.int64)
+    before = c.mse(Xd, Td)
+    hist = dd.closure.train(c, Xd, Td, idx, epochs=6, batch=8192, lr=3e-3, lr_min=1e-4)
+    after = c.mse(Xd, Td)
+    assert after < before / 10, (before, after, hist)
+
+
+@pytest.mark.gpu
+def test_filtered_samples_match_oracle(dd, cuda):
+    import torch
+    dns, les = (32, 32, 32), (16, 16, 16)
+    u = dd.init_cond.turbulence_3d(dns, seed=11)
+    s = dd.closure.FilteredSampler(dns, les)
+    raw = torch.empty((int(np.prod(les)), 16), dtype=torch.float32, device="cuda")
+    s.samples([_dev(c) for c in u], raw)
+    r = raw.cpu().numpy()
+    ro = OC.samples(u, dns, les, s.delta)
+    for col in range(16):
+        scale = np.max(np.abs(ro[:, col]))
+        assert np.max(np.abs(r[:, col] - ro[:, col])) <= 1e-6 * scale + 1e-30, col
+
+
+@pytest.mark.gpu
+def test_truncation_copies_kept_modes(dd, cuda):
+    import torch
+    dns, les = (64, 64, 64), (32, 32, 32)
+    u = dd.init_cond.turbulence_3d(dns, seed=12)
+    s = dd.closure.FilteredSampler(dns, les)
+    out = s.filter_velocity([_dev(c) for c in u])
+    for a in range(3):
+        assert np.array_equal(out[a].cpu().numpy(), OC.truncate(u[a], dns, les))
+
+
+def _les_pair(dd, shape, closure, u):
+    M = dd.mods
+    R = M.LESHydro(shape, M.FourierRepresentation, closure=closure)
+    R.parameters['nu'] = 5e-3
+    d = R.create_fields(0.)
+    for i in range(3):
+        d['u'][i]['kspace'] = u[i].copy()
+    return R, d
+
+
+def _norm_for(dd, shape, u, delta):
+    """Normalisation of the network inputs from the field's own gradients."""
+    G = OC.gradients(u, shape)
+    g = np.stack([x.ravel() for x in G], 1)
+    in_mean = np.zeros(10)
+    in_scale = np.ones(10)
+    in_mean[:9] = g.mean(0)
+    in_scale[:9] = 1.0 / g.std(0)
+    in_scale[9] = 1.0 / delta
+    return in_mean, in_scale, np.array([0.05, 0.04, 0.03, 0.0, 0.01, -0.01]), np.full(6, 0.02)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape", [(16, 16, 16), (32, 32, 32)])
+def test_les_closure_term_matches_oracle(dd, cuda, shape):
+    u = dd.init_cond.turbulence_3d(shape, seed=21)
+    delta = np.pi / (np.ceil(shape[0] / 3) - 1)
+    c = _closure(dd, _params(4), delta)
+    c.set_norm(*_norm_for(dd, shape, u, delta))
+    Rl, dl = _les_pair(dd, shape, c, u)
+    Rp, dp = _les_pair(dd, shape, None, u)
+    kl, kp = Rl.create_fields(0.), Rp.create_fields(0.)
+    Rl.RHS(dl, kl)
+    Rp.RHS(dp, kp)
+    term = [kl['u'][i].to_numpy('kspace') - kp['u'][i].to_numpy('kspace') for i in range(3)]
+    ref = OC.closure_term(u, shape, c.params.cpu().numpy(), c.norm.cpu().numpy(), delta)
+    num = np.sqrt(sum(np.sum(np.abs(a - b) ** 2) for a, b in zip(term, ref)))
+    den = np.sqrt(sum(np.sum(np.abs(b) ** 2) for b in ref))
+    assert den > 0 and num / den < 2e-3, num / den
+
+
+@pytest.mark.gpu
+def test_zero_stress_leaves_hydro_rhs_bitwise(dd, cuda):
+    import torch
+    shape = (32, 32, 32)
+    u = dd.init_cond.turbulence_3d(shape, seed=22)
+    p = _params(5)
+    w = OC.unpack(p.astype(np.float64))
+    w["W3"][:] = 0.0
+    w["b3"][:] = 0.0
+    c = _closure(dd, OC.pack(w).astype(np.float32), 0.2)
+    Rl, dl = _les_pair(dd, shape, c, u)
+    Rp, dp = _les_pair(dd, shape, None, u)
+    kl, kp = Rl.create_fields(0.), Rp.create_fields(0.)
+    Rl.RHS(dl, kl)
+    Rp.RHS(dp, kp)
+    for i in range(3):
+        assert torch.equal(kl['u'][i].kdata, kp['u'][i].kdata)
+
+
+@pytest.mark.gpu
+def test_fused_les_step_matches_generic_rk4(dd, cuda):
+    shape = (32, 32, 32)
+    u = dd.init_cond.turbulence_3d(shape, seed=23)
+    delta = np.pi / 10
+    c = _closure(dd, _params(6), delta)
+    c.set_norm(*_norm_for(dd, shape, u, delta))
+    M = dd.mods
+    Ra, da = _les_pair(dd, shape, c, u)
+    Rb, db = _les_pair(dd, shape, c, u)
+    ta, tb = M.RK4(Ra), M.RK4(Rb)
+    tb.use_fused = False
+    for _ in range(3):
+        ta.advance(da, 2e-3)
+        tb.advance(db, 2e-3)
+    for i in range(3):
+        a, b = da['u'][i].to_numpy('kspace'), db['u'][i].to_numpy('kspace')
+        assert _rel(a, b) < 1e-6
+    # and the closure changed the solution
+    Rn, dn = _les_pair(dd, shape, None, u)
+    tn = M.RK4(Rn)
+    for _ in range(3):
+        tn.advance(dn, 2e-3)
+    assert _rel(dn['u'][0].to_numpy('kspace'), da['u'][0].to_numpy('kspace')) > 1e-8
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("fused", [True, False])
+def test_les_rk4_step_matches_oracle(dd, cuda, fused):
+    """One RK4 step of the closed LES (fused C-ABI step and the generic
+    integrator over dd_les_rhs3d) against the oracle's RK4 over the oracle
+    RHS + closure term: the step increments agree to 1e-3 relative L2."""
+    from oracle import time_step as OT
+    shape = (32, 32, 32)
+    u = dd.init_cond.turbulence_3d(shape, seed=24)
+    delta = np.pi / 10
+    c = _closure(dd, _params(6), delta)
+    c.set_norm(*_norm_for(dd, shape, u, delta))
+    R, d = _les_pair(dd, shape, c, u)
+    ti = dd.mods.RK4(R)
+    ti.use_fused = fused
+    ti.advance(d, 2e-3)
+    ro = OC.les_physics(shape, c.params.cpu().numpy(), c.norm.cpu().numpy(), delta)
+    ro.parameters['nu'] = 5e-3
+    do = ro.create_fields(0.)
+    for i in range(3):
+        do['u'][i]['kspace'] = u[i].copy()
+    OT.RK4(ro).do_advance(do, 2e-3)
+    num = den = 0.0
+    for i in range(3):
+        a = d['u'][i].to_numpy('kspace') - u[i]
+        b = do['u'][i]['kspace'] - u[i]
+        num += np.sum(np.abs(a - b) ** 2)
+        den += np.sum(np.abs(b) ** 2)
+    assert np.sqrt(num / den) < 1e-3, np.sqrt(num / den)

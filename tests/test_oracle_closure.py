@@ -1,0 +1,98 @@
+"""The closure oracle (oracle/closure.py) pinned on the CPU: the analytic MLP
+gradient against central finite differences, the BF16 rounding helper against
+known values, and the sharp-filter identity of the training stress."""
+import numpy as np
+import pytest
+
+from oracle import closure as OC
+
+
+def _problem(n=37, seed=0):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    p = OC.init_params(seed).astype(np.float64)
+    w = OC.unpack(p.copy())
+    w["b1"][:] = rng.normal(0, 0.1, 64)
+    w["b2"][:] = rng.normal(0, 0.1, 64)
+    w["b3"][:6] = rng.normal(0, 0.1, 6)
+    p = OC.pack(w)
+    X = np.zeros((n, 16))
+    X[:, :10] = rng.normal(0, 1, (n, 10))
+    T = np.zeros((n, 8))
+    T[:, :6] = rng.normal(0, 1, (n, 6))
+    return p, X, T
+
+
+def test_exact_gradient_matches_finite_differences():
+    p, X, T = _problem()
+    g, _ = OC.grad(p, X, T, rounding=False)
+    rng = np.random.Generator(np.random.PCG64(5))
+    live = [i for i in range(OC.NPARAM) if g[i] != 0.0]
+    pick = rng.choice(live, 60, replace=False)
+    h = 1e-6
+    for i in pick:
+        a, b = p.copy(), p.copy()
+        a[i] += h
+        b[i] -= h
+        fd = (OC.loss(a, X, T, rounding=False)[0] - OC.loss(b, X, T, rounding=False)[0]) / (2 * h)
+        assert abs(fd - g[i]) <= 1e-7 * max(1.0, abs(g[i])), (i, fd, g[i])
+
+
+def test_unused_inputs_and_outputs_get_zero_gradient():
+    p, X, T = _problem()
+    g = OC.unpack(OC.grad(p, X, T)[0])
+    assert np.all(g["W1"][:, 10:] == 0)
+    assert np.all(g["W3"][6:] == 0) and np.all(g["b3"][6:] == 0)
+
+
+def test_bf16_rounding():
+    v = np.array([1.0, 1.0 + 2.0 ** -8, 1.0 + 3 * 2.0 ** -8, -2.5, 3.0e-3, 1.0 + 2.0 ** -7])
+    r = OC.bf16(v)
+    assert r[0] == 1.0
+    assert r[1] == 1.0                       # tie -> even
+    assert r[2] == 1.0 + 2.0 ** -6           # tie -> even (upwards)
+    assert r[3] == -2.5
+    assert abs(r[4] - 3.0e-3) <= 3.0e-3 * 2.0 ** -8
+    assert r[5] == 1.0 + 2.0 ** -7
+
+
+def test_sharp_filter_identity():
+    """A DNS field that is band-limited to the LES kept set gives stresses
+    whose kept modes vanish: filt(uu) - filt(ubar ubar) = 0."""
+    dns, les = (24, 24, 24), (12, 12, 12)
+    rng = np.random.Generator(np.random.PCG64(2))
+    keep = OC.kept_mask(les)
+    u = []
+    for _ in range(3):
+        x = rng.normal(size=les)
+        u.append(OC.to_k(x) * keep)
+    # embed on the DNS grid
+    u_dns = []
+    kxl, kyl, kzl = OC.kvectors(les)
+    for c in u:
+        big = np.zeros((dns[1], dns[0], dns[2] // 2 + 1), dtype=np.complex128)
+        for iy in range(les[1]):
+            for iz in range(les[0]):
+                big[int(kyl.ravel()[iy]) % dns[1], int(kzl.ravel()[iz]) % dns[0], :les[2] // 2 + 1] = c[iy, iz]
+        u_dns.append(big * OC.kept_mask(dns))
+    raw = OC.samples(u_dns, dns, les, delta=np.pi / 3)
+    assert np.all(raw[:, 9] == np.float32(np.pi / 3))
+    scale = max(np.max(np.abs(OC.to_x(c, les))) for c in u) ** 2
+    assert np.max(np.abs(raw[:, 10:])) < 1e-12 * scale
+    # gradients are those of the filtered field itself
+    G = OC.gradients(u, les)
+    assert np.allclose(raw[:, 0].reshape(les), G[0], atol=1e-5 * np.max(np.abs(G[0])))
+
+
+def test_constant_stress_gives_no_closure_term():
+    shape = (12, 12, 12)
+    rng = np.random.Generator(np.random.PCG64(3))
+    u = [OC.to_k(rng.normal(size=shape)) for _ in range(3)]
+    p = OC.init_params(1)
+    w = OC.unpack(p.astype(np.float64))
+    w["W3"][:] = 0.0
+    norm = np.zeros(48, dtype=np.float32)
+    norm[16:32] = 1.0
+    norm[40:48] = 1.0
+    norm[32:38] = [0.3, 0.2, 0.1, 0.05, 0.0, -0.1]
+    t = OC.closure_term(u, shape, OC.pack(w), norm, 0.1)
+    assert max(np.max(np.abs(c)) for c in t) < 1e-14
