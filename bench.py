@@ -15,8 +15,13 @@ configuration of the project):
     hydro3d-128-fp64              the same at 128^3
     mhd3d-256-{fp32,fp64}         3D MHD 256^3 RK4, nu = eta = 5e-3, dt = 1e-3
     hydro2d-128                   2D hydro 128^2 RK2mid, nu = 1e-3, dt = 1e-3
-    bouss2d-ensemble-512          512 2D Boussinesq runs, sizes uniform in {64,128,256,512}^2,
+    bouss2d-ensemble-512[-fp32]   512 2D Boussinesq runs, sizes uniform in {64,128,256,512}^2,
                                   nu = kappa = 2e-3, N^2 = 1, RK2mid, dt = 1e-2, one CUDA graph per step
+                                  (FP64 or autotuned FP32 transforms; the FP32 line reports its
+                                  difference from the FP64 ensemble)
+    les64-closure                 64^3 LES with the learned subgrid closure (trained weights in
+                                  dedalus-1.0_gb300/data), RK4, nu = 5e-3, dt = 2e-3, FP32 transforms,
+                                  one CUDA graph per step; reports the FP64 256^3 DNS rate beside it
 
 Prints one JSON line (rank 0).  Multi-GPU runs are independent replicas (weak
 scaling, no collective on the data path).  ``--impl reference`` times the
@@ -48,6 +53,9 @@ WORKLOADS = {
     "hydro2d-128": dict(kind="hydro2d", shape=(128, 128), nu=1e-3, dt=1e-3, precision="fp64"),
     "bouss2d-ensemble-512": dict(kind="ensemble", nrun=512, sizes=(64, 128, 256, 512), nu=2e-3, dt=1e-2,
                                  precision="fp64"),
+    "bouss2d-ensemble-512-fp32": dict(kind="ensemble", nrun=512, sizes=(64, 128, 256, 512), nu=2e-3, dt=1e-2,
+                                      precision="fp32"),
+    "les64-closure": dict(kind="les", shape=(64,) * 3, nu=5e-3, dt=2e-3, precision="fp32"),
 }
 
 
@@ -164,9 +172,12 @@ class Hydro2Runner:
             self.data["u"][i]["kspace"] = self.host[i]
         self.ti = M.RK2mid(self.rhs)
         self.launches_per_step = None
+        self.launch_bound = True
 
     def step(self):
         self.ti.do_advance(self.data, self.wl["dt"])
+
+    eager_step = step
 
     def state(self):
         return [self.data["u"][i].kdata for i in range(2)]
@@ -212,6 +223,9 @@ class EnsembleRunner:
     def step(self):
         self.ens.step(self.wl["dt"])
 
+    def eager_step(self):
+        self.ens.step(self.wl["dt"], graph=False)
+
     def state(self):
         return [c.slab for c in self.ens.classes]
 
@@ -237,7 +251,84 @@ class EnsembleRunner:
         return "512-run 2D Boussinesq ensemble steps/s", "ensemble steps/s"
 
 
-RUNNERS = {"hydro3d": Hydro3Runner, "mhd3d": Hydro3Runner, "hydro2d": Hydro2Runner, "ensemble": EnsembleRunner}
+class LesRunner:
+    """64^3 LES with the learned closure: the fused closed RK4 step
+    (dd_les_rk4_step3d), replayed as one CUDA graph per step."""
+
+    def __init__(self, dd, wl, rank):
+        import torch
+        self.torch, self.dd, self.wl = torch, dd, wl
+        C = dd.closure
+        if not os.path.isfile(C.DEFAULT_WEIGHTS):
+            raise FileNotFoundError("trained closure weights missing: %s" % C.DEFAULT_WEIGHTS)
+        self.cl = C.MLPClosure.load(C.DEFAULT_WEIGHTS)
+        self.rhs, self.data, self.ti = C.les_problem(wl["shape"][0], wl["nu"], self.cl, wl["precision"])
+        self.host = dd.init_cond.turbulence_3d(wl["shape"], seed=rank)
+        for i in range(3):
+            self.data["u"][i]["kspace"] = self.host[i]
+        for _ in range(2):
+            self.eager_step()
+        torch.cuda.synchronize()
+        self.graph = torch.cuda.CUDAGraph()
+        cap = torch.cuda.Stream()
+        cap.wait_stream(torch.cuda.current_stream())
+        n0 = dd._lib.launch_count()
+        with torch.cuda.stream(cap):
+            with torch.cuda.graph(self.graph, stream=cap):
+                self.eager_step()
+        torch.cuda.current_stream().wait_stream(cap)
+        torch.cuda.synchronize()
+        self.launches_per_step = dd._lib.launch_count() - n0
+        for i in range(3):
+            self.data["u"][i]["kspace"] = self.host[i]
+
+    def step(self):
+        self.graph.replay()
+
+    def eager_step(self):
+        self.ti.do_advance(self.data, self.wl["dt"])
+
+    api_step = eager_step
+
+    def state(self):
+        return [self.data["u"][i].kdata for i in range(3)]
+
+    def bytes_per_step(self):
+        N = self.wl["shape"][0]
+        # 4 RHS x 21 transforms (u 3, grad u 9, u x w 3, tau 6) + 4 stages x 3 components x 3 complex passes
+        return 4 * 21 * B3(N) + 4 * 3 * 3 * C3(N)
+
+    def point_stages(self):
+        return float(np.prod(self.wl["shape"])) * 4
+
+    def kernel_bytes(self, label):
+        n = int(np.prod(self.wl["shape"]))
+        if label == "les_mlp":
+            return 15 * 8 * n          # 9 gradients in, 6 stresses out (FP64)
+        return None
+
+    def kernel_flops(self, label):
+        if label == "les_mlp":
+            return 2 * (10 * 64 + 64 * 64 + 64 * 6) * int(np.prod(self.wl["shape"]))
+        return None
+
+    def config(self, ws):
+        w = self.wl
+        meta = self.cl.meta or {}
+        return {"workload": "64^3 LES of 3D incompressible hydro with the learned subgrid closure (MLP "
+                            "10-64-64-6, BF16 tensor cores), RK4, dt=%g, nu=%g, 2/3 dealiasing, %s transforms, "
+                            "one CUDA graph per step" % (w["dt"], w["nu"], w["precision"]),
+                "grid": list(w["shape"]), "integrator": "RK4", "dt": w["dt"], "precision": w["precision"],
+                "closure_weights": os.path.basename(self.dd.closure.DEFAULT_WEIGHTS),
+                "closure_training": meta.get("data"), "closure_accuracy": meta.get("eval"),
+                "parallelism": "replicas x%d" % ws, "l2": "state fits in L2 (launch/latency-bound workload)"}
+
+    def metric(self):
+        return "64³ LES + closure steps/s", "steps/s"
+
+
+RUNNERS = {"hydro3d": Hydro3Runner, "mhd3d": Hydro3Runner, "hydro2d": Hydro2Runner, "ensemble": EnsembleRunner,
+           "les": LesRunner}
 
 
 # ---------------------------------------------------------------- CPU side
@@ -260,6 +351,13 @@ def cpu_reference_steps(wl, nsteps, workers, time_budget, seed=0):
         ti_cls = OT.RK4
     elif kind == "hydro3d":
         rhs = OP.IncompressibleHydro(shape, OR.FourierRepresentation)
+        rhs.parameters["nu"] = wl["nu"]
+        fields = list(zip([("u", 0), ("u", 1), ("u", 2)], dd.init_cond.turbulence_3d(shape, seed=seed)))
+        ti_cls = OT.RK4
+    elif kind == "les":
+        from oracle import closure as OC
+        z = np.load(dd.closure.DEFAULT_WEIGHTS)
+        rhs = OC.les_physics(shape, z["params"], z["norm"], float(z["delta"]))
         rhs.parameters["nu"] = wl["nu"]
         fields = list(zip([("u", 0), ("u", 1), ("u", 2)], dd.init_cond.turbulence_3d(shape, seed=seed)))
         ti_cls = OT.RK4
@@ -337,7 +435,8 @@ def run_reference(args, wl, ws, rank):
 def metric_of(wl):
     return {"hydro3d": (HEADLINE, "steps/s"), "mhd3d": ("256³ MHD steps/s", "steps/s"),
             "hydro2d": ("128² 2D hydro steps/s", "steps/s"),
-            "ensemble": ("512-run 2D Boussinesq ensemble steps/s", "ensemble steps/s")}[wl["kind"]]
+            "ensemble": ("512-run 2D Boussinesq ensemble steps/s", "ensemble steps/s"),
+            "les": ("64³ LES + closure steps/s", "steps/s")}[wl["kind"]]
 
 
 # ---------------------------------------------------------------- clocks
@@ -456,7 +555,11 @@ def main():
 
     sampler = ClockSampler(gpu_uuid(torch, local))
     sampler.start()
-    dd._lib.timing_enable(run.launches_per_step is None)   # per-launch events only for non-graph workloads
+    # per-launch CUDA events inside the timed region only where their host cost
+    # is negligible (not for CUDA-graph or launch-bound workloads, whose kernel
+    # table comes from a separate eager pass after the timed region)
+    events_in_timed = run.launches_per_step is None and not getattr(run, "launch_bound", False)
+    dd._lib.timing_enable(events_in_timed)
     dd._lib.timing_reset()
     n0 = dd._lib.launch_count()
     barrier()
@@ -472,9 +575,21 @@ def main():
     if run.launches_per_step is not None:
         launches = run.launches_per_step * args.steps      # graph replays launch the captured kernels
     ms = max_over_ranks(e0.elapsed_time(e1))
-    kt = dd._lib.timing_report()
-    dd._lib.timing_enable(False)
     clocks = sampler.stop()
+    kt = dd._lib.timing_report() if events_in_timed else {}
+    kernel_timing = "CUDA events per launch inside the timed region"
+    if not events_in_timed and hasattr(run, "eager_step"):
+        kp = max(3, min(args.steps, 20))
+        dd._lib.timing_enable(True)
+        run.eager_step()
+        torch.cuda.synchronize()
+        dd._lib.timing_reset()
+        for _ in range(kp):
+            run.eager_step()
+        torch.cuda.synchronize()
+        kt = dd._lib.timing_report()
+        kernel_timing = "CUDA events per launch in a separate eager pass of %d steps after the timed region" % kp
+    dd._lib.timing_enable(False)
     ms_per_step = ms / args.steps
     value = ws * args.steps / (ms / 1e3)
 
@@ -484,6 +599,7 @@ def main():
         peaks = json.load(open(pk))
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    bf16_peak = float(peaks.get("bf16_tflops", 1900.0))
     kernels, roofline = {}, None
     total_kt = sum(v[1] for v in kt.values()) or 1.0
     for name, (cnt, tot) in sorted(kt.items(), key=lambda kv: -kv[1][1]):
@@ -498,7 +614,11 @@ def main():
         ach = b / avg / 1e9 if b else None
         roofline = {"bound": "hbm", "kernel": name, "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
                     "frac": (ach / hbm_peak) if ach else None, "traffic": None, "peak_source": peak_src,
-                    "algorithmic_bytes_per_launch": b, "avg_launch_ms": avg * 1e3}
+                    "algorithmic_bytes_per_launch": b, "avg_launch_ms": avg * 1e3, "kernel_timing": kernel_timing}
+        fl = getattr(run, "kernel_flops", lambda _n: None)(name)
+        if fl:
+            roofline["tensor"] = {"achieved": fl / avg / 1e12, "peak": bf16_peak, "unit": "TFLOP/s",
+                                  "frac": fl / avg / 1e12 / bf16_peak, "algorithmic_flops_per_launch": fl}
     else:
         ach = B / (ms_per_step / 1e3) / 1e9
         roofline = {"bound": "hbm", "kernel": "whole step (CUDA graph)", "achieved": ach, "peak": hbm_peak,
@@ -521,10 +641,11 @@ def main():
         torch.cuda.synchronize()
         f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         f0.record(stream)
+        api_step = getattr(run, "api_step", run.step)
         for _ in range(ke):
             for d, h in zip(dev_state, host_in):
                 d.copy_(h, non_blocking=True)
-            run.step()
+            api_step()
             for d, h in zip(dev_state, host_out):
                 h.copy_(d, non_blocking=True)
         f1.record(stream)
@@ -532,7 +653,8 @@ def main():
         me = max_over_ranks(f0.elapsed_time(f1))
         nb = sum(h.numel() * h.element_size() for h in host_in)
         e2e = {"value": ws * ke / (me / 1e3), "unit": run.metric()[1], "h2d_bytes_per_step": nb,
-               "d2h_bytes_per_step": nb, "steps": ke}
+               "d2h_bytes_per_step": nb, "steps": ke,
+               "path": "eager public API (ti.advance)" if hasattr(run, "api_step") else "same step as value"}
 
     # the headline workload with the other transform arithmetics, each with its
     # difference from the FP64 state after the same steps
@@ -566,6 +688,57 @@ def main():
                               "rel_l2_vs_fp64_after_%d_steps" % (kv + 1): (num / den) ** 0.5}
         variants["fp64_repeat"] = {"steps_per_s": ws * 1e3 / ms64, "ms_per_step": ms64}
 
+    # FP32 transforms against FP64 from the same state: per-field error and
+    # total-energy drift (MHD), or the whole-ensemble error (ensemble)
+    if not args.no_variants and wl["kind"] in ("mhd3d", "ensemble") and wl["precision"] == "fp32":
+        kv = max(3, min(args.steps, 10))
+        variants = {"steps_compared": kv}
+
+        def states(prec):
+            w2 = dict(wl, precision=prec)
+            r = RUNNERS[wl["kind"]](dd, w2, rank)
+            series = []
+            for _ in range(kv):
+                r.step()
+                if wl["kind"] == "mhd3d":
+                    series.append(dd.diagnostics.ekin(r.data) + dd.diagnostics.emag(r.data))
+            torch.cuda.synchronize()
+            out = [x.clone() for x in r.state()]
+            dd.config.decfg.set("FFT", "precision", wl["precision"])
+            return out, series
+
+        s32, e32 = states("fp32")
+        s64, e64 = states("fp64")
+        if wl["kind"] == "mhd3d":
+            names = ["u_x", "u_y", "u_z", "B_x", "B_y", "B_z"]
+            variants["per_field_rel_l2_vs_fp64"] = {
+                n: float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(b))
+                for n, a, b in zip(names, s32, s64)}
+            variants["total_energy_fp64"] = e64
+            variants["total_energy_drift_fp32_vs_fp64"] = [(a - b) / b for a, b in zip(e32, e64)]
+        else:
+            num = sum(float(torch.sum(torch.abs(a - b) ** 2)) for a, b in zip(s32, s64))
+            den = sum(float(torch.sum(torch.abs(b) ** 2)) for b in s64)
+            variants["ensemble_rel_l2_vs_fp64"] = (num / den) ** 0.5
+
+    # the LES against the plain FP64 DNS it stands in for (256^3, same nu, dt)
+    versus_dns = None
+    if wl["kind"] == "les":
+        rd = Hydro3Runner(dd, WORKLOADS["hydro3d-256-fp64"], rank)
+        rd.step()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(3):
+            rd.step()
+        b.record(stream)
+        torch.cuda.synchronize()
+        dns = 3e3 / a.elapsed_time(b)
+        versus_dns = {"dns_256_fp64_steps_per_s": dns, "les_over_dns": (value / ws) / dns,
+                      "target": ">= 20x the plain-DNS steps/s"}
+        del rd
+        dd.config.decfg.set("FFT", "precision", "fp64")
+
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         times = cpu_reference_steps(wl, 1, 1, 60.0)
@@ -582,10 +755,16 @@ def main():
     metric, unit = run.metric()
     line = {"metric": metric, "value": value, "unit": unit, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": {"fp64": "f64", "df64": "df64", "fp32": "f32"}[wl["precision"]],
-            "data": DATA3 if "3d" in wl["kind"] else "synthetic (seeded)", "config": run.config(ws),
+            "vs_baseline": None,
+            "dtype": {"fp64": "f64", "df64": "df64", "fp32": "f32"}[wl["precision"]] + (
+                "+bf16 (closure MLP)" if wl["kind"] == "les" else ""),
+            "data": (DATA3 if wl["kind"] in ("hydro3d", "mhd3d", "les") else "synthetic (seeded)") + (
+                "; closure trained on filtered snapshots of the FP64 256^3 DNS of the same generator"
+                if wl["kind"] == "les" else ""), "config": run.config(ws),
             "clocks": clocks, "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
             "step_roofline": step_hbm, "kernels": kernels, "variants": variants, "cpu_baseline": cpu}
+    if versus_dns is not None:
+        line["versus_dns"] = versus_dns
     print(json.dumps(line))
     return 0
 

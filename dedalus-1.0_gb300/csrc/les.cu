@@ -51,36 +51,78 @@ __global__ void k_les_grad9(Geo3 g, const double* kx, const double* ky, const do
     }
 }
 
-// Per tile of 64 grid points: the 9 gradients and the width are normalised to
-// BF16 network inputs, the MLP runs on the tensor cores and the 6 stresses are
-// written.  tau may alias gx[0..5]: a block reads all inputs of a tile before
-// it writes that tile's outputs, and tiles are disjoint.
-__global__ void __launch_bounds__(MLP_THREADS) k_les_mlp(CPtrs gx, Ptrs tau, int64_t npts, const bf16* wb,
-                                                         const float* p, const float* norm, double delta) {
+// Closure network at the grid points.  Every warp works on its own tiles of
+// 16 points with private activation buffers (no block-wide barrier after the
+// weights are staged): the 9 gradients and the width are normalised to BF16
+// inputs, the MLP runs on the tensor cores and the 6 stresses are written.
+// tau may alias gx[0..5]: a warp reads all inputs of a tile before it writes
+// that tile's outputs, and tiles are disjoint.
+constexpr int LES_WARPS = 8;
+
+struct LesMlpSmem {
+    bf16 w1[MLP_H * LDI];
+    bf16 w2[MLP_H * LDH];
+    bf16 w3[16 * LDH];
+    float b1[MLP_H], b2[MLP_H], b3[MLP_OUT];
+    float norm[MLP_NNORM];
+    struct Warp {
+        bf16 x[16 * LDI];
+        bf16 h1[16 * LDH];
+        bf16 h2[16 * LDH];
+    } w[LES_WARPS];
+};
+
+__global__ void __launch_bounds__(32 * LES_WARPS) k_les_mlp(CPtrs gx, Ptrs tau, int64_t npts, const bf16* wb,
+                                                            const float* p, const float* norm, double delta) {
     extern __shared__ __align__(16) unsigned char les_smem[];
-    MlpFwdSmem& s = *reinterpret_cast<MlpFwdSmem*>(les_smem);
-    mlp_load_weights(s, wb, p);
-    const int r0 = 16 * (threadIdx.x >> 5);
-    for (int64_t base = (int64_t)blockIdx.x * 64; base < npts; base += (int64_t)gridDim.x * 64) {
-        __syncthreads();
-        for (int i = threadIdx.x; i < 64 * MLP_IN; i += blockDim.x) {
-            const int a = i >> 6, r = i & 63;
+    LesMlpSmem& s = *reinterpret_cast<LesMlpSmem*>(les_smem);
+    for (int i = threadIdx.x; i < MLP_H * MLP_IN; i += blockDim.x)
+        s.w1[(i / MLP_IN) * LDI + i % MLP_IN] = wb[BOFF_W1 + i];
+    for (int i = threadIdx.x; i < MLP_H * MLP_H; i += blockDim.x)
+        s.w2[(i / MLP_H) * LDH + i % MLP_H] = wb[BOFF_W2 + i];
+    for (int i = threadIdx.x; i < 16 * MLP_H; i += blockDim.x)
+        s.w3[(i / MLP_H) * LDH + i % MLP_H] = wb[BOFF_W3 + i];
+    for (int i = threadIdx.x; i < MLP_H; i += blockDim.x) {
+        s.b1[i] = p[OFF_B1 + i];
+        s.b2[i] = p[OFF_B2 + i];
+    }
+    if (threadIdx.x < MLP_OUT) s.b3[threadIdx.x] = p[OFF_B3 + threadIdx.x];
+    if (threadIdx.x < MLP_NNORM) s.norm[threadIdx.x] = norm[threadIdx.x];
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    LesMlpSmem::Warp& w = s.w[warp];
+    const MlpW W{s.w1, s.w2, s.w3, s.b1, s.b2, s.b3};
+    const int64_t ntiles = (npts + 15) / 16;
+    for (int64_t t = (int64_t)blockIdx.x * LES_WARPS + warp; t < ntiles; t += (int64_t)gridDim.x * LES_WARPS) {
+        const int64_t base = t * 16;
+        __syncwarp();
+        // 16 points x 16 input columns: lane -> point lane % 16, columns of
+        // parity lane / 16 (field indices stay compile-time constants)
+        {
+            const int r = lane & 15, half = lane >> 4;
             const int64_t pt = base + r;
-            float v = 0.f;
-            if (a < 9) v = pt < npts ? (float)((const double*)gx.p[a])[pt] : 0.f;
-            else if (a == 9) v = (float)delta;
-            if (a < MLP_NIN) v = (v - norm[NORM_IN_MEAN + a]) * norm[NORM_IN_SCALE + a];
-            s.x[r * LDI + a] = __float2bfloat16_rn(v);
+#pragma unroll
+            for (int a = 0; a < MLP_IN; a++) {
+                if ((a & 1) != half) continue;
+                float v = 0.f;
+                if (a < 9) v = pt < npts ? (float)((const double*)gx.p[a])[pt] : 0.f;
+                else if (a == 9) v = (float)delta;
+                if (a < MLP_NIN) v = (v - s.norm[NORM_IN_MEAN + a]) * s.norm[NORM_IN_SCALE + a];
+                w.x[r * LDI + a] = __float2bfloat16_rn(v);
+            }
         }
-        __syncthreads();
+        __syncwarp();
         float y[4];
-        mlp_forward_warp(s, r0, y);
+        mlp_forward16(W, w.x, w.h1, w.h2, y);
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             const int c = frag_col(q);
-            const int64_t pt = base + r0 + frag_row(q);
-            if (c < MLP_NOUT && pt < npts)
-                ((double*)tau.p[c])[pt] = (double)(y[q] * norm[NORM_OUT_SCALE + c] + norm[NORM_OUT_MEAN + c]);
+            const int64_t pt = base + frag_row(q);
+            if (pt >= npts) continue;
+            const double v = (double)(y[q] * s.norm[NORM_OUT_SCALE + (c & 7)] + s.norm[NORM_OUT_MEAN + (c & 7)]);
+#pragma unroll
+            for (int cc = 0; cc < MLP_NOUT; cc++)
+                if (cc == c) ((double*)tau.p[cc])[pt] = v;
         }
     }
 }
@@ -203,7 +245,7 @@ static int les_grads(const dd_plan* p, int prec, bool compact, const void* const
 static int les_mlp(const dd_plan* p, const dd_closure* cl, const LesWork& w, double* const* tau, cudaStream_t st) {
     static bool configured = false;
     if (!configured) {
-        DD_CUDA(cudaFuncSetAttribute(k_les_mlp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(MlpFwdSmem)));
+        DD_CUDA(cudaFuncSetAttribute(k_les_mlp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(LesMlpSmem)));
         configured = true;
     }
     const int64_t npts = p->g3.xcount();
@@ -211,11 +253,11 @@ static int les_mlp(const dd_plan* p, const dd_closure* cl, const LesWork& w, dou
     Ptrs t{};
     for (int f = 0; f < 9; f++) gx.p[f] = w.gx[f];
     for (int c = 0; c < 6; c++) t.p[c] = tau[c];
-    unsigned nb = les_grid(npts, 64);
-    if (nb > 152 * 4) nb = 152 * 4;
+    unsigned nb = les_grid(npts, 16 * LES_WARPS);
+    if (nb > 152 * 3) nb = 152 * 3;
     DD_KT("les_mlp", st,
-          k_les_mlp<<<nb, MLP_THREADS, sizeof(MlpFwdSmem), st>>>(gx, t, npts, (const bf16*)cl->wbf16, cl->params,
-                                                                  cl->norm, cl->delta));
+          k_les_mlp<<<nb, 32 * LES_WARPS, sizeof(LesMlpSmem), st>>>(gx, t, npts, (const bf16*)cl->wbf16, cl->params,
+                                                                     cl->norm, cl->delta));
     DD_LAUNCH_CHECK();
     return DD_OK;
 }

@@ -102,23 +102,33 @@ __device__ inline void mlp_load_weights(MlpFwdSmem& s, const bf16* wb, const flo
     for (int i = threadIdx.x; i < MLP_OUT; i += blockDim.x) s.b3[i] = p[OFF_B3 + i];
 }
 
-// Forward pass of the 16 samples [r0, r0 + 16) of the tile in s.x: writes the
-// BF16 activations to s.h1 / s.h2 and returns the FP32 outputs as the
-// accumulator fragment y (16 x 8).
-__device__ inline void mlp_forward_warp(MlpFwdSmem& s, int r0, float y[4]) {
+// Shared-memory weights of the network (padded rows).
+struct MlpW {
+    const bf16* w1;
+    const bf16* w2;
+    const bf16* w3;
+    const float* b1;
+    const float* b2;
+    const float* b3;
+};
+
+// Forward pass of 16 samples: x (16 rows, stride LDI) -> BF16 activations h1,
+// h2 (16 rows, stride LDH) and the FP32 outputs as the accumulator fragment y
+// (16 x 8).  One warp; x must be complete before the call.
+__device__ inline void mlp_forward16(const MlpW& W, const bf16* x, bf16* h1, bf16* h2, float y[4]) {
     {   // H1 = tanh(X W1^T + b1)
         uint32_t a[4];
-        mlp_load_a(a, s.x + r0 * LDI, LDI, 1);
+        mlp_load_a(a, x, LDI, 1);
 #pragma unroll
         for (int nt = 0; nt < MLP_H / 8; nt++) {
             float c[4] = {0.f, 0.f, 0.f, 0.f};
             uint32_t b[2];
-            mlp_load_b(b, s.w1 + (8 * nt) * LDI, 1, LDI);
+            mlp_load_b(b, W.w1 + (8 * nt) * LDI, 1, LDI);
             mma_bf16_16816(c, a, b);
 #pragma unroll
             for (int q = 0; q < 4; q++) {
                 const int col = 8 * nt + frag_col(q);
-                s.h1[(r0 + frag_row(q)) * LDH + col] = __float2bfloat16_rn(tanhf(c[q] + s.b1[col]));
+                h1[frag_row(q) * LDH + col] = __float2bfloat16_rn(tanhf(c[q] + W.b1[col]));
             }
         }
     }
@@ -126,20 +136,20 @@ __device__ inline void mlp_forward_warp(MlpFwdSmem& s, int r0, float y[4]) {
     {   // H2 = tanh(H1 W2^T + b2)
         uint32_t a[4][4];
 #pragma unroll
-        for (int kt = 0; kt < 4; kt++) mlp_load_a(a[kt], s.h1 + r0 * LDH + 16 * kt, LDH, 1);
+        for (int kt = 0; kt < 4; kt++) mlp_load_a(a[kt], h1 + 16 * kt, LDH, 1);
 #pragma unroll
         for (int nt = 0; nt < MLP_H / 8; nt++) {
             float c[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
             for (int kt = 0; kt < 4; kt++) {
                 uint32_t b[2];
-                mlp_load_b(b, s.w2 + (8 * nt) * LDH + 16 * kt, 1, LDH);
+                mlp_load_b(b, W.w2 + (8 * nt) * LDH + 16 * kt, 1, LDH);
                 mma_bf16_16816(c, a[kt], b);
             }
 #pragma unroll
             for (int q = 0; q < 4; q++) {
                 const int col = 8 * nt + frag_col(q);
-                s.h2[(r0 + frag_row(q)) * LDH + col] = __float2bfloat16_rn(tanhf(c[q] + s.b2[col]));
+                h2[frag_row(q) * LDH + col] = __float2bfloat16_rn(tanhf(c[q] + W.b2[col]));
             }
         }
     }
@@ -149,13 +159,19 @@ __device__ inline void mlp_forward_warp(MlpFwdSmem& s, int r0, float y[4]) {
 #pragma unroll
         for (int kt = 0; kt < 4; kt++) {
             uint32_t a[4], b[2];
-            mlp_load_a(a, s.h2 + r0 * LDH + 16 * kt, LDH, 1);
-            mlp_load_b(b, s.w3 + 16 * kt, 1, LDH);
+            mlp_load_a(a, h2 + 16 * kt, LDH, 1);
+            mlp_load_b(b, W.w3 + 16 * kt, 1, LDH);
             mma_bf16_16816(c, a, b);
         }
 #pragma unroll
-        for (int q = 0; q < 4; q++) y[q] = c[q] + s.b3[frag_col(q)];
+        for (int q = 0; q < 4; q++) y[q] = c[q] + W.b3[frag_col(q)];
     }
+}
+
+// Forward pass of the 16 samples [r0, r0 + 16) of the tile in s.x.
+__device__ inline void mlp_forward_warp(MlpFwdSmem& s, int r0, float y[4]) {
+    const MlpW W{s.w1, s.w2, s.w3, s.b1, s.b2, s.b3};
+    mlp_forward16(W, s.x + r0 * LDI, s.h1 + r0 * LDH, s.h2 + r0 * LDH, y);
 }
 
 }  // namespace dd
