@@ -75,6 +75,34 @@ def C2(N):
     return 16 * N * (N // 2 + 1)
 
 
+def fft_flops(shape):
+    """Canonical flops of one real transform of a grid: 2.5 n log2 n."""
+    n = float(np.prod(shape))
+    return 2.5 * n * np.log2(n)
+
+
+def measured_gemm_tflops(torch, dtype, n=4096, reps=5):
+    """FP64 / FP32 (no TF32) cuBLAS GEMM rate on this GPU, best of reps."""
+    old = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        a = torch.randn(n, n, dtype=dtype, device="cuda")
+        b = torch.randn(n, n, dtype=dtype, device="cuda")
+        torch.matmul(a, b)
+        torch.cuda.synchronize()
+        best = 0.0
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.matmul(a, b)
+            e1.record()
+            torch.cuda.synchronize()
+            best = max(best, 2.0 * n ** 3 / (e0.elapsed_time(e1) / 1e3) / 1e12)
+        return best
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = old
+
+
 # ---------------------------------------------------------------- runners
 class Hydro3Runner:
     """3D hydro (kind hydro3d) or MHD (kind mhd3d) with the fused RK4 step."""
@@ -118,6 +146,9 @@ class Hydro3Runner:
 
     def point_stages(self):
         return float(np.prod(self.wl["shape"])) * 4
+
+    def flops_per_step(self):
+        return 4 * (18 if self.mhd else 9) * fft_flops(self.wl["shape"])
 
     def kernel_bytes(self, label):
         Nz, Ny, Nx = self.wl["shape"]
@@ -171,13 +202,31 @@ class Hydro2Runner:
         for i in range(2):
             self.data["u"][i]["kspace"] = self.host[i]
         self.ti = M.RK2mid(self.rhs)
-        self.launches_per_step = None
-        self.launch_bound = True
+        # launch-bound at 128^2: one CUDA graph per step (the eager public-API
+        # step is the e2e path)
+        for _ in range(2):
+            self.eager_step()
+        torch.cuda.synchronize()
+        self.graph = torch.cuda.CUDAGraph()
+        cap = torch.cuda.Stream()
+        cap.wait_stream(torch.cuda.current_stream())
+        n0 = dd._lib.launch_count()
+        with torch.cuda.stream(cap):
+            with torch.cuda.graph(self.graph, stream=cap):
+                self.eager_step()
+        torch.cuda.current_stream().wait_stream(cap)
+        torch.cuda.synchronize()
+        self.launches_per_step = dd._lib.launch_count() - n0
+        for i in range(2):
+            self.data["u"][i]["kspace"] = self.host[i]
 
     def step(self):
+        self.graph.replay()
+
+    def eager_step(self):
         self.ti.do_advance(self.data, self.wl["dt"])
 
-    eager_step = step
+    api_step = eager_step
 
     def state(self):
         return [self.data["u"][i].kdata for i in range(2)]
@@ -189,6 +238,9 @@ class Hydro2Runner:
     def point_stages(self):
         return float(np.prod(self.wl["shape"])) * 2
 
+    def flops_per_step(self):
+        return 2 * 5 * fft_flops(self.wl["shape"])
+
     def kernel_bytes(self, label):
         return None
 
@@ -197,7 +249,8 @@ class Hydro2Runner:
         return {"workload": "2D incompressible hydro %dx%d, RK2mid, dt=%g, nu=%g, 2/3 dealiasing" % (*w["shape"], w["dt"],
                                                                                                   w["nu"]),
                 "grid": list(w["shape"]), "integrator": "RK2mid", "dt": w["dt"], "precision": w["precision"],
-                "parallelism": "replicas x%d" % ws, "l2": "state fits in L2 (launch-bound workload)"}
+                "parallelism": "replicas x%d" % ws, "l2": "state fits in L2 (launch-bound workload)",
+                "stepping": "one CUDA graph per RK2mid step (e2e: eager public API)"}
 
     def metric(self):
         return "128² 2D hydro steps/s", "steps/s"
@@ -234,6 +287,9 @@ class EnsembleRunner:
 
     def point_stages(self):
         return float(self.ens.grid_point_stages())
+
+    def flops_per_step(self):
+        return sum(2 * 8 * fft_flops((n, n)) for n in self.sizes)
 
     def kernel_bytes(self, label):
         return None
@@ -300,6 +356,9 @@ class LesRunner:
 
     def point_stages(self):
         return float(np.prod(self.wl["shape"])) * 4
+
+    def flops_per_step(self):
+        return 4 * 21 * fft_flops(self.wl["shape"])
 
     def kernel_bytes(self, label):
         n = int(np.prod(self.wl["shape"]))
@@ -627,6 +686,17 @@ def main():
     step_hbm = {"algorithmic_bytes_per_step": B, "t_roofline_ms": B / (hbm_peak * 1e9) * 1e3,
                 "hbm_frac": (B / (hbm_peak * 1e9)) / (ms_per_step / 1e3),
                 "grid_point_stages_per_s": run.point_stages() * value}
+    # combined roofline max(B / BW, F / P) with P the measured cuBLAS GEMM rate
+    # of the transform arithmetic (FP64 DGEMM, FP32 SGEMM without TF32)
+    if wl["precision"] in ("fp64", "fp32") and hasattr(run, "flops_per_step"):
+        F = run.flops_per_step()
+        P = measured_gemm_tflops(torch, torch.float64 if wl["precision"] == "fp64" else torch.float32)
+        t_b, t_f = B / (hbm_peak * 1e9), F / (P * 1e12)
+        step_hbm.update({"flops_per_step": F, "arith_peak_tflops": P,
+                         "arith_peak_source": "measured cuBLAS %s GEMM 4096^3 in this run" % (
+                             "DGEMM" if wl["precision"] == "fp64" else "SGEMM (no TF32)"),
+                         "t_flops_ms": t_f * 1e3, "combined_bound": "hbm" if t_b >= t_f else "flops",
+                         "combined_frac": max(t_b, t_f) / (ms_per_step / 1e3)})
 
     # end to end through the public API: the state in from pinned host memory,
     # one step, the state back out, every step

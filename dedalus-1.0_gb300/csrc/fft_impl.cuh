@@ -94,9 +94,11 @@ int fft_c2r(const dd_plan* pl, int nf, const void* const* k, double* const* x, v
     return DD_OK;
 }
 
+// zero_nonkept = false leaves the entries outside the kept set unwritten (for
+// internal callers that read kept modes only).
 template <typename T>
 int fft_r2c(const dd_plan* pl, int nf, const double* const* x, void* const* k, void* work, size_t wb,
-            cudaStream_t st) {
+            cudaStream_t st, bool zero_nonkept = true) {
     DD_CHECK_ARG(wb >= ws_bytes<T>(pl, nf), "workspace too small: %zu < %zu bytes", wb, ws_bytes<T>(pl, nf));
     CPtrs xin{}; Ptrs ko{};
     for (int f = 0; f < nf; f++) { xin.p[f] = x[f]; ko.p[f] = k[f]; }
@@ -117,8 +119,10 @@ int fft_r2c(const dd_plan* pl, int nf, const double* const* x, void* const* k, v
         DD_TRY((launch_pass_len<T, false, false, false>(g.Ny, b, g.Kx, g.Nz, nf, st)));
         OpZFwd3<T, double> c{g, w1c, ko, TwSel<T>::z(pl)};
         DD_TRY((launch_pass_len<T, false, false, false>(g.Nz, c, g.Kx, g.Ky, nf, st)));
-        DD_KT("zero_nonkept3", st, k_zero_nonkept3<double><<<dim3(ew_grid(g.kcount()), nf), 256, 0, st>>>(g, ko));
-        DD_LAUNCH_CHECK();
+        if (zero_nonkept) {
+            DD_KT("zero_nonkept3", st, k_zero_nonkept3<double><<<dim3(ew_grid(g.kcount()), nf), 256, 0, st>>>(g, ko));
+            DD_LAUNCH_CHECK();
+        }
     } else {
         const Geo2& g = pl->g2;
         C<T>* W = (C<T>*)work;
@@ -129,7 +133,7 @@ int fft_r2c(const dd_plan* pl, int nf, const double* const* x, void* const* k, v
         OpYFwd2<T, double> b{g, wc, ko, TwSel<T>::y(pl)};
         DD_TRY((launch_pass_len<T, false, false, true>(g.Ny, b, g.Kx, 1, nf, st)));
         const int64_t nz = g.kcount() - (int64_t)g.Kx * g.Ny;
-        if (nz > 0) {
+        if (nz > 0 && zero_nonkept) {
             DD_KT("zero_nonkept2", st, k_zero_nonkept2<double><<<dim3(ew_grid(nz), nf), 256, 0, st>>>(g, ko));
             DD_LAUNCH_CHECK();
         }
@@ -139,6 +143,7 @@ int fft_r2c(const dd_plan* pl, int nf, const double* const* x, void* const* k, v
 
 #define DD_FFT_INSTANTIATE(EXT, T)                                                                       \
     EXT template int fft_c2r<T>(const dd_plan*, int, const void* const*, double* const*, void*, size_t, cudaStream_t); \
-    EXT template int fft_r2c<T>(const dd_plan*, int, const double* const*, void* const*, void*, size_t, cudaStream_t);
+    EXT template int fft_r2c<T>(const dd_plan*, int, const double* const*, void* const*, void*, size_t, cudaStream_t, \
+                                bool);
 
 }  // namespace dd

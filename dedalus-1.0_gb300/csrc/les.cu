@@ -93,24 +93,40 @@ __global__ void __launch_bounds__(32 * LES_WARPS) k_les_mlp(CPtrs gx, Ptrs tau, 
     LesMlpSmem::Warp& w = s.w[warp];
     const MlpW W{s.w1, s.w2, s.w3, s.b1, s.b2, s.b3};
     const int64_t ntiles = (npts + 15) / 16;
-    for (int64_t t = (int64_t)blockIdx.x * LES_WARPS + warp; t < ntiles; t += (int64_t)gridDim.x * LES_WARPS) {
+    const int64_t stride = (int64_t)gridDim.x * LES_WARPS;
+    // lane -> point lane % 16 of a tile and the gradient columns of parity
+    // lane / 16 (field indices stay compile-time constants); the next tile's
+    // gradients are loaded into registers while the current tile computes
+    const int r = lane & 15, half = lane >> 4;
+    double g[5];
+    const double* src[5];
+#pragma unroll
+    for (int j = 0; j < 5; j++) {
+        const double* p0 = (const double*)gx.p[2 * j];
+        const double* p1 = 2 * j + 1 < 9 ? (const double*)gx.p[2 * j + 1] : p0;
+        src[j] = half ? p1 : p0;
+    }
+    auto fetch = [&](int64_t tile) {
+        const int64_t pt = tile * 16 + r;
+        const bool ok = tile < ntiles && pt < npts;
+#pragma unroll
+        for (int j = 0; j < 5; j++) g[j] = (ok && 2 * j + half < 9) ? src[j][pt] : 0.;
+    };
+    int64_t t = (int64_t)blockIdx.x * LES_WARPS + warp;
+    fetch(t);
+    for (; t < ntiles; t += stride) {
         const int64_t base = t * 16;
         __syncwarp();
-        // 16 points x 16 input columns: lane -> point lane % 16, columns of
-        // parity lane / 16 (field indices stay compile-time constants)
-        {
-            const int r = lane & 15, half = lane >> 4;
-            const int64_t pt = base + r;
 #pragma unroll
-            for (int a = 0; a < MLP_IN; a++) {
-                if ((a & 1) != half) continue;
-                float v = 0.f;
-                if (a < 9) v = pt < npts ? (float)((const double*)gx.p[a])[pt] : 0.f;
-                else if (a == 9) v = (float)delta;
-                if (a < MLP_NIN) v = (v - s.norm[NORM_IN_MEAN + a]) * s.norm[NORM_IN_SCALE + a];
-                w.x[r * LDI + a] = __float2bfloat16_rn(v);
-            }
+        for (int j = 0; j < 8; j++) {
+            const int a = 2 * j + half;
+            float v = 0.f;
+            if (a < 9) v = (float)g[j < 5 ? j : 4];
+            else if (a == 9) v = (float)delta;
+            if (a < MLP_NIN) v = (v - s.norm[NORM_IN_MEAN + a]) * s.norm[NORM_IN_SCALE + a];
+            w.x[r * LDI + a] = __float2bfloat16_rn(v);
         }
+        fetch(t + stride);
         __syncwarp();
         float y[4];
         mlp_forward16(W, w.x, w.h1, w.h2, y);
@@ -271,8 +287,9 @@ int les_closure_add(const dd_plan* p, const LesHook& h, int prec, bool compact, 
     const double* xin[6];
     void* kout[6];
     for (int c = 0; c < 6; c++) { xin[c] = w.gx[c]; kout[c] = w.gk[c]; }
-    if (prec == DD_FP32) DD_TRY(fft_r2c<float>(p, 6, xin, kout, w.fw, w.fwb, st));
-    else DD_TRY(fft_r2c<double>(p, 6, xin, kout, w.fw, w.fwb, st));
+    // k_les_add reads the kept modes only: no zeroing of the rest
+    if (prec == DD_FP32) DD_TRY(fft_r2c<float>(p, 6, xin, kout, w.fw, w.fwb, st, false));
+    else DD_TRY(fft_r2c<double>(p, 6, xin, kout, w.fw, w.fwb, st, false));
     const Geo3& g = p->g3;
     CPtrs tk{};
     Ptrs n{};
