@@ -31,6 +31,7 @@ the Cython stage kernels) on the host cores for the same workload.
 import argparse
 import json
 import os
+import re
 import subprocess
 import sys
 import threading
@@ -73,6 +74,32 @@ def B2(N):
 
 def C2(N):
     return 16 * N * (N // 2 + 1)
+
+
+def bytes_2d(label, runs, cs, ni, no, nf):
+    """Algorithmic bytes of one launch of a 2D pass for size classes runs
+    {N: number of runs in the launch}: compact intermediates W [y][kxc]
+    (cs bytes per complex), kept-mode arrays Kx x Ky complex128."""
+    m = re.search(r"_(\d+)_f(32|64)$", label)
+    sizes = [int(m.group(1))] if m else list(runs)
+    tot = 0.0
+    for N in sizes:
+        nr = runs.get(N, 0)
+        M = (N - 1) // 3
+        Kx, Ky = M + 1, 2 * M + 1
+        w, kc = N * Kx * cs, Kx * Ky * 16
+        if label.startswith("x_prod"):
+            b = (ni + no) * w
+        elif label.startswith("y_inv"):
+            b = nf * kc + ni * w
+        elif label.startswith("y_fwd_compact"):
+            b = no * (w + kc)
+        elif label.startswith("rk2mid_stage2d"):
+            b = nf * 5 * kc
+        else:
+            return None
+        tot += nr * b
+    return tot if m else tot / max(len(sizes), 1)
 
 
 def fft_flops(shape):
@@ -149,6 +176,29 @@ class Hydro3Runner:
 
     def flops_per_step(self):
         return 4 * (18 if self.mhd else 9) * fft_flops(self.wl["shape"])
+
+    def kernel_flops(self, label):
+        """Canonical transform flops of one launch (5 L log2 L per complex
+        pencil, 2.5 N log2 N per real row) plus the products."""
+        Nz, Ny, Nx = self.wl["shape"]
+        Mx, My, Mz = (Nx - 1) // 3, (Ny - 1) // 3, (Nz - 1) // 3
+        Kx, Ky = Mx + 1, 2 * My + 1
+        g = 2 if self.mhd else 1
+        ni, no = 6 * g, 3 * g
+        cf = lambda L: 5.0 * L * np.log2(L)
+        if label.startswith("z_inv_curl"):
+            return ni * Kx * Ky * cf(Nz)
+        if label.startswith("y_inv"):
+            return ni * Kx * Nz * cf(Ny)
+        if label.startswith("x_cross"):
+            return Nz * Ny * ((ni + no) * 0.5 * cf(Nx) + Nx * (9 if not self.mhd else 30))
+        if label.startswith("y_fwd"):
+            return no * Kx * Nz * cf(Ny)
+        if label.startswith("z_fwd_compact"):
+            return no * Kx * Ky * cf(Nz)
+        return None
+
+    kernel_flops_pipe = property(lambda self: {"fp64": "fp64", "fp32": "fp32"}.get(self.wl["precision"]))
 
     def kernel_bytes(self, label):
         Nz, Ny, Nx = self.wl["shape"]
@@ -242,7 +292,8 @@ class Hydro2Runner:
         return 2 * 5 * fft_flops(self.wl["shape"])
 
     def kernel_bytes(self, label):
-        return None
+        cs = 16 if self.wl["precision"] == "fp64" else 8
+        return bytes_2d(label, {self.wl["shape"][0]: 1}, cs, 3, 2, 2)
 
     def config(self, ws):
         w = self.wl
@@ -292,7 +343,8 @@ class EnsembleRunner:
         return sum(2 * 8 * fft_flops((n, n)) for n in self.sizes)
 
     def kernel_bytes(self, label):
-        return None
+        cs = 16 if self.wl["precision"] == "fp64" else 8
+        return bytes_2d(label, {n: self.sizes.count(n) for n in self.wl["sizes"]}, cs, 5, 3, 3)
 
     def config(self, ws):
         w = self.wl
@@ -527,7 +579,10 @@ class ClockSampler:
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
-    def stop(self):
+    def mark(self):
+        return len(self.lines)
+
+    def stop(self, since=0):
         if self.proc is None:
             return None
         self.proc.terminate()
@@ -538,7 +593,7 @@ class ClockSampler:
         self.thread.join(timeout=5)
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.lines:
+        for line in self.lines[since:]:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) < len(self.FIELDS):
                 continue
@@ -614,6 +669,10 @@ def main():
 
     sampler = ClockSampler(gpu_uuid(torch, local))
     sampler.start()
+    t_wait = time.time()
+    while sampler.proc is not None and sampler.mark() == 0 and time.time() - t_wait < 3.0:
+        time.sleep(0.02)                  # nvidia-smi's first (pre-region) line
+    clock_mark = sampler.mark()
     # per-launch CUDA events inside the timed region only where their host cost
     # is negligible (not for CUDA-graph or launch-bound workloads, whose kernel
     # table comes from a separate eager pass after the timed region)
@@ -634,7 +693,18 @@ def main():
     if run.launches_per_step is not None:
         launches = run.launches_per_step * args.steps      # graph replays launch the captured kernels
     ms = max_over_ranks(e0.elapsed_time(e1))
-    clocks = sampler.stop()
+    # a timed region shorter than the 200 ms sampling period may hold no
+    # sample: keep stepping (untimed) until two samples follow its start
+    extra = 0
+    t_wait = time.time()
+    while sampler.proc is not None and sampler.mark() - clock_mark < 2 and time.time() - t_wait < 5.0:
+        run.step()
+        torch.cuda.synchronize()
+        extra += 1
+    clocks = sampler.stop(since=clock_mark)
+    if clocks is not None:
+        clocks["window"] = ("timed region" if extra == 0 else
+                            "timed region + %d untimed steps of the same workload right after it" % extra)
     kt = dd._lib.timing_report() if events_in_timed else {}
     kernel_timing = "CUDA events per launch inside the timed region"
     if not events_in_timed and hasattr(run, "eager_step"):
@@ -659,6 +729,12 @@ def main():
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
     bf16_peak = float(peaks.get("bf16_tflops", 1900.0))
+    _arith = {}
+
+    def arith_peak(pipe):
+        if pipe not in _arith:
+            _arith[pipe] = measured_gemm_tflops(torch, torch.float64 if pipe == "fp64" else torch.float32)
+        return _arith[pipe]
     kernels, roofline = {}, None
     total_kt = sum(v[1] for v in kt.values()) or 1.0
     for name, (cnt, tot) in sorted(kt.items(), key=lambda kv: -kv[1][1]):
@@ -675,9 +751,16 @@ def main():
                     "frac": (ach / hbm_peak) if ach else None, "traffic": None, "peak_source": peak_src,
                     "algorithmic_bytes_per_launch": b, "avg_launch_ms": avg * 1e3, "kernel_timing": kernel_timing}
         fl = getattr(run, "kernel_flops", lambda _n: None)(name)
-        if fl:
+        pipe = getattr(run, "kernel_flops_pipe", "bf16")
+        if fl and pipe == "bf16":
             roofline["tensor"] = {"achieved": fl / avg / 1e12, "peak": bf16_peak, "unit": "TFLOP/s",
                                   "frac": fl / avg / 1e12 / bf16_peak, "algorithmic_flops_per_launch": fl}
+        elif fl and pipe in ("fp64", "fp32"):
+            P = arith_peak(pipe)
+            roofline["compute"] = {"pipe": pipe, "achieved": fl / avg / 1e12, "peak": P, "unit": "TFLOP/s",
+                                   "frac": fl / avg / 1e12 / P, "algorithmic_flops_per_launch": fl,
+                                   "peak_source": "measured cuBLAS %s 4096^3 in this run" % (
+                                       "DGEMM" if pipe == "fp64" else "SGEMM (no TF32)")}
     else:
         ach = B / (ms_per_step / 1e3) / 1e9
         roofline = {"bound": "hbm", "kernel": "whole step (CUDA graph)", "achieved": ach, "peak": hbm_peak,
@@ -690,7 +773,7 @@ def main():
     # of the transform arithmetic (FP64 DGEMM, FP32 SGEMM without TF32)
     if wl["precision"] in ("fp64", "fp32") and hasattr(run, "flops_per_step"):
         F = run.flops_per_step()
-        P = measured_gemm_tflops(torch, torch.float64 if wl["precision"] == "fp64" else torch.float32)
+        P = arith_peak(wl["precision"])
         t_b, t_f = B / (hbm_peak * 1e9), F / (P * 1e12)
         step_hbm.update({"flops_per_step": F, "arith_peak_tflops": P,
                          "arith_peak_source": "measured cuBLAS %s GEMM 4096^3 in this run" % (
