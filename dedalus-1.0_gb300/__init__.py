@@ -23,9 +23,10 @@ try:  # the device layers need torch; host helpers (kgrid, init_cond) do not
     from . import diagnostics
     from . import ensemble
     from . import closure
+    from . import restart
 except ImportError as e:  # pragma: no cover
     if "torch" not in str(e):
         raise
 
 __all__ = ["_lib", "kgrid", "config", "init_cond", "engine", "representations", "fields", "physics",
-           "time_step", "mods", "diagnostics", "ensemble", "closure"]
+           "time_step", "mods", "diagnostics", "ensemble", "closure", "restart"]

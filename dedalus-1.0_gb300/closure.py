@@ -264,7 +264,7 @@ def generate_dataset(n_seeds=50, n_snap=20, stride=50, dns_n=256, les_n=64, nu=5
         data.set_time(0.)
         for j in range(n_snap):
             for _ in range(stride):
-                ti.advance(data, dt)
+                ti.do_advance(data, dt)
                 steps += 1
             k = (s * n_snap + j) * npts
             sampler.samples([data['u'][i].kdata for i in range(3)], raw[k:k + npts])
@@ -458,11 +458,11 @@ def evaluate(models, seed=7, dns_n=256, les_n=64, nu=5e-3, dt=2e-3, nsteps=1000,
     for step in range(1, nsteps + 1):
         torch.cuda.synchronize()
         a = time.time()
-        ti.advance(dd, dt)
+        ti.do_advance(dd, dt)
         torch.cuda.synchronize()
         b = time.time()
         for name, (RHS, data, ti_l, _c) in runs.items():
-            ti_l.advance(data, dt)
+            ti_l.do_advance(data, dt)
         torch.cuda.synchronize()
         c = time.time()
         t_dns += b - a

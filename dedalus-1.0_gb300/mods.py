@@ -15,7 +15,8 @@ from .time_step import RK2mid, RK2trap, RK4
 from .fields import StateData, create_field_classes
 from .kgrid import swap_indices
 from . import init_cond
+from .restart import restart
 
 __all__ = ["decfg", "FourierRepresentation", "GpuFourierRepresentation", "Physics", "IncompressibleHydro",
            "BoussinesqHydro", "IncompressibleMHD", "LESHydro", "RK2mid", "RK2trap", "RK4", "StateData",
-           "create_field_classes", "swap_indices", "init_cond"]
+           "create_field_classes", "swap_indices", "init_cond", "restart"]

@@ -23,7 +23,7 @@ import time
 import numpy as np
 import torch
 
-from . import _lib
+from . import _lib, restart
 from .engine import current_stream, dptr
 
 
@@ -71,7 +71,11 @@ class TimeStepBase:
         return True
 
     def advance(self, data, dt=None):
+        """time_step.py:101-107: snapshot when the iteration is a multiple of
+        save_cadence or max_save_period has passed, then one step."""
         t0 = time.time()
+        if (self.iteration % self.save_cadence) == 0 or (self.time - self._tlastsnap >= self.max_save_period):
+            self.snapshot(data)
         if dt is None:
             dt = self.cfl_dt(data)
         self.do_advance(data, dt)
@@ -81,8 +85,9 @@ class TimeStepBase:
         raise NotImplementedError("do_advance must be provided by subclass.")
 
     def snapshot(self, data):
-        """Host dump of the state (npz) in place of the reference's HDF5."""
-        data.save_npz("snap_%05i.npz" % self._nsnap)
+        """time_step.py:112-151: directory snap_%05i with the fields, the
+        run description and the forcing sidecar (layout in restart.py)."""
+        restart.save(restart.SNAP_DIR % self._nsnap, self.RHS, data, self)
         self._nsnap += 1
         self._tlastsnap = self.time
 

@@ -239,8 +239,8 @@ def test_fused_les_step_matches_generic_rk4(dd, cuda):
     ta, tb = M.RK4(Ra), M.RK4(Rb)
     tb.use_fused = False
     for _ in range(3):
-        ta.advance(da, 2e-3)
-        tb.advance(db, 2e-3)
+        ta.do_advance(da, 2e-3)
+        tb.do_advance(db, 2e-3)
     for i in range(3):
         a, b = da['u'][i].to_numpy('kspace'), db['u'][i].to_numpy('kspace')
         assert _rel(a, b) < 1e-6
@@ -248,7 +248,7 @@ def test_fused_les_step_matches_generic_rk4(dd, cuda):
     Rn, dn = _les_pair(dd, shape, None, u)
     tn = M.RK4(Rn)
     for _ in range(3):
-        tn.advance(dn, 2e-3)
+        tn.do_advance(dn, 2e-3)
     assert _rel(dn['u'][0].to_numpy('kspace'), da['u'][0].to_numpy('kspace')) > 1e-8
 
 
@@ -267,7 +267,7 @@ def test_les_rk4_step_matches_oracle(dd, cuda, fused):
     R, d = _les_pair(dd, shape, c, u)
     ti = dd.mods.RK4(R)
     ti.use_fused = fused
-    ti.advance(d, 2e-3)
+    ti.do_advance(d, 2e-3)
     ro = OC.les_physics(shape, c.params.cpu().numpy(), c.norm.cpu().numpy(), delta)
     ro.parameters['nu'] = 5e-3
     do = ro.create_fields(0.)
