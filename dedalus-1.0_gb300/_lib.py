@@ -84,9 +84,9 @@ SIGNATURES = {
 
 class Closure(ctypes.Structure):
     """dd_closure: device pointers of the BF16 weights, FP32 parameters and
-    normalisation vector, and the filter width."""
+    normalisation vector, the filter width and the closure-term band."""
     _fields_ = [("wbf16", ctypes.c_void_p), ("params", ctypes.c_void_p), ("norm", ctypes.c_void_p),
-                ("delta", ctypes.c_double)]
+                ("delta", ctypes.c_double), ("band_lo", ctypes.c_double), ("band_hi", ctypes.c_double)]
 _RESTYPE = {"dd_last_error": ctypes.c_char_p, "dd_launch_count": ctypes.c_longlong}
 
 

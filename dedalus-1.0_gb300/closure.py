@@ -88,6 +88,10 @@ class MLPClosure:
         self.loss_buf = torch.zeros(1, dtype=torch.float32, device=self.device)
         self.step = 0
         self.meta = {}
+        # spectral band of the closure term: weight 0 below band[0], 1 above
+        # band[1], linear between; (0, 0) applies it at every mode
+        self.band = (0.0, 0.0)
+        self.gain = 1.0                 # applied to the stress fluctuation (out_scale)
         self._ws = None
         self.pack()
 
@@ -97,7 +101,21 @@ class MLPClosure:
 
     def struct(self):
         """dd_closure for the C ABI (keep the returned object alive)."""
-        return _lib.Closure(self.wbf16.data_ptr(), self.params.data_ptr(), self.norm.data_ptr(), self.delta)
+        return _lib.Closure(self.wbf16.data_ptr(), self.params.data_ptr(), self.norm.data_ptr(), self.delta,
+                            float(self.band[0]), float(self.band[1]))
+
+    def with_band(self, lo, hi, gain=1.0):
+        """A view of this network (shared weights) with another closure-term
+        band and the predicted stress fluctuation scaled by gain (the
+        constant mean stress has no divergence)."""
+        c = object.__new__(MLPClosure)
+        c.__dict__.update(self.__dict__)
+        c.band = (float(lo), float(hi))
+        if gain != 1.0:
+            c.norm = self.norm.clone()
+            c.norm[40:46] *= float(gain)
+        c.gain = float(gain) * self.gain
+        return c
 
     def set_norm(self, in_mean, in_scale, out_mean, out_scale):
         n = np.zeros(self.nnorm, dtype=np.float32)
@@ -155,8 +173,11 @@ class MLPClosure:
     # ------------------------------------------------------------ storage
     def save(self, path, **meta):
         meta = dict(self.meta, **meta)
-        np.savez(path, params=self.params.cpu().numpy(), norm=self.norm.cpu().numpy(),
-                 delta=np.float64(self.delta), meta=np.array(json.dumps(meta)))
+        norm = self.norm.cpu().numpy().copy()
+        norm[40:46] /= np.float32(self.gain)          # stored without the gain
+        np.savez(path, params=self.params.cpu().numpy(), norm=norm, delta=np.float64(self.delta),
+                 band=np.array(self.band, dtype=np.float64), gain=np.float64(self.gain),
+                 meta=np.array(json.dumps(meta)))
 
     @classmethod
     def load(cls, path=DEFAULT_WEIGHTS, device=None):
@@ -165,6 +186,11 @@ class MLPClosure:
         c.params.copy_(torch.from_numpy(z["params"].astype(np.float32)))
         c.norm.copy_(torch.from_numpy(z["norm"].astype(np.float32)))
         c.meta = json.loads(str(z["meta"]))
+        if "band" in z.files:
+            c.band = tuple(float(x) for x in z["band"])
+        if "gain" in z.files and float(z["gain"]) != 1.0:
+            c.gain = float(z["gain"])
+            c.norm[40:46] *= c.gain
         c.pack()
         return c
 

@@ -143,15 +143,23 @@ __global__ void __launch_bounds__(32 * LES_WARPS) k_les_mlp(CPtrs gx, Ptrs tau, 
     }
 }
 
-// nc_i -= i k_j tau_ij on the kept modes; tau spectra in full layout, order
-// xx, yy, zz, xy, xz, yz; nc compact complex128.
-__global__ void k_les_add(Geo3 g, const double* kx, const double* ky, const double* kz, CPtrs tk, Ptrs nc) {
+// nc_i -= w(|k|) i k_j tau_ij on the kept modes; tau spectra in full layout,
+// order xx, yy, zz, xy, xz, yz; nc compact complex128.  w ramps linearly from
+// 0 at |k| = lo to 1 at |k| = hi (w = 1 everywhere when hi <= 0).
+__global__ void k_les_add(Geo3 g, const double* kx, const double* ky, const double* kz, CPtrs tk, Ptrs nc,
+                          double lo, double hi) {
     const int64_t n = (int64_t)g.Ky * g.Kz * g.Kx;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         int ky_i, kz_i, ix;
         int64_t o;
         les_kept(g, i, ky_i, kz_i, ix, o);
         const double k0 = kx[ix], k1 = ky[ky_i], k2 = kz[kz_i];
+        double w = 1.;
+        if (hi > 0.) {
+            const double kk = sqrt(k0 * k0 + k1 * k1 + k2 * k2);
+            w = kk <= lo ? 0. : (kk >= hi ? 1. : (kk - lo) / (hi - lo));
+        }
+        if (w == 0.) continue;
         double2 t[6];
 #pragma unroll
         for (int c = 0; c < 6; c++) t[c] = ((const double2*)tk.p[c])[o];
@@ -162,7 +170,7 @@ __global__ void k_les_add(Geo3 g, const double* kx, const double* ky, const doub
             const double2 d0 = les_ik(t[row[a][0]], k0), d1 = les_ik(t[row[a][1]], k1), d2 = les_ik(t[row[a][2]], k2);
             double2* N = (double2*)nc.p[a];
             const double2 v = N[i];
-            N[i] = make_double2(v.x - ((d0.x + d1.x) + d2.x), v.y - ((d0.y + d1.y) + d2.y));
+            N[i] = make_double2(v.x - w * ((d0.x + d1.x) + d2.x), v.y - w * ((d0.y + d1.y) + d2.y));
         }
     }
 }
@@ -296,7 +304,8 @@ int les_closure_add(const dd_plan* p, const LesHook& h, int prec, bool compact, 
     for (int c = 0; c < 6; c++) tk.p[c] = w.gk[c];
     for (int a = 0; a < 3; a++) n.p[a] = nc[a];
     DD_KT("les_add", st,
-          k_les_add<<<les_grid((int64_t)g.Ky * g.Kz * g.Kx), 256, 0, st>>>(g, p->kx, p->ky, p->kz, tk, n));
+          k_les_add<<<les_grid((int64_t)g.Ky * g.Kz * g.Kx), 256, 0, st>>>(g, p->kx, p->ky, p->kz, tk, n,
+                                                                          h.cl->band_lo, h.cl->band_hi));
     DD_LAUNCH_CHECK();
     return DD_OK;
 }

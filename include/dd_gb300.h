@@ -249,6 +249,8 @@ typedef struct dd_closure {
     const float* params;
     const float* norm;
     double delta;          /* filter width fed to input 9 */
+    double band_lo;        /* closure-term weight w(|k|): 0 for |k| <= band_lo, */
+    double band_hi;        /* 1 for |k| >= band_hi, linear between; band_hi <= 0: w = 1 */
 } dd_closure;
 
 int dd_mlp_sizes(int* nparam, int* nbf16, int* nnorm, int* in_dim, int* out_dim);

@@ -201,8 +201,9 @@ def stress(u, shape, p, norm, delta, rounding=True):
     return [tau[:, c].astype(np.float64).reshape(shape) for c in range(NOUT)]
 
 
-def closure_term(u, shape, p, norm, delta, rounding=True):
-    """-P[d_j tau_ij]^ (3 k arrays, kept modes) for velocity u."""
+def closure_term(u, shape, p, norm, delta, rounding=True, band=(0.0, 0.0)):
+    """-w(|k|) P[d_j tau_ij]^ (3 k arrays, kept modes) for velocity u; w ramps
+    linearly from 0 at |k| = band[0] to 1 at band[1] (w = 1 if band[1] <= 0)."""
     tau = [to_k(t) for t in stress(u, shape, p, norm, delta, rounding)]
     kx, ky, kz = kvectors(shape)
     kv = (kx, ky, kz)
@@ -212,10 +213,14 @@ def closure_term(u, shape, p, norm, delta, rounding=True):
     k2 = np.where(k2 == 0, 1.0, k2)
     div = sum(kv[a] * s[a] for a in range(3)) / k2
     keep = kept_mask(shape)
-    return [-(s[a] - kv[a] * div) * keep for a in range(3)]
+    w = 1.0
+    if band[1] > 0:
+        kk = np.sqrt(kx ** 2 + ky ** 2 + kz ** 2)
+        w = np.clip((kk - band[0]) / (band[1] - band[0]), 0.0, 1.0)
+    return [-(s[a] - kv[a] * div) * keep * w for a in range(3)]
 
 
-def les_physics(shape, p, norm, delta):
+def les_physics(shape, p, norm, delta, band=(0.0, 0.0)):
     """Oracle RHS object of the closed LES: the oracle IncompressibleHydro RHS
     with its pressure projection, plus closure_term()."""
     from .physics import IncompressibleHydro
@@ -226,7 +231,7 @@ def les_physics(shape, p, norm, delta):
             IncompressibleHydro.RHS(self, data, deriv)
             self.pressure_projection(data, deriv)     # skipped by the base for subclasses
             u = [data['u'][i]['kspace'] for i in range(3)]
-            term = closure_term(u, shape, p, norm, delta)
+            term = closure_term(u, shape, p, norm, delta, band=band)
             for i in range(3):
                 deriv['u'][i]['kspace'] += term[i]
 
