@@ -693,6 +693,8 @@ def main():
     if run.launches_per_step is not None:
         launches = run.launches_per_step * args.steps      # graph replays launch the captured kernels
     ms = max_over_ranks(e0.elapsed_time(e1))
+    kt = dd._lib.timing_report() if events_in_timed else {}
+    dd._lib.timing_enable(False)
     # a timed region shorter than the 200 ms sampling period may hold no
     # sample: keep stepping (untimed) until two samples follow its start
     extra = 0
@@ -705,7 +707,6 @@ def main():
     if clocks is not None:
         clocks["window"] = ("timed region" if extra == 0 else
                             "timed region + %d untimed steps of the same workload right after it" % extra)
-    kt = dd._lib.timing_report() if events_in_timed else {}
     kernel_timing = "CUDA events per launch inside the timed region"
     if not events_in_timed and hasattr(run, "eager_step"):
         kp = max(3, min(args.steps, 20))
