@@ -63,7 +63,7 @@ SIGNATURES = {
     "dd_rk4_step3d": [P, I, P, PP, P, PP, PP, P, I, D, I, ctypes.POINTER(I), P, SZ, P],
     "dd_rhs2d_workspace_size": [P, I, I, ctypes.POINTER(SZ)],
     "dd_rhs2d": [P, I, P, I, PP, I64, PP, I64, P, I, I, P, SZ, P],
-    "dd_rk2mid_step2d": [P, I, P, I, PP, I64, P, PP, PP, P, I, D, I, P, SZ, P],
+    "dd_rk2mid_step2d": [P, I, P, I, PP, I64, P, PP, PP, P, I, D, I, ctypes.POINTER(I), P, SZ, P],
     "dd_mlp_sizes": [ctypes.POINTER(I)] * 5,
     "dd_mlp_workspace_size": [I64, ctypes.POINTER(SZ)],
     "dd_mlp_pack": [P, P, P],

@@ -37,6 +37,15 @@ __device__ __forceinline__ void project2(double2& nx, double2& ny, double kxv, d
     ny = make_double2(rsub(ny.x, gy.x), rsub(ny.y, gy.y));
 }
 
+// The projection with fused multiply-adds (N -= k (k . N) / k^2), for the
+// fused RK2mid stages.
+__device__ __forceinline__ void project2_fma(double2& nx, double2& ny, double kxv, double kyv, double s) {
+    const double cr = fma(kyv, ny.x, kxv * nx.x) * s;
+    const double ci = fma(kyv, ny.y, kxv * nx.y) * s;
+    nx = make_double2(fma(-kxv, cr, nx.x), fma(-kxv, ci, nx.y));
+    ny = make_double2(fma(-kyv, cr, ny.x), fma(-kyv, ci, ny.y));
+}
+
 __device__ __forceinline__ void phis2(const Stage2Args& a, int c, int q, double k2, double& Z, double& f0,
                                       double& f1, double& f2) {
     if (a.tab[c]) {
@@ -50,15 +59,18 @@ __device__ __forceinline__ void phis2(const Stage2Args& a, int c, int q, double 
     }
 }
 
+// One thread per kept entry of every run.  NF (2 hydro, 3 Boussinesq) and
+// MODE (0 = write deriv, 1 = RK2mid stage 1, 2 = stage 2) are template
+// parameters so that the per-field loop unrolls with static indices.
+template <int NF, int MODE>
 __global__ void k_stage2(Stage2Args a) {
     const Geo2& g = a.g;
-    const int64_t per = (int64_t)g.Kx * g.Ky;
-    const int64_t n = per * a.nrun;
-    const int nf = a.phys == PHYS_HYDRO ? 2 : 3;
+    const int per = g.Kx * g.Ky;
+    const int64_t n = (int64_t)per * a.nrun;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const int run = (int)(i / per);
-        const int64_t j = i - run * per;
-        const int kyc = (int)(j % g.Ky), ix = (int)(j / g.Ky);
+        const int j = (int)(i - (int64_t)run * per);
+        const int kyc = j % g.Ky, ix = j / g.Ky;
         const int ky_i = compact_to_full(kyc, g.Ny, g.Ky);
         const double kxv = a.kx[ix], kyv = a.ky[ky_i];
         // k2 = (0 + kx^2) + ky^2 (2D k dict order x, y)
@@ -67,40 +79,51 @@ __global__ void k_stage2(Stage2Args a) {
         double s;
         if (a.intk && a.inv_k2) s = a.inv_k2[q];
         else s = rdiv(1., k2 == 0. ? 1. : k2);
-        double2 N[3];
+        double2 N[NF];
         N[0] = ((const double2*)a.nc.p[0])[run * a.nc_rs + j];
         N[1] = ((const double2*)a.nc.p[1])[run * a.nc_rs + j];
-        if (a.phys == PHYS_BOUSS) {
+        if constexpr (NF == 3) {
             const int64_t ri = a.rin_compact ? run * a.rin_rs + j : run * a.rin_rs + (int64_t)ix * g.Ny + ky_i;
             const double2 T = ((const double2*)a.rin.p[2])[ri];
             const double2 ud = ((const double2*)a.rin.p[a.pp.dir])[ri];
             // buoyancy: ((T * g) * alpha_t) added to u_dir (physics.py:691-694)
             const double2 b = make_double2(rmul(rmul(T.x, a.pp.g), a.pp.alpha_t), rmul(rmul(T.y, a.pp.g), a.pp.alpha_t));
-            N[a.pp.dir] = make_double2(radd(N[a.pp.dir].x, b.x), radd(N[a.pp.dir].y, b.y));
+            if (a.pp.dir == 0) N[0] = make_double2(radd(N[0].x, b.x), radd(N[0].y, b.y));
+            else N[1] = make_double2(radd(N[1].x, b.x), radd(N[1].y, b.y));
             // temperature: (-(u.grad T)) - (u_dir * beta) (physics.py:702-708)
             const double2 adv = ((const double2*)a.nc.p[2])[run * a.nc_rs + j];
             N[2] = make_double2(rsub(-adv.x, rmul(ud.x, a.pp.beta)), rsub(-adv.y, rmul(ud.y, a.pp.beta)));
         }
-        project2(N[0], N[1], kxv, kyv, s);
+        if constexpr (MODE == 0) project2(N[0], N[1], kxv, kyv, s);
+        else project2_fma(N[0], N[1], kxv, kyv, s);
         const int64_t full = run * a.y_rs + (int64_t)ix * g.Ny + ky_i;
-        for (int c = 0; c < nf; c++) {
-            if (a.mode == 0) {
+#pragma unroll
+        for (int c = 0; c < NF; c++) {
+            if constexpr (MODE == 0) {
                 ((double2*)a.deriv.p[c])[run * a.d_rs + (int64_t)ix * g.Ny + ky_i] = N[c];
-                continue;
-            }
-            double Z, f0, f1, f2;
-            phis2(a, c, q, k2, Z, f0, f1, f2);
-            const double2 y0 = ((const double2*)a.y.p[c])[full];
-            const int64_t ci = run * a.c_rs + j;
-            if (a.mode == 1) {
-                ((double2*)a.k1.p[c])[ci] = N[c];
-                ((double2*)a.ys.p[c])[ci] = etd1_entry(y0, N[c], Z, f0, f1, a.h);
             } else {
-                const double2 d1 = ((const double2*)a.k1.p[c])[ci];
-                ((double2*)a.y.p[c])[full] = etd2rk2_entry(y0, d1, N[c], Z, f0, f1, f2, a.h);
+                double Z, f0, f1, f2;
+                phis2(a, c, q, k2, Z, f0, f1, f2);
+                const double2 y0 = ((const double2*)a.y.p[c])[full];
+                const int64_t ci = run * a.c_rs + j;
+                if constexpr (MODE == 1) {
+                    ((double2*)a.k1.p[c])[ci] = N[c];
+                    ((double2*)a.ys.p[c])[ci] = etd1_fma(y0, N[c], f0, f1 * a.h);
+                } else {
+                    const double2 d1 = ((const double2*)a.k1.p[c])[ci];
+                    ((double2*)a.y.p[c])[full] = etd2rk2_fma(y0, d1, N[c], f0, f1 * a.h, 2. * f2 * a.h);
+                }
             }
         }
     }
+}
+
+template <int MODE>
+static int launch_stage2(const Stage2Args& a, unsigned nb, const char* label, cudaStream_t st) {
+    if (a.phys == PHYS_HYDRO) DD_KT(label, st, k_stage2<2, MODE><<<nb, 256, 0, st>>>(a));
+    else DD_KT(label, st, k_stage2<3, MODE><<<nb, 256, 0, st>>>(a));
+    DD_LAUNCH_CHECK();
+    return DD_OK;
 }
 
 // Non-kept modes see no forcing: RK2mid gives y <- etd2rk2(y, 0, 0, dt) = f0 y.
@@ -225,15 +248,13 @@ int dd_rhs2d(const dd_plan* p, int phys, const double* params, int nrun, const v
                                        p->g2, d, deriv_rs, nrun));
         DD_LAUNCH_CHECK();
     }
-    DD_KT("stage2d", st, k_stage2<<<ew_grid2((int64_t)p->g2.Kx * p->g2.Ky * nrun), 256, 0, st>>>(a));
-    DD_LAUNCH_CHECK();
-    return DD_OK;
+    return launch_stage2<0>(a, ew_grid2((int64_t)p->g2.Kx * p->g2.Ky * nrun), "stage2d", st);
 }
 
 int dd_rk2mid_step2d(const dd_plan* p, int phys, const double* params, int nrun, void* const* state,
                      int64_t state_rs, const double* inv_k2, const void* const* tab_half,
                      const void* const* tab_full, const double* nu, int viscosity_order, double dt,
-                     int precision, void* work, size_t work_bytes, void* stream) {
+                     int precision, const int* nonkept_flag, void* work, size_t work_bytes, void* stream) {
     DD_TRY(check2(p, phys, nrun, params));
     DD_CHECK_ARG(state && work && nu, "dd_rk2mid_step2d: null pointer");
     DD_CHECK_ARG(viscosity_order >= 1, "viscosity_order must be >= 1");
@@ -260,18 +281,18 @@ int dd_rk2mid_step2d(const dd_plan* p, int phys, const double* params, int nrun,
     DD_TRY(nonlinear2_phys(phys, p, precision, false, w, (const void* const*)state, state_rs, st));
     for (int c = 0; c < nf; c++) { a.rin.p[c] = state[c]; a.tab[c] = intk ? (const double4*)tab_half[c] : nullptr; }
     a.rin_rs = state_rs; a.rin_compact = 0; a.h = dt / 2.; a.mode = 1;
-    DD_KT("rk2mid_stage2d", st, k_stage2<<<nb, 256, 0, st>>>(a));
-    DD_LAUNCH_CHECK();
+    DD_TRY(launch_stage2<1>(a, nb, "rk2mid_stage2d", st));
     // stage 2: k2 = N(y2); y = etd2rk2(y, k1, k2, dt)       (time_step.py:297-305)
     const void* ysp[3] = {a.ys.p[0], a.ys.p[1], a.ys.p[2]};
     DD_TRY(nonlinear2_phys(phys, p, precision, true, w, ysp, (int64_t)w.kc, st));
     for (int c = 0; c < nf; c++) { a.rin.p[c] = ysp[c]; a.tab[c] = intk ? (const double4*)tab_full[c] : nullptr; }
     a.rin_rs = (int64_t)w.kc; a.rin_compact = 1; a.h = dt; a.mode = 2;
-    DD_KT("rk2mid_stage2d", st, k_stage2<<<nb, 256, 0, st>>>(a));
-    DD_LAUNCH_CHECK();
-    DD_KT("decay_nonkept2", st, k_decay_nonkept2<<<ew_grid2(p->g2.kcount() * nrun), 256, 0, st>>>(
-                                    p->g2, a.y, state_rs, nf, nrun, p->kx, p->ky, a));
-    DD_LAUNCH_CHECK();
+    DD_TRY(launch_stage2<2>(a, nb, "rk2mid_stage2d", st));
+    if (!nonkept_flag || *nonkept_flag) {
+        DD_KT("decay_nonkept2", st, k_decay_nonkept2<<<ew_grid2(p->g2.kcount() * nrun), 256, 0, st>>>(
+                                        p->g2, a.y, state_rs, nf, nrun, p->kx, p->ky, a));
+        DD_LAUNCH_CHECK();
+    }
     return DD_OK;
 }
 

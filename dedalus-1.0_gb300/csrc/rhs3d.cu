@@ -37,6 +37,17 @@ __device__ __forceinline__ void project(double2& nx, double2& ny, double2& nz, d
     nz = make_double2(rsub(nz.x, gz.x), rsub(nz.y, gz.y));
 }
 
+// The same projection with fused multiply-adds: c = (k . N) / k^2, N -= k c
+// (i k_i (-(i k . N) / k^2) = k_i (k . N) / k^2).  Used inside the fused step.
+__device__ __forceinline__ void project_fma(double2& nx, double2& ny, double2& nz, double kxv, double kyv,
+                                            double kzv, double s) {
+    const double cr = fma(kzv, nz.x, fma(kyv, ny.x, kxv * nx.x)) * s;
+    const double ci = fma(kzv, nz.y, fma(kyv, ny.y, kxv * nx.y)) * s;
+    nx = make_double2(fma(-kxv, cr, nx.x), fma(-kxv, ci, nx.y));
+    ny = make_double2(fma(-kyv, cr, ny.x), fma(-kyv, ci, ny.y));
+    nz = make_double2(fma(-kzv, cr, nz.x), fma(-kzv, ci, nz.y));
+}
+
 // curlX of a k-space vector (physics.py:394-396), in place.
 __device__ __forceinline__ void curl_k(double2& vx, double2& vy, double2& vz, double kxv, double kyv, double kzv) {
     const double2 a0 = ideriv(vz, kyv), b0 = ideriv(vy, kzv);
@@ -123,32 +134,43 @@ template <int PH>
 __global__ void k_rk4_stage3(RK4Args a) {
     const Geo3& g = a.pa.g;
     constexpr int NF = Phys3<PH>::NF, NG = Phys3<PH>::NG;
-    const int64_t n = (int64_t)g.Ky * g.Kz * g.Kx;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        int kyc, kzc, ix, q;
-        kept_index(g, i, kyc, kzc, ix);
+    const int n = g.Ky * g.Kz * g.Kx;      // < 2^31 for every supported grid
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int ix = i % g.Kx, r = i / g.Kx;
+        const int kzc = r % g.Kz, kyc = r / g.Kz;
         const int ky_i = compact_to_full(kyc, g.Ny, g.Ky), kz_i = compact_to_full(kzc, g.Nz, g.Kz);
+        const double kxv = a.pa.kx[ix], kyv = a.pa.ky[ky_i], kzv = a.pa.kz[kz_i];
         const double k2 = k2_of(a.pa, ix, ky_i, kz_i);
+        int q;
         const double s = inv_k2_of(a.pa, k2, q);
         double2 k[6];
-        rhs_at<PH>(a.nc, i, a.pa.kx[ix], a.pa.ky[ky_i], a.pa.kz[kz_i], s, k);
-        double Z[NG], f0[NG], f1[NG];
 #pragma unroll
-        for (int grp = 0; grp < NG; grp++) phis_for(a, grp, q, k2, Z[grp], f0[grp], f1[grp]);
+        for (int c = 0; c < Phys3<PH>::NO; c++) k[c] = ((const double2*)a.nc.p[c])[i];
+        project_fma(k[0], k[1], k[2], kxv, kyv, kzv, s);
+        if constexpr (PH == P3_MHD) curl_k(k[3], k[4], k[5], kxv, kyv, kzv);
+        double f0[NG], f1h[NG];
+#pragma unroll
+        for (int grp = 0; grp < NG; grp++) {
+            double Z, f1;
+            phis_for(a, grp, q, k2, Z, f0[grp], f1);
+            f1h[grp] = f1 * a.h;
+        }
         const int64_t o = ((int64_t)ky_i * g.Nz + kz_i) * g.Nh + ix;
 #pragma unroll
         for (int c = 0; c < NF; c++) {
             const int grp = c / 3;
-            const double2 kw = make_double2(rmul(k[c].x, a.w), rmul(k[c].y, a.w));
             double2 t;
-            if (a.stage == 1) t = kw;
-            else { t = ((const double2*)a.tot.p[c])[i]; t = make_double2(radd(t.x, kw.x), radd(t.y, kw.y)); }
+            if (a.stage == 1) t = make_double2(k[c].x * a.w, k[c].y * a.w);
+            else {
+                t = ((const double2*)a.tot.p[c])[i];
+                t = make_double2(fma(k[c].x, a.w, t.x), fma(k[c].y, a.w, t.y));
+            }
             const double2 y0 = ((const double2*)a.y.p[c])[o];
             if (a.stage < 4) {
                 ((double2*)a.tot.p[c])[i] = t;
-                ((double2*)a.ys.p[c])[i] = etd1_entry(y0, k[c], Z[grp], f0[grp], f1[grp], a.h);
+                ((double2*)a.ys.p[c])[i] = etd1_fma(y0, k[c], f0[grp], f1h[grp]);
             } else {
-                ((double2*)a.y.p[c])[o] = etd1_entry(y0, t, Z[grp], f0[grp], f1[grp], a.h);
+                ((double2*)a.y.p[c])[o] = etd1_fma(y0, t, f0[grp], f1h[grp]);
             }
         }
     }

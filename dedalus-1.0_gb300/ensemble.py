@@ -76,6 +76,9 @@ class BoussinesqEnsemble2D:
         self.order = list(range(len(self.classes)))
         self.time = 0.
         self.iteration = 0
+        # per size class: 1 while some run may hold energy outside the kept
+        # modes (their decay is then applied every step), 0 once known clean
+        self._nonkept = {c.n: ctypes.c_int(1) for c in self.classes}
         self._tables = {}
         self._graph = None
         self._graph_dt = None
@@ -89,6 +92,7 @@ class BoussinesqEnsemble2D:
             for j, r in enumerate(c.runs):
                 host[j, 2] = init_cond.band_limited_noise_2d(c.shape, seed=seed + r, kmax=kmax, amplitude=amplitude)
             c.slab.copy_(torch.from_numpy(host))
+            self._nonkept[c.n].value = int(self._has_nonkept(c, host))
         self._graph = None
 
     def run_state(self, r):
@@ -105,9 +109,21 @@ class BoussinesqEnsemble2D:
                 j = c.runs.index(r)
                 for f in range(3):
                     c.slab[j, f].copy_(torch.as_tensor(np.asarray(fields[f])))
+                if self._has_nonkept(c, np.stack([np.asarray(x) for x in fields])[None]):
+                    self._nonkept[c.n].value = 1
                 self._graph = None
                 return
         raise IndexError(r)
+
+    @staticmethod
+    def _has_nonkept(c, host):
+        """Any non-zero entry outside the kept modes in host [run][field][kx][ky]?"""
+        kx, ky = c.kshape
+        M = c.plan.mx
+        keep = np.zeros((kx, ky), dtype=bool)
+        iy = np.arange(ky)
+        keep[:M + 1, :] = ((iy <= c.plan.my) | (iy >= ky - c.plan.my))[None, :]
+        return bool(np.any(host[..., ~keep] != 0))
 
     # ---------------------------------------------------------------- tables
     def _phi(self, c, coeff, h):
@@ -150,7 +166,8 @@ class BoussinesqEnsemble2D:
             base = c.slab[j0]
             fp, _f = _lib.ptr_array([base[f].data_ptr() for f in range(3)])
             _lib.call("dd_rk2mid_step2d", c.plan.handle, PHYS_BOUSS, self.params, nr, fp, rs, dptr(ik2), thp, tfp,
-                      nus, self.vo, float(dt), self.prec, dptr(ws), ws.numel(), st)
+                      nus, self.vo, float(dt), self.prec, ctypes.byref(self._nonkept[c.n]), dptr(ws), ws.numel(),
+                      st)
 
     def _issue_step(self, dt):
         main = torch.cuda.current_stream()

@@ -311,7 +311,7 @@ class IncompressibleHydro(Physics):
         ppa = None if pp is None else (ctypes.c_double * 4)(*pp)
         nus = (ctypes.c_double * 3)(*(coeffs + [0.] * (3 - len(coeffs))))
         _lib.call("dd_rk2mid_step2d", plan.handle, self._phys2d, ppa, 1, sp, 0,
-                  None if ik2 is None else dptr(ik2), th, tf, nus, vo, float(dt), prec,
+                  None if ik2 is None else dptr(ik2), th, tf, nus, vo, float(dt), prec, None,
                   dptr(ws), ws.numel(), current_stream())
         return True
 

@@ -175,7 +175,9 @@ int dd_hydro3d_rk4_step(const dd_plan* plan, void* const* u, const double* inv_k
  * zeroes the non-kept entries); dd_rk2mid_step2d advances the state in place
  * by one RK2mid step (time_step.py:275-309; euler/etd1/etd2rk2 with the 2D
  * Taylor branch), tab_half[c] / tab_full[c] being dd_phi_table(2, nu[c], vo, dt/2 or dt)
- * tables per state field when inv_k2 is given. */
+ * tables per state field when inv_k2 is given.  nonkept_flag: host int, 0
+ * when the caller knows no run has energy outside the kept modes (the decay
+ * of those modes is then skipped), or NULL to always treat them. */
 int dd_rhs2d_workspace_size(const dd_plan* plan, int nrun, int precision, size_t* bytes);
 int dd_rhs2d(const dd_plan* plan, int physics, const double* params, int nrun, const void* const* state,
              int64_t state_rs, void* const* deriv, int64_t deriv_rs, const double* inv_k2, int precision,
@@ -183,7 +185,7 @@ int dd_rhs2d(const dd_plan* plan, int physics, const double* params, int nrun, c
 int dd_rk2mid_step2d(const dd_plan* plan, int physics, const double* params, int nrun, void* const* state,
                      int64_t state_rs, const double* inv_k2, const void* const* tab_half,
                      const void* const* tab_full, const double* nu, int viscosity_order, double dt,
-                     int precision, void* work, size_t work_bytes, void* stream);
+                     int precision, const int* nonkept_flag, void* work, size_t work_bytes, void* stream);
 
 /* ------------------------------------------------------ fused 3D physics
  * physics 0 = IncompressibleHydro (state u_x, u_y, u_z; physics.py:527-599),
