@@ -623,6 +623,47 @@ def setup_dist():
             int(os.environ.get("LOCAL_RANK", "0")))
 
 
+class Replicas:
+    """The host side of an N-rank run: independent replicas (one per GPU),
+    joined only by barriers and a max over ranks of the timed durations (no
+    collective on the data path).  backend "nccl" on GPUs, "gloo" on CPU."""
+
+    def __init__(self, ws, backend="nccl", device=None):
+        self.ws = ws
+        self.dist = None
+        self.device = device
+        if ws > 1:
+            import torch.distributed as dist
+            if backend == "nccl":
+                dist.init_process_group("nccl", device_id=device)
+            else:
+                dist.init_process_group(backend)
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist is not None:
+            self.dist.barrier()
+
+    def max(self, x):
+        """Max of a float over ranks (every rank gets it)."""
+        if self.dist is None:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64, device=self.device)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def throughput(self, steps, ms_local):
+        """(whole-job steps/s over all replicas, slowest rank's ms)."""
+        ms = self.max(ms_local)
+        return self.ws * steps / (ms / 1e3), ms
+
+    def close(self):
+        if self.dist is not None:
+            self.dist.barrier()
+            self.dist.destroy_process_group()
+
+
 # ---------------------------------------------------------------- main
 def main():
     ap = argparse.ArgumentParser()
@@ -645,21 +686,8 @@ def main():
     dd = __graft_entry__.load_package()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    dist = None
-    if ws > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=dev)
-
-    def barrier():
-        if dist is not None:
-            dist.barrier()
-
-    def max_over_ranks(x):
-        if dist is None:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    reps = Replicas(ws, "nccl", dev)
+    barrier, max_over_ranks = reps.barrier, reps.max
 
     run = RUNNERS[wl["kind"]](dd, wl, rank)
     stream = torch.cuda.current_stream()
@@ -692,7 +720,7 @@ def main():
     launches = dd._lib.launch_count() - n0
     if run.launches_per_step is not None:
         launches = run.launches_per_step * args.steps      # graph replays launch the captured kernels
-    ms = max_over_ranks(e0.elapsed_time(e1))
+    value, ms = reps.throughput(args.steps, e0.elapsed_time(e1))
     kt = dd._lib.timing_report() if events_in_timed else {}
     dd._lib.timing_enable(False)
     # a timed region shorter than the 200 ms sampling period may hold no
@@ -721,7 +749,6 @@ def main():
         kernel_timing = "CUDA events per launch in a separate eager pass of %d steps after the timed region" % kp
     dd._lib.timing_enable(False)
     ms_per_step = ms / args.steps
-    value = ws * args.steps / (ms / 1e3)
 
     peaks = {}
     pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -901,9 +928,7 @@ def main():
                           "of its Cython stage kernels), single thread" % args.workload) if wl["kind"] != "ensemble"
                else "one oracle run per size class timed for 2-3 steps on one core, summed over the 512 runs"}
 
-    if dist is not None:
-        dist.barrier()
-        dist.destroy_process_group()
+    reps.close()
     if rank != 0:
         return 0
     metric, unit = run.metric()
