@@ -60,6 +60,18 @@ WORKLOADS = {
 }
 
 
+# DRAM bytes per launch of a workload's dominant kernel from one ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum), scaled to the full launch by
+# the units processed when the capture ran on a smaller grid.
+TRAFFIC = {
+    ("hydro3d-256-fp64", "x_cross_256_f64"): (
+        8 * (67.76e6 + 18.20e6),
+        "ncu capture of the same kernel on 128^3 FP64 (67.76 MB read + 18.20 MB written), x8 for 256^3"),
+    ("les64-closure", "les_mlp"): (
+        18.92e6 + 0.0, "ncu capture at full size (18.92 MB read, stresses still in L2 at kernel end)"),
+}
+
+
 def B3(N):
     return 8 * N ** 3 + 16 * N ** 2 * (N // 2 + 1)
 
@@ -775,8 +787,10 @@ def main():
         b = run.kernel_bytes(name)
         avg = tot / cnt / 1e3
         ach = b / avg / 1e9 if b else None
+        tr = TRAFFIC.get((args.workload, name))
         roofline = {"bound": "hbm", "kernel": name, "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
-                    "frac": (ach / hbm_peak) if ach else None, "traffic": None, "peak_source": peak_src,
+                    "frac": (ach / hbm_peak) if ach else None, "traffic": tr[0] if tr else None,
+                    "traffic_source": tr[1] if tr else None, "peak_source": peak_src,
                     "algorithmic_bytes_per_launch": b, "avg_launch_ms": avg * 1e3, "kernel_timing": kernel_timing}
         fl = getattr(run, "kernel_flops", lambda _n: None)(name)
         pipe = getattr(run, "kernel_flops_pipe", "bf16")
