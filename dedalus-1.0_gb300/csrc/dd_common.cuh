@@ -8,6 +8,7 @@
 
 #include "dd_gb300.h"
 #include "timing.cuh"
+#include <atomic>
 #include <string>
 
 namespace dd {
@@ -52,6 +53,18 @@ const char* last_error();
         int s_ = (expr);                                             \
         if (s_ != DD_OK) return s_;                                  \
     } while (0)
+
+// Raise a kernel's dynamic shared-memory limit once per device (the attribute
+// belongs to the device current at the call); `done` holds one bit per device.
+inline int ensure_smem(const void* fn, size_t bytes, std::atomic<unsigned long long>& done) {
+    int dev = 0;
+    DD_CUDA(cudaGetDevice(&dev));
+    const unsigned long long bit = dev < 64 ? (1ull << dev) : 0ull;
+    if (bit && (done.load(std::memory_order_acquire) & bit)) return DD_OK;
+    DD_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    done.fetch_or(bit, std::memory_order_release);
+    return DD_OK;
+}
 
 // ---------------------------------------------------------------- complex
 template <typename T>

@@ -51,11 +51,8 @@ int launch_pass(const Op& op, int npencil, int nslow, int nfield, cudaStream_t s
     constexpr int P = Pencil<L>::P, NT = Pencil<L>::NT;
     const size_t smem = Pencil<L>::template smem_bytes<T>();
     auto kern = k_pass<T, L, INV, LD_E, ST_E, Op>;
-    static bool configured = false;  // per instantiation
-    if (!configured) {
-        DD_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        configured = true;
-    }
+    static std::atomic<unsigned long long> configured{0};  // per instantiation and device
+    DD_TRY(ensure_smem((const void*)kern, smem, configured));
     if (npencil <= 0 || nslow <= 0 || nfield <= 0) return DD_OK;
     if (nslow > 65535 && nslow % 65535 != 0) {
         set_error("pass: slow extent %d must be <= 65535 or a multiple of it", nslow);

@@ -267,11 +267,8 @@ static int les_grads(const dd_plan* p, int prec, bool compact, const void* const
 }
 
 static int les_mlp(const dd_plan* p, const dd_closure* cl, const LesWork& w, double* const* tau, cudaStream_t st) {
-    static bool configured = false;
-    if (!configured) {
-        DD_CUDA(cudaFuncSetAttribute(k_les_mlp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(LesMlpSmem)));
-        configured = true;
-    }
+    static std::atomic<unsigned long long> configured{0};
+    DD_TRY(ensure_smem((const void*)k_les_mlp, sizeof(LesMlpSmem), configured));
     const int64_t npts = p->g3.xcount();
     CPtrs gx{};
     Ptrs t{};

@@ -279,11 +279,6 @@ __global__ void k_mlp_normalize(const float* __restrict__ raw, int64_t n, const 
     }
 }
 
-static int set_smem(const void* fn, size_t bytes) {
-    DD_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-    return DD_OK;
-}
-
 }  // namespace dd
 
 using namespace dd;
@@ -318,11 +313,8 @@ int dd_mlp_infer(const void* X, float* Y, int64_t n, const void* wbf16, const fl
     DD_CHECK_ARG(X && Y && wbf16 && params && n >= 0, "dd_mlp_infer: bad arguments");
     if (n == 0) return DD_OK;
     cudaStream_t st = (cudaStream_t)stream;
-    static bool configured = false;
-    if (!configured) {
-        DD_TRY(set_smem((const void*)k_mlp_infer, sizeof(MlpFwdSmem)));
-        configured = true;
-    }
+    static std::atomic<unsigned long long> configured{0};
+    DD_TRY(ensure_smem((const void*)k_mlp_infer, sizeof(MlpFwdSmem), configured));
     unsigned nb = ew_blocks(n, 64);
     if (nb > 152 * 4) nb = 152 * 4;
     DD_KT("mlp_infer", st,
@@ -337,11 +329,8 @@ int dd_mlp_grad(const void* X, const float* T, const int64_t* idx, int64_t n, in
     const int nb = grad_blocks(n);
     DD_CHECK_ARG(work_bytes >= (size_t)nb * MLP_PSTRIDE * sizeof(float), "dd_mlp_grad: workspace too small");
     cudaStream_t st = (cudaStream_t)stream;
-    static bool configured = false;
-    if (!configured) {
-        DD_TRY(set_smem((const void*)k_mlp_grad, sizeof(MlpSmem)));
-        configured = true;
-    }
+    static std::atomic<unsigned long long> configured{0};
+    DD_TRY(ensure_smem((const void*)k_mlp_grad, sizeof(MlpSmem), configured));
     const float scale = 2.0f / ((float)n_total * (float)MLP_NOUT);
     float* part = (float*)work;
     DD_KT("mlp_grad", st,

@@ -160,11 +160,8 @@ int launch_x_prod(const char* name, int nrows, int Kx, const CPtrs& win, const P
                   int64_t out_rs, const typename Vec2<T>::type* tw, T scale, const Op& op, cudaStream_t st) {
     using CC = ProdCfg<L, Op::NI, Op::NO>;
     const size_t smem = prod_smem<L, Op::NI, Op::NO>(sizeof(C<T>));
-    static bool configured = false;
-    if (!configured) {
-        DD_CUDA(cudaFuncSetAttribute(k_x_prod<T, L, Op>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        configured = true;
-    }
+    static std::atomic<unsigned long long> configured{0};
+    DD_TRY(ensure_smem((const void*)k_x_prod<T, L, Op>, smem, configured));
     static const std::string label = std::string(name) + "_" + std::to_string(L) + PrecName<T>::s;
     DD_KT(label.c_str(), st,
           k_x_prod<T, L, Op><<<dim3(cdiv(nrows, CC::Q), nrun), CC::NT, smem, st>>>(nrows, Kx, win, wout, in_rs, out_rs,
