@@ -12,13 +12,14 @@ so no L2 flush is needed between steps.  Other workloads (one per benchmark
 configuration of the project):
 
     hydro3d-256-{fp64,df64,fp32}  3D hydro 256^3 RK4 with FP64 / double-float / FP32 transforms
-    hydro3d-128-fp64              the same at 128^3
+    hydro3d-128-{fp64,df64}       the same at 128^3 (small cases for profiling)
     mhd3d-256-{fp32,fp64}         3D MHD 256^3 RK4, nu = eta = 5e-3, dt = 1e-3
     hydro2d-128                   2D hydro 128^2 RK2mid, nu = 1e-3, dt = 1e-3
     bouss2d-ensemble-512[-fp32]   512 2D Boussinesq runs, sizes uniform in {64,128,256,512}^2,
                                   nu = kappa = 2e-3, N^2 = 1, RK2mid, dt = 1e-2, one CUDA graph per step
                                   (FP64 or autotuned FP32 transforms; the FP32 line reports its
                                   difference from the FP64 ensemble)
+    bouss2d-ensemble-64-fp32      64 runs in {256,512}^2, FP32 (small case for profiling)
     les64-closure                 64^3 LES with the learned subgrid closure (trained weights in
                                   dedalus-1.0_gb300/data), RK4, nu = 5e-3, dt = 2e-3, FP32 transforms,
                                   one CUDA graph per step; reports the FP64 256^3 DNS rate beside it
@@ -49,6 +50,7 @@ WORKLOADS = {
     "hydro3d-256-df64": dict(kind="hydro3d", shape=(256,) * 3, nu=5e-3, dt=2e-3, precision="df64"),
     "hydro3d-256-fp32": dict(kind="hydro3d", shape=(256,) * 3, nu=5e-3, dt=2e-3, precision="fp32"),
     "hydro3d-128-fp64": dict(kind="hydro3d", shape=(128,) * 3, nu=5e-3, dt=2e-3, precision="fp64"),
+    "hydro3d-128-df64": dict(kind="hydro3d", shape=(128,) * 3, nu=5e-3, dt=2e-3, precision="df64"),
     "mhd3d-256-fp32": dict(kind="mhd3d", shape=(256,) * 3, nu=5e-3, dt=1e-3, precision="fp32"),
     "mhd3d-256-fp64": dict(kind="mhd3d", shape=(256,) * 3, nu=5e-3, dt=1e-3, precision="fp64"),
     "hydro2d-128": dict(kind="hydro2d", shape=(128, 128), nu=1e-3, dt=1e-3, precision="fp64"),
@@ -56,6 +58,8 @@ WORKLOADS = {
                                  precision="fp64"),
     "bouss2d-ensemble-512-fp32": dict(kind="ensemble", nrun=512, sizes=(64, 128, 256, 512), nu=2e-3, dt=1e-2,
                                       precision="fp32"),
+    "bouss2d-ensemble-64-fp32": dict(kind="ensemble", nrun=64, sizes=(256, 512), nu=2e-3, dt=1e-2,
+                                     precision="fp32"),
     "les64-closure": dict(kind="les", shape=(64,) * 3, nu=5e-3, dt=2e-3, precision="fp32"),
 }
 
