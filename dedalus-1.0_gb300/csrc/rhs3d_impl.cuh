@@ -43,7 +43,7 @@ template <typename T, bool COMPACT, int NG>
 struct OpZInvCurl3 {
     using V = typename Vec2<T>::type;
     static constexpr const char* name = NG == 1 ? "z_inv_curl" : "z_inv_curl_mhd";
-    static constexpr int lmin = 16, lmax = 256;
+    static constexpr int lmin = 16, lmax = 512;
     Geo3 g; CPtrs u; Ptrs out; const V* tw;
     const double* kx; const double* ky; const double* kz;
     __device__ int npencil() const { return g.Kx; }
@@ -79,7 +79,7 @@ struct OpZInvCurl3 {
 template <typename T>
 struct ProdHydro3 {
     static constexpr int NI = 6, NO = 3;
-    static constexpr int lmin = 16, lmax = 256;
+    static constexpr int lmin = 16, lmax = 512;
     __device__ void operator()(const T* in, T* out, int) const {
         const T ux = in[0], uy = in[1], uz = in[2], wx = in[3], wy = in[4], wz = in[5];
         out[0] = uy * wz - uz * wy;
@@ -92,7 +92,7 @@ struct ProdHydro3 {
 template <typename T>
 struct ProdMHD3 {
     static constexpr int NI = 12, NO = 6;
-    static constexpr int lmin = 16, lmax = 256;
+    static constexpr int lmin = 16, lmax = 512;
     T inv_fpr;
     __device__ void operator()(const T* in, T* out, int) const {
         const T ux = in[0], uy = in[1], uz = in[2], wx = in[3], wy = in[4], wz = in[5];
@@ -111,7 +111,7 @@ template <typename T>
 struct OpZFwdCompact3 {
     using V = typename Vec2<T>::type;
     static constexpr const char* name = "z_fwd_compact";
-    static constexpr int lmin = 16, lmax = 256;
+    static constexpr int lmin = 16, lmax = 512;
     Geo3 g; CPtrs in; Ptrs out; const V* tw;
     __device__ int npencil() const { return g.Kx; }
     __device__ int nstore() const { return g.Nz; }

@@ -119,3 +119,45 @@ def test_boussinesq2d_general_box(dd, cuda):
         to.do_advance(do, 1e-2)
         tg.do_advance(dg, 1e-2)
     assert rel_l2(*states(do, dg, names)) < 1e-12
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape", [(512, 32, 32), (32, 512, 32), (32, 32, 512)])
+def test_hydro3d_rk4_512_axis(dd, cuda, shape):
+    """Length-512 transforms along each axis of the fused 3D step (the largest
+    supported length), one RK4 step against the oracle."""
+    u = dd.init_cond.turbulence_3d(shape, seed=38)
+    ro, do, rg, dg = pair(dd, 'IncompressibleHydro', shape, None, {'nu': 5e-3}, {f: u[f[1]] for f in U3})
+    OT.RK4(ro).do_advance(do, 2e-3)
+    dd.mods.RK4(rg).do_advance(dg, 2e-3)
+    assert rel_l2(*states(do, dg, U3)) < 1e-12
+
+
+@pytest.mark.gpu
+def test_mhd_rk4_512_x_axis(dd, cuda):
+    shape = (16, 32, 512)
+    u = dd.init_cond.turbulence_3d(shape, seed=39, k0=3.0)
+    b = dd.init_cond.turbulence_3d(shape, seed=40, k0=3.0)
+    f = {('u', i): u[i] for i in range(3)}
+    f.update({('B', i): b[i] for i in range(3)})
+    ro, do, rg, dg = pair(dd, 'IncompressibleMHD', shape, None, {'nu': 5e-3, 'eta': 5e-3}, f)
+    names = U3 + [('B', 0), ('B', 1), ('B', 2)]
+    OT.RK4(ro).do_advance(do, 1e-3)
+    dd.mods.RK4(rg).do_advance(dg, 1e-3)
+    assert rel_l2(*states(do, dg, names)) < 1e-12
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape", [(8, 16, 16), (16, 16, 1024)])
+def test_3d_lengths_outside_the_supported_range_raise(dd, cuda, shape):
+    """8 points (below the fused passes' 16) and 1024 (above the plans' 512)
+    raise NotImplementedError, as the reference does for unsupported options."""
+    u = dd.init_cond.turbulence_3d(shape, seed=41)
+    M = dd.mods
+    with pytest.raises(NotImplementedError):
+        rg = M.IncompressibleHydro(shape, M.FourierRepresentation)
+        rg.parameters['nu'] = 5e-3
+        dg = rg.create_fields(0.)
+        for i in range(3):
+            dg['u'][i]['kspace'] = u[i]
+        M.RK4(rg).do_advance(dg, 2e-3)
