@@ -67,7 +67,7 @@ constexpr size_t prod_smem(size_t csize) {
 }
 
 template <typename T, int L, class Op>
-__global__ void __launch_bounds__(ProdCfg<L, Op::NI, Op::NO>::NT)
+__global__ void __launch_bounds__(ProdCfg<L, Op::NI, Op::NO>::NT, std::is_same<T, df64>::value ? 5 : 1)
 k_x_prod(int nrows, int Kx, CPtrs win, Ptrs wout, int64_t in_rs, int64_t out_rs,
          const typename Vec2<T>::type* gtw, T scale, const Op op) {
     using V = typename Vec2<T>::type;
