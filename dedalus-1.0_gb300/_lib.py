@@ -76,6 +76,7 @@ SIGNATURES = {
     "dd_les_gradients": [P, PP, PP, I, P, SZ, P],
     "dd_les_samples": [I64, PP, PP, PP, D, P, P],
     "dd_les_stress": [P, PP, PP, P, I, P, SZ, P],
+    "dd_les_band": [P, I, PP, D, D, P],
     "dd_les_workspace_size": [P, I, ctypes.POINTER(SZ)],
     "dd_les_rhs3d": [P, PP, PP, P, I, I, P, P, SZ, P],
     "dd_les_rk4_step3d": [P, PP, P, PP, PP, P, I, D, I, ctypes.POINTER(I), P, P, SZ, P],

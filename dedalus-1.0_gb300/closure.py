@@ -232,9 +232,11 @@ class FilteredSampler:
         _lib.call("dd_les_truncate3", self.dns.handle, self.les.handle, 3, sp, dp, current_stream())
         return out
 
-    def samples(self, u_k, raw):
+    def samples(self, u_k, raw, raw_band=None, band=None):
         """Fill raw [npts][16] FP32 with the samples of the DNS velocity u_k
-        (3 full-layout k arrays on the DNS grid)."""
+        (3 full-layout k arrays on the DNS grid); with raw_band and band =
+        (lo, hi), also the samples of the stress restricted to that spectral
+        band (weight 0 below lo, 1 above hi, linear between)."""
         st = current_stream()
         self.dns.c2r(list(u_k), self._ux)
         up, _a = _ptrs(self._ux)
@@ -257,20 +259,32 @@ class FilteredSampler:
         _lib.call("dd_les_gradients", self.les.handle, kp, gp, _lib.DD_FP64, dptr(self._ws), self._ws.numel(), st)
         fp, _g = _ptrs(self._lx[3:])
         _lib.call("dd_les_samples", self.npts, gp, fp, rpp, self.delta, dptr(raw), st)
+        if raw_band is not None:
+            tau = [a - b for a, b in zip(self._lx[3:], self._rp)]
+            self.les.r2c(tau, self._rk)
+            kp2, _j = _ptrs(self._rk)
+            _lib.call("dd_les_band", self.les.handle, 6, kp2, float(band[0]), float(band[1]), st)
+            self.les.c2r(self._rk, tau)
+            zero = [torch.zeros_like(tau[0])] * 6
+            tp, _k = _ptrs(tau)
+            zp, _l = _ptrs(zero)
+            _lib.call("dd_les_samples", self.npts, gp, tp, zp, self.delta, dptr(raw_band), st)
 
 
 def generate_dataset(n_seeds=50, n_snap=20, stride=50, dns_n=256, les_n=64, nu=5e-3, dt=2e-3, seed0=1000,
-                     log=None):
+                     log=None, band=None):
     """Run the FP64 DNS (RK4, nu, dt) from n_seeds random turbulent states
     (turbulence_3d, unit energy) and sample n_snap filtered snapshots per seed,
     one every `stride` steps.  Returns (raw [n][16] FP32 device tensor, seed of
-    each snapshot, info)."""
+    each snapshot, info); with band = (lo, hi) the info dict also holds
+    "raw_band", the samples of the band-restricted stress."""
     from . import mods
     from .init_cond import turbulence_3d
     shape = (dns_n,) * 3
     sampler = FilteredSampler(shape, (les_n,) * 3)
     npts = sampler.npts
     raw = torch.empty((n_seeds * n_snap * npts, 16), dtype=torch.float32, device=sampler.les.device)
+    raw_band = torch.empty_like(raw) if band is not None else None
     RHS = mods.IncompressibleHydro(shape, mods.FourierRepresentation)
     RHS.parameters['nu'] = nu
     data = RHS.create_fields(0.)
@@ -293,7 +307,8 @@ def generate_dataset(n_seeds=50, n_snap=20, stride=50, dns_n=256, les_n=64, nu=5
                 ti.do_advance(data, dt)
                 steps += 1
             k = (s * n_snap + j) * npts
-            sampler.samples([data['u'][i].kdata for i in range(3)], raw[k:k + npts])
+            sampler.samples([data['u'][i].kdata for i in range(3)], raw[k:k + npts],
+                            None if raw_band is None else raw_band[k:k + npts], band)
             seeds.append(seed0 + s)
         if log:
             torch.cuda.synchronize()
@@ -302,6 +317,9 @@ def generate_dataset(n_seeds=50, n_snap=20, stride=50, dns_n=256, les_n=64, nu=5
     torch.cuda.synchronize()
     info = {"n_seeds": n_seeds, "n_snap": n_snap, "stride": stride, "dns_n": dns_n, "les_n": les_n, "nu": nu,
             "dt": dt, "seed0": seed0, "dns_steps": steps, "seconds": time.time() - t0, "delta": sampler.delta}
+    if raw_band is not None:
+        info["band"] = list(band)
+        info["raw_band"] = raw_band
     return raw, np.array(seeds), info
 
 

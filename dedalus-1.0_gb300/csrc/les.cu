@@ -207,6 +207,27 @@ __global__ void k_les_truncate3(Geo3 gs, Geo3 gd, CPtrs s, Ptrs d) {
     }
 }
 
+__global__ void k_les_band(Geo3 g, const double* kx, const double* ky, const double* kz, Ptrs k, double lo,
+                           double hi) {
+    double2* K = (double2*)k.p[blockIdx.y];
+    const int64_t n = g.kcount();
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int ix = (int)(i % g.Nh);
+        const int64_t r = i / g.Nh;
+        const int kz_i = (int)(r % g.Nz), ky_i = (int)(r / g.Nz);
+        double w = 0.;
+        if (ix <= g.Mx && kept_full(ky_i, g.Ny, g.My) && kept_full(kz_i, g.Nz, g.Mz)) {
+            w = 1.;
+            if (hi > 0.) {
+                const double kk = sqrt(kx[ix] * kx[ix] + ky[ky_i] * ky[ky_i] + kz[kz_i] * kz[kz_i]);
+                w = kk <= lo ? 0. : (kk >= hi ? 1. : (kk - lo) / (hi - lo));
+            }
+        }
+        const double2 v = K[i];
+        K[i] = make_double2(v.x * w, v.y * w);
+    }
+}
+
 __global__ void k_les_samples(int64_t npts, CPtrs gx, CPtrs f, CPtrs fr, double delta, float* raw) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < npts; i += (int64_t)gridDim.x * blockDim.x) {
         __align__(16) float r[16];
@@ -385,6 +406,19 @@ int dd_les_gradients(const dd_plan* p, const void* const* u, double* const* gx, 
     DD_TRY(les_grads(p, precision, false, u, w, st));
     const int64_t xb = p->g3.xcount() * (int64_t)sizeof(double);
     for (int f = 0; f < 9; f++) DD_CUDA(cudaMemcpyAsync(gx[f], w.gx[f], xb, cudaMemcpyDeviceToDevice, st));
+    return DD_OK;
+}
+
+int dd_les_band(const dd_plan* p, int nfield, void* const* k, double lo, double hi, void* stream) {
+    DD_TRY(les_check_plan(p));
+    DD_CHECK_ARG(k && nfield >= 1 && nfield <= DD_MAXF, "dd_les_band: bad arguments");
+    Ptrs kp{};
+    for (int f = 0; f < nfield; f++) { DD_CHECK_ARG(k[f], "null field %d", f); kp.p[f] = k[f]; }
+    const Geo3& g = p->g3;
+    cudaStream_t st = (cudaStream_t)stream;
+    DD_KT("les_band", st,
+          k_les_band<<<dim3(les_grid(g.kcount()), nfield), 256, 0, st>>>(g, p->kx, p->ky, p->kz, kp, lo, hi));
+    DD_LAUNCH_CHECK();
     return DD_OK;
 }
 

@@ -1,14 +1,18 @@
 """Make the learned LES closure: run the FP64 DNS, sample filtered snapshots,
-train the MLP on the GPU, save the weights and (optionally) evaluate the closed
-and unclosed 64^3 LES against the filtered DNS.
+train the MLP on the GPU, choose the closure-term band and gain on a
+validation seed, save the weights and evaluate the closed and unclosed 64^3
+LES against the filtered DNS on a test seed.
 
     python dedalus-1.0_gb300/data/make_closure.py --seeds 50 --snaps 20 \
-        --stride 50 --epochs 6 --eval-steps 1000 --out les_closure_256to64.npz \
-        --report closure_report.json
+        --stride 50 --epochs 10 --band-target 10.5 21 --select-seed 11 \
+        --eval-seed 7 --eval-steps 1000 --report closure_report.json
 
-Seeds seed0 .. seed0 + seeds - 1 make the training data; the last
-``--val-seeds`` of them are held out for validation; the evaluation run uses
-``--eval-seed`` (not a training seed).
+Seeds seed0 .. seed0 + seeds - 1 make the training data (the last
+``--val-seeds`` of them held out for the validation loss); ``--select-seed``
+chooses among the candidate closures, ``--eval-seed`` (used for neither)
+measures the chosen one.  With ``--band-target lo hi`` a second network is
+trained on the stress restricted to that spectral band (the part of tau the
+banded closure term uses) and competes in the selection.
 """
 import argparse
 import json
@@ -33,11 +37,13 @@ def main(argv=None):
     ap.add_argument("--les", type=int, default=64)
     ap.add_argument("--nu", type=float, default=5e-3)
     ap.add_argument("--dt", type=float, default=2e-3)
-    ap.add_argument("--epochs", type=int, default=6)
+    ap.add_argument("--epochs", type=int, default=10)
     ap.add_argument("--batch", type=int, default=65536)
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--lr-min", type=float, default=2e-5)
     ap.add_argument("--init-seed", type=int, default=0)
+    ap.add_argument("--band-target", type=float, nargs=2, default=None, metavar=("LO", "HI"))
+    ap.add_argument("--select-seed", type=int, default=None)
     ap.add_argument("--eval-steps", type=int, default=0)
     ap.add_argument("--eval-every", type=int, default=100)
     ap.add_argument("--eval-seed", type=int, default=7)
@@ -58,7 +64,16 @@ def main(argv=None):
         print(msg, flush=True)
 
     rep = {"args": vars(a)}
-    raw, seeds, info = C.generate_dataset(a.seeds, a.snaps, a.stride, a.dns, a.les, a.nu, a.dt, a.seed0, log=log)
+
+    def write_report():
+        if a.report:
+            with open(a.report, "w") as f:
+                json.dump(rep, f)
+
+    band = tuple(a.band_target) if a.band_target else None
+    raw, seeds, info = C.generate_dataset(a.seeds, a.snaps, a.stride, a.dns, a.les, a.nu, a.dt, a.seed0, log=log,
+                                          band=band)
+    raw_band = info.pop("raw_band", None)
     rep["data"] = info
     log("samples: %d (%.1f s of DNS, %d steps)" % (raw.shape[0], info["seconds"], info["dns_steps"]))
     if a.dump_samples:
@@ -66,44 +81,71 @@ def main(argv=None):
         g.manual_seed(1)
         pick = torch.randperm(raw.shape[0], generator=g, device=raw.device)[:a.dump_samples]
         np.save(a.dump_path, raw[pick].cpu().numpy())
-    cl = C.MLPClosure(info["delta"], seed=a.init_seed)
-    cl.set_norm(*C.fit_norm(raw))
-    X, T = C.normalise(cl, raw)
-    del raw
-    torch.cuda.empty_cache()
-    npts = (a.les ** 3)
+    npts = a.les ** 3
     nval = min(a.val_seeds, a.seeds - 1) * a.snaps * npts
-    ntr = X.shape[0] - nval
-    tr = torch.arange(ntr, device=X.device, dtype=torch.int64)
-    va = torch.arange(ntr, X.shape[0], device=X.device, dtype=torch.int64) if nval else None
-    t0 = time.time()
-    hist = C.train(cl, X, T, tr, va, epochs=a.epochs, batch=a.batch, lr=a.lr, lr_min=a.lr_min, log=log)
-    torch.cuda.synchronize()
-    rep["train"] = {"history": hist, "seconds": time.time() - t0, "adam_steps": cl.step,
-                    "samples_per_s": a.epochs * (ntr // a.batch) * a.batch / (time.time() - t0)}
-    if va is not None:
-        rep["train"]["val_correlation"] = C.correlation(cl, X, T, va).tolist()
-        log("validation correlation per component: %s" % np.round(rep["train"]["val_correlation"], 3))
-    cl.meta = {"data": info, "train": {k: v for k, v in rep["train"].items() if k != "history"},
-               "final": hist[-1] if hist else None}
-    cl.save(a.out)
-    log("saved %s" % a.out)
-    if a.report:
-        with open(a.report, "w") as f:
-            json.dump(rep, f)
-    del X, T
+
+    def fit(samples, name):
+        cl = C.MLPClosure(info["delta"], seed=a.init_seed)
+        cl.set_norm(*C.fit_norm(samples))
+        X, T = C.normalise(cl, samples)
+        ntr = X.shape[0] - nval
+        tr = torch.arange(ntr, device=X.device, dtype=torch.int64)
+        va = torch.arange(ntr, X.shape[0], device=X.device, dtype=torch.int64) if nval else None
+        t0 = time.time()
+        hist = C.train(cl, X, T, tr, va, epochs=a.epochs, batch=a.batch, lr=a.lr, lr_min=a.lr_min, log=log)
+        torch.cuda.synchronize()
+        tinfo = {"history": hist, "seconds": time.time() - t0, "adam_steps": cl.step,
+                 "samples_per_s": a.epochs * (ntr // a.batch) * a.batch / (time.time() - t0)}
+        if va is not None:
+            tinfo["val_correlation"] = C.correlation(cl, X, T, va).tolist()
+            log("%s: validation correlation per component %s" % (name, np.round(tinfo["val_correlation"], 3)))
+        cl.meta = {"data": info, "train": {k: v for k, v in tinfo.items() if k != "history"},
+                   "final": hist[-1] if hist else None, "target": name}
+        del X, T
+        torch.cuda.empty_cache()
+        return cl, tinfo
+
+    models = {}
+    models["stress"], rep["train"] = fit(raw, "stress")
+    del raw
+    if raw_band is not None:
+        models["band_stress"], rep["train_band"] = fit(raw_band, "band_stress [%g, %g]" % band)
+        del raw_band
     torch.cuda.empty_cache()
+    write_report()
+
+    chosen = models["stress"]
+    if a.select_seed is not None:
+        cands = {"stress_all_modes": models["stress"]}
+        for lo, hi, gn in [(10.5, 21.0, 1.0), (10.5, 21.0, 2.0), (10.5, 15.75, 1.5)]:
+            cands["stress_band_%g_%g_x%g" % (lo, hi, gn)] = models["stress"].with_band(lo, hi, gn)
+        if "band_stress" in models:
+            for gn in (1.0, 1.5, 2.0, 3.0):
+                cands["band_stress_x%g" % gn] = models["band_stress"].with_band(band[0], band[1], gn)
+        cands["no_model"] = None
+        ev = C.evaluate(cands, seed=a.select_seed, dns_n=a.dns, les_n=a.les, nu=a.nu, dt=a.dt,
+                        nsteps=a.eval_steps or 1000, every=a.eval_every, log=log)
+        score = {n: max(ev[n]["err_half"]) for n in ev["models"]}
+        rep["selection"] = {"seed": a.select_seed, "max_err_k_le_kmax_half": score}
+        best = min((n for n in score if n != "no_model"), key=lambda n: score[n])
+        chosen = cands[best]
+        rep["selection"]["chosen"] = {"name": best, "band": list(chosen.band), "gain": chosen.gain}
+        log("selected %s (%.4f) on seed %d" % (best, score[best], a.select_seed))
+        write_report()
+
+    chosen.meta["selection"] = rep.get("selection")
+    chosen.save(a.out)
+    log("saved %s" % a.out)
     if a.eval_steps:
-        ev = C.evaluate(cl, seed=a.eval_seed, dns_n=a.dns, les_n=a.les, nu=a.nu, dt=a.dt, nsteps=a.eval_steps,
+        final = {"chosen": chosen, "stress_all_modes": models["stress"], "no_model": None}
+        ev = C.evaluate(final, seed=a.eval_seed, dns_n=a.dns, les_n=a.les, nu=a.nu, dt=a.dt, nsteps=a.eval_steps,
                         every=a.eval_every, log=log)
         rep["eval"] = ev
         for name in ev["models"]:
             r = ev[name]
             log("%s: max E(k) err k<=kmax/2 %.4f, k<=kmax %.4f, final diss %.5f + sgs %.5f (DNS %.5f)" % (
                 name, max(r["err_half"]), max(r["err_full"]), r["diss"][-1], r["diss_sgs"][-1], ev["dns_diss"][-1]))
-    if a.report:
-        with open(a.report, "w") as f:
-            json.dump(rep, f)
+    write_report()
 
 
 if __name__ == "__main__":

@@ -293,6 +293,10 @@ int dd_les_gradients(const dd_plan* plan, const void* const* u, double* const* g
  * (all grid-point values on the LES grid). */
 int dd_les_samples(int64_t npts, const double* const* g, const double* const* f, const double* const* fr,
                    double delta, float* raw, void* stream);
+/* Spectral band weight in place on nfield full-layout complex128 arrays: kept
+ * modes times w(|k|) (0 for |k| <= lo, 1 for |k| >= hi, linear between; w = 1
+ * when hi <= 0), non-kept modes zeroed. */
+int dd_les_band(const dd_plan* plan, int nfield, void* const* k, double lo, double hi, void* stream);
 /* Grid-point subgrid stress predicted by the closure for velocity u. */
 int dd_les_stress(const dd_plan* plan, const void* const* u, double* const* tau, const dd_closure* cl,
                   int precision, void* work, size_t work_bytes, void* stream);

@@ -163,8 +163,16 @@ def gradients(u, shape):
     return [to_x(1j * kv[j] * u[a], shape) for a in range(3) for j in range(3)]
 
 
-def samples(u_dns, dns_shape, les_shape, delta):
-    """raw [n][16] FP32 rows (G, delta, tau) of one DNS state u_dns (k arrays)."""
+def band_weight(shape, band):
+    """w(|k|) on the k layout: 0 for |k| <= band[0], 1 for |k| >= band[1]."""
+    kx, ky, kz = kvectors(shape)
+    kk = np.sqrt(kx ** 2 + ky ** 2 + kz ** 2)
+    return np.clip((kk - band[0]) / (band[1] - band[0]), 0.0, 1.0)
+
+
+def samples(u_dns, dns_shape, les_shape, delta, band=None):
+    """raw [n][16] FP32 rows (G, delta, tau) of one DNS state u_dns (k arrays);
+    with band = (lo, hi) the stress is restricted to that spectral band."""
     ux = [to_x(c, dns_shape) for c in u_dns]
     prods = [to_k(ux[a] * ux[b]) for a, b in PAIRS]
     ub = [truncate(c, dns_shape, les_shape) for c in u_dns]
@@ -179,7 +187,10 @@ def samples(u_dns, dns_shape, les_shape, delta):
     raw[:, 9] = delta
     for c, (a, b) in enumerate(PAIRS):
         fr = to_x(to_k(ubx[a] * ubx[b]), les_shape)
-        raw[:, 10 + c] = (fbx[c] - fr).ravel()
+        tau = fbx[c] - fr
+        if band is not None:
+            tau = to_x(to_k(tau) * band_weight(les_shape, band), les_shape)
+        raw[:, 10 + c] = tau.ravel()
     return raw
 
 

@@ -156,6 +156,24 @@ def test_filtered_samples_match_oracle(dd, cuda):
 
 
 @pytest.mark.gpu
+def test_band_restricted_samples_match_oracle(dd, cuda):
+    import torch
+    dns, les = (64, 64, 64), (32, 32, 32)
+    u = dd.init_cond.turbulence_3d(dns, seed=14)
+    s = dd.closure.FilteredSampler(dns, les)
+    raw = torch.empty((int(np.prod(les)), 16), dtype=torch.float32, device="cuda")
+    rawb = torch.empty_like(raw)
+    s.samples([_dev(c) for c in u], raw, rawb, (5.0, 10.0))
+    r, rb = raw.cpu().numpy(), rawb.cpu().numpy()
+    ro = OC.samples(u, dns, les, s.delta, band=(5.0, 10.0))
+    assert np.array_equal(r[:, :10], rb[:, :10])
+    for col in range(10, 16):
+        scale = np.max(np.abs(ro[:, col]))
+        assert np.max(np.abs(rb[:, col] - ro[:, col])) <= 1e-6 * scale, col
+        assert np.max(np.abs(rb[:, col] - r[:, col])) > 1e-3 * scale      # the band removed something
+
+
+@pytest.mark.gpu
 def test_truncation_copies_kept_modes(dd, cuda):
     import torch
     dns, les = (64, 64, 64), (32, 32, 32)
