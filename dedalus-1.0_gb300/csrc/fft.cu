@@ -19,7 +19,11 @@ void set_error(const char* fmt, ...) {
 }
 const char* last_error() { return g_err; }
 
-static bool is_pow2(int64_t n) { return n >= 8 && n <= 512 && (n & (n - 1)) == 0; }
+// Supported axis lengths: powers of two 8..512 and 3 x a power of two 24..192.
+static bool is_supported_len(int64_t n) {
+    if (n >= 8 && n <= 512 && (n & (n - 1)) == 0) return true;
+    return n == 24 || n == 48 || n == 96 || n == 192;
+}
 
 // exp(-2 pi i m / L) for m < L, from the first octant by symmetry so that the
 // quadrant points are exact.  Long double keeps the rounding to double
@@ -98,7 +102,8 @@ int dd_plan_create(int ndim, const int64_t* xshape, const double* kx, const doub
     DD_CHECK_ARG(ndim == 2 || kz, "dd_plan_create: kz table required in 3D");
     *out = nullptr;
     for (int i = 0; i < ndim; i++)
-        DD_CHECK_SUPPORTED(is_pow2(xshape[i]), "dd_plan_create: axis %d has size %lld; sizes must be powers of two in [8, 512]",
+        DD_CHECK_SUPPORTED(is_supported_len(xshape[i]),
+                           "dd_plan_create: axis %d has size %lld; sizes must be powers of two in [8, 512] or 24, 48, 96, 192",
                            i, (long long)xshape[i]);
     dd_plan* p = (dd_plan*)calloc(1, sizeof(dd_plan));
     DD_CHECK_ARG(p, "dd_plan_create: out of host memory");

@@ -6,8 +6,9 @@
 // for 8- and 16-byte complex entries).  The transform is a mixed-radix
 // Stockham autosort (decimation in time): each pass reads R inputs at stride
 // L/R, twiddles by W_{Ns R}^{r k}, does an in-register radix-R DFT and writes
-// the outputs at ((j-k) R + k) + r Ns.  Radices are 2, 4, 8 and 16; in-register
-// twiddles are exact constants (multiples of pi/8), the inter-pass twiddles
+// the outputs at ((j-k) R + k) + r Ns.  Radices are 2, 3, 4, 8 and 16 (a radix
+// 3 only as the last pass, so that every Ns before it is a power of two); in-register
+// twiddles are exact constants (multiples of pi/8, and sqrt(3)/2), the inter-pass twiddles
 // come from a per-length table W_L^m = exp(-2 pi i m / L) staged in shared
 // memory (conjugated for the inverse transform).
 //
@@ -23,6 +24,7 @@ namespace dd {
 #define DD_C8 0.92387953251128675613
 #define DD_S8 0.38268343236508977173
 #define DD_R2 0.70710678118654752440
+#define DD_S3 0.86602540378443864676
 
 // v * W_R^m (forward) or v * conj(W_R^m) (inverse), m a compile-time constant
 // with R in {8, 16}; trivial multiples are exact.
@@ -109,8 +111,17 @@ __device__ __forceinline__ void dft(C<T>* v) {
             dft4<INV>(a0, a1, a2, a3);
             v[k1] = a0; v[k1 + 4] = a1; v[k1 + 8] = a2; v[k1 + 12] = a3;
         }
+    } else if constexpr (R == 3) {
+        // X1,2 = v0 - (v1 + v2)/2 -/+ i sqrt(3)/2 (v1 - v2) (forward; conjugate for inverse)
+        const C<T> t1 = v[1] + v[2], t2 = v[1] - v[2];
+        const C<T> m1 = mk<T>(v[0].x - t1.x * T(0.5), v[0].y - t1.y * T(0.5));
+        const C<T> r = mul_mi<INV>(t2);
+        const C<T> m2 = mk<T>(r.x * T(DD_S3), r.y * T(DD_S3));
+        v[0] = v[0] + t1;
+        v[1] = m1 + m2;
+        v[2] = m1 - m2;
     } else {
-        static_assert(R == 2 || R == 4 || R == 8 || R == 16, "unsupported radix");
+        static_assert(R == 2 || R == 3 || R == 4 || R == 8 || R == 16, "unsupported radix");
     }
 }
 
@@ -120,6 +131,10 @@ __device__ __forceinline__ void dft(C<T>* v) {
 // pass has (L / R) / TPP butterflies per thread, an integer >= 1.
 template <int L> struct FFTCfg;
 template <> struct FFTCfg<8>    { static constexpr int P = 64, NT = 64,  R1 = 8,  R2 = 1,  R3 = 1; };
+template <> struct FFTCfg<24>   { static constexpr int P = 64, NT = 64,  R1 = 8,  R2 = 3,  R3 = 1; };
+template <> struct FFTCfg<48>   { static constexpr int P = 64, NT = 256, R1 = 4,  R2 = 4,  R3 = 3; };
+template <> struct FFTCfg<96>   { static constexpr int P = 64, NT = 256, R1 = 8,  R2 = 4,  R3 = 3; };
+template <> struct FFTCfg<192>  { static constexpr int P = 32, NT = 256, R1 = 8,  R2 = 8,  R3 = 3; };
 template <> struct FFTCfg<16>   { static constexpr int P = 64, NT = 256, R1 = 4,  R2 = 4,  R3 = 1; };
 template <> struct FFTCfg<32>   { static constexpr int P = 64, NT = 256, R1 = 8,  R2 = 4,  R3 = 1; };
 template <> struct FFTCfg<64>   { static constexpr int P = 32, NT = 256, R1 = 8,  R2 = 8,  R3 = 1; };

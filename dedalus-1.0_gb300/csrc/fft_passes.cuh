@@ -124,7 +124,7 @@ __device__ __forceinline__ C<T> pack_rows(const V* ra, const V* rb, int e, int N
 template <typename T>
 __device__ __forceinline__ void unpack_rows(const C<T>* col, int PS, int k, int N, T s, C<T>& A, C<T>& B) {
     const C<T> z = col[k * PS];
-    const C<T> zn = col[((N - k) & (N - 1)) * PS];
+    const C<T> zn = col[(k == 0 ? 0 : N - k) * PS];
     const T h = T(0.5) * s;
     A = mk<T>((z.x + zn.x) * h, (z.y - zn.y) * h);
     B = mk<T>((z.y + zn.y) * h, (zn.x - z.x) * h);

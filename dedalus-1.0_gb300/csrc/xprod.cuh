@@ -179,6 +179,10 @@ int launch_x_prod_len(const char* name, int L, int nrows, int Kx, const CPtrs& w
     switch (L) {
         DD_LEN_CASE(8, DD_XP(8))
         DD_LEN_CASE(16, DD_XP(16))
+        DD_LEN_CASE(24, DD_XP(24))
+        DD_LEN_CASE(48, DD_XP(48))
+        DD_LEN_CASE(96, DD_XP(96))
+        DD_LEN_CASE(192, DD_XP(192))
         DD_LEN_CASE(32, DD_XP(32))
         DD_LEN_CASE(64, DD_XP(64))
         DD_LEN_CASE(128, DD_XP(128))

@@ -15,7 +15,8 @@
  *      3D x-space float64 [z][y][x],  k-space complex128 [ky][kz][kx], kx < Nx/2+1
  *      2D x-space float64 [y][x],     k-space complex128 [kx][ky]
  *    complex128 is interleaved (re, im) doubles.
- *  - Transform sizes: powers of two, 8 <= N <= 512 per axis.
+ *  - Transform sizes per axis: powers of two 8 .. 512, and 24, 48, 96, 192
+ *    (3 x a power of two; FP64/FP32 arithmetic).
  */
 #ifndef DD_GB300_H
 #define DD_GB300_H
@@ -66,7 +67,7 @@ int dd_timing_report(char* buf, size_t len);
  * order: kx[Nx/2+1], ky[Ny], kz[Nz] (3D) or kx[Nx/2+1], ky[Ny] (2D), on the
  * host.  mx, my, mz give the largest kept |mode index| per axis after
  * dealiasing (representations.py:359-408): kept modes are 0..m and N-m..N-1.
- * Fails with DD_ERR_UNSUPPORTED for non power-of-two sizes.
+ * Fails with DD_ERR_UNSUPPORTED for other sizes.
  */
 int dd_plan_create(int ndim, const int64_t* xshape, const double* kx, const double* ky,
                    const double* kz, int mx, int my, int mz, dd_plan** out);

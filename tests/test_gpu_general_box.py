@@ -161,3 +161,64 @@ def test_3d_lengths_outside_the_supported_range_raise(dd, cuda, shape):
         for i in range(3):
             dg['u'][i]['kspace'] = u[i]
         M.RK4(rg).do_advance(dg, 2e-3)
+
+
+# ------------------------------------------------ 3 x 2^k lengths (radix-3 pass)
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape", [(48, 48, 48), (24, 96, 48), (192, 24, 16)])
+def test_fft_roundtrip_3x2k(dd, cuda, shape):
+    """r2c against numpy's rfftn (the oracle's transform) and c2r back."""
+    import torch
+    from oracle import closure as OC
+    rng = np.random.Generator(np.random.PCG64(50))
+    x = rng.normal(size=shape)
+    plan = dd.engine.get_plan(shape, (2 * np.pi,) * 3)
+    xt = torch.from_numpy(x).cuda()
+    k = torch.empty(tuple(plan.kshape), dtype=torch.complex128, device="cuda")
+    plan.r2c([xt], [k])
+    ref = OC.to_k(x)
+    got = k.cpu().numpy()
+    assert np.max(np.abs(got - ref)) <= 1e-14 * np.max(np.abs(ref))
+    xb = torch.empty_like(xt)
+    plan.c2r([k], [xb])
+    assert np.max(np.abs(xb.cpu().numpy() - OC.to_x(ref, shape))) <= 1e-12 * np.max(np.abs(x))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape", [(48, 48, 48), (24, 96, 48), (16, 192, 32)])
+def test_hydro3d_rk4_3x2k(dd, cuda, shape):
+    u = dd.init_cond.turbulence_3d(shape, seed=51)
+    ro, do, rg, dg = pair(dd, 'IncompressibleHydro', shape, None, {'nu': 5e-3}, {f: u[f[1]] for f in U3})
+    OT.RK4(ro).do_advance(do, 2e-3)
+    dd.mods.RK4(rg).do_advance(dg, 2e-3)
+    assert rel_l2(*states(do, dg, U3)) < 1e-12
+
+
+@pytest.mark.gpu
+def test_mhd_rk4_3x2k(dd, cuda):
+    shape = (48, 48, 48)
+    u = dd.init_cond.turbulence_3d(shape, seed=52, k0=3.0)
+    b = dd.init_cond.turbulence_3d(shape, seed=53, k0=3.0)
+    f = {('u', i): u[i] for i in range(3)}
+    f.update({('B', i): b[i] for i in range(3)})
+    ro, do, rg, dg = pair(dd, 'IncompressibleMHD', shape, None, {'nu': 5e-3, 'eta': 5e-3}, f)
+    names = U3 + [('B', 0), ('B', 1), ('B', 2)]
+    OT.RK4(ro).do_advance(do, 1e-3)
+    dd.mods.RK4(rg).do_advance(dg, 1e-3)
+    assert rel_l2(*states(do, dg, names)) < 1e-12
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape", [(96, 192), (48, 48)])
+def test_2d_rk2mid_3x2k(dd, cuda, shape):
+    T = dd.init_cond.band_limited_noise_2d(shape, seed=54)
+    u = dd.init_cond.turbulence_2d(shape, seed=55, energy_target=1e-2)
+    names = [('u', 0), ('u', 1), ('T', 0)]
+    ro, do, rg, dg = pair(dd, 'BoussinesqHydro', shape, None,
+                          {'nu': 2e-3, 'kappa': 2e-3, 'boussinesq_direction': 'y'},
+                          {('u', 0): u[0], ('u', 1): u[1], ('T', 0): T})
+    to, tg = OT.RK2mid(ro), dd.mods.RK2mid(rg)
+    for _ in range(3):
+        to.do_advance(do, 1e-2)
+        tg.do_advance(dg, 1e-2)
+    assert rel_l2(*states(do, dg, names)) < 1e-12
