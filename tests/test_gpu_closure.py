@@ -305,21 +305,18 @@ def test_les_rk4_step_matches_oracle(dd, cuda, fused):
 @pytest.mark.gpu
 def test_trained_closure_beats_no_model(dd, cuda):
     """The committed network (trained on filtered FP64 256^3 DNS, seeds
-    1000-1049; band and gain chosen on seed 11) against the unclosed 64^3 LES
-    on a seed used for neither (13): after 500 steps (t = 1) its spectrum is
-    closer to the filtered DNS both for k <= kmax/2 and over all resolved k,
-    with the stored band and with the closure term at every mode."""
+    1000-1049; target, band and gain chosen on seed 11) against the unclosed
+    64^3 LES on a seed used for neither (13): after 500 steps (t = 1) its
+    spectrum is closer to the filtered DNS both for k <= kmax/2 and over all
+    resolved k, and it drains energy on average."""
     C = dd.closure
     if not os.path.isfile(C.DEFAULT_WEIGHTS):
         pytest.fail("trained weights missing: %s" % C.DEFAULT_WEIGHTS)
     cl = C.MLPClosure.load()
     assert cl.meta["data"]["n_seeds"] == 50 and cl.meta["data"]["n_snap"] == 20
     assert cl.band == (10.5, 21.0) and cl.gain == 2.0
-    ev = C.evaluate({"closure": cl, "full_band": cl.with_band(0.0, 0.0, 0.5), "no_model": None}, seed=13,
-                    nsteps=500, every=500)
-    n = ev["no_model"]
-    for name in ("closure", "full_band"):
-        c = ev[name]
-        assert c["err_half"][-1] < n["err_half"][-1], (name, c["err_half"], n["err_half"])
-        assert c["err_full"][-1] < n["err_full"][-1], (name, c["err_full"], n["err_full"])
-        assert c["diss_sgs"][-1] > 0.0          # the closure drains energy on average
+    ev = C.evaluate({"closure": cl, "no_model": None}, seed=13, nsteps=500, every=500)
+    c, n = ev["closure"], ev["no_model"]
+    assert c["err_half"][-1] < n["err_half"][-1], (c["err_half"], n["err_half"])
+    assert c["err_full"][-1] < n["err_full"][-1], (c["err_full"], n["err_full"])
+    assert c["diss_sgs"][-1] > 0.0
