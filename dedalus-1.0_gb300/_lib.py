@@ -77,6 +77,14 @@ SIGNATURES = {
     "dd_les_samples": [I64, PP, PP, PP, D, P, P],
     "dd_les_stress": [P, PP, PP, P, I, P, SZ, P],
     "dd_les_band": [P, I, PP, D, D, P],
+    "dd_les_transfer": [P, PP, PP, I, P, P, SZ, P],
+    "dd_shear_workspace_size": [P, I, ctypes.POINTER(SZ)],
+    "dd_shear_r2c": [P, I, PP, PP, P, D, P, D, P, SZ, P],
+    "dd_shear_c2r": [P, I, PP, PP, P, D, P, D, P, SZ, P],
+    "dd_shear_dealias": [P, I, PP, P, D, P],
+    "dd_shear_deriv_y": [P, P, P, P, P],
+    "dd_kspace_real": [I64, P, P, D, I, I, P, P],
+    "dd_xspace_fma": [I64, P, P, D, I, P, P],
     "dd_les_workspace_size": [P, I, ctypes.POINTER(SZ)],
     "dd_les_rhs3d": [P, PP, PP, P, I, I, P, P, SZ, P],
     "dd_les_rk4_step3d": [P, PP, P, PP, PP, P, I, D, I, ctypes.POINTER(I), P, P, SZ, P],
@@ -85,9 +93,12 @@ SIGNATURES = {
 
 class Closure(ctypes.Structure):
     """dd_closure: device pointers of the BF16 weights, FP32 parameters and
-    normalisation vector, the filter width and the closure-term band."""
+    normalisation vector, the filter width, the closure-term band and the
+    optional per-shell weight table (device pointer and length)."""
     _fields_ = [("wbf16", ctypes.c_void_p), ("params", ctypes.c_void_p), ("norm", ctypes.c_void_p),
-                ("delta", ctypes.c_double), ("band_lo", ctypes.c_double), ("band_hi", ctypes.c_double)]
+                ("delta", ctypes.c_double), ("band_lo", ctypes.c_double), ("band_hi", ctypes.c_double),
+                ("shell_w", ctypes.c_void_p), ("n_shell", ctypes.c_int)]
+
 _RESTYPE = {"dd_last_error": ctypes.c_char_p, "dd_launch_count": ctypes.c_longlong}
 
 

@@ -92,6 +92,9 @@ class MLPClosure:
         # band[1], linear between; (0, 0) applies it at every mode
         self.band = (0.0, 0.0)
         self.gain = 1.0                 # applied to the stress fluctuation (out_scale)
+        # per-shell closure-term weights (entry i at |k| = i, linear between);
+        # when set they replace the band
+        self.shell_w = None
         self._ws = None
         self.pack()
 
@@ -101,8 +104,10 @@ class MLPClosure:
 
     def struct(self):
         """dd_closure for the C ABI (keep the returned object alive)."""
+        sw = self.shell_w
         return _lib.Closure(self.wbf16.data_ptr(), self.params.data_ptr(), self.norm.data_ptr(), self.delta,
-                            float(self.band[0]), float(self.band[1]))
+                            float(self.band[0]), float(self.band[1]), None if sw is None else sw.data_ptr(),
+                            0 if sw is None else int(sw.numel()))
 
     def with_band(self, lo, hi, gain=1.0):
         """A view of this network (shared weights) with another closure-term
@@ -115,6 +120,18 @@ class MLPClosure:
             c.norm = self.norm.clone()
             c.norm[40:46] *= float(gain)
         c.gain = float(gain) * self.gain
+        return c
+
+    def with_shells(self, weights):
+        """A view of this network (shared weights) whose closure term is
+        weighted per wavenumber shell: w(|k|) = weights linearly interpolated
+        at |k| (entry i at |k| = i, the last entry beyond the table)."""
+        w = np.asarray(weights, dtype=np.float64).reshape(-1)
+        if w.size < 2:
+            raise ValueError("the shell table needs at least two entries")
+        c = object.__new__(MLPClosure)
+        c.__dict__.update(self.__dict__)
+        c.shell_w = torch.from_numpy(w.copy()).to(self.device)
         return c
 
     def set_norm(self, in_mean, in_scale, out_mean, out_scale):
@@ -175,9 +192,10 @@ class MLPClosure:
         meta = dict(self.meta, **meta)
         norm = self.norm.cpu().numpy().copy()
         norm[40:46] /= np.float32(self.gain)          # stored without the gain
+        extra = {} if self.shell_w is None else {"shell_w": self.shell_w.cpu().numpy()}
         np.savez(path, params=self.params.cpu().numpy(), norm=norm, delta=np.float64(self.delta),
                  band=np.array(self.band, dtype=np.float64), gain=np.float64(self.gain),
-                 meta=np.array(json.dumps(meta)))
+                 meta=np.array(json.dumps(meta)), **extra)
 
     @classmethod
     def load(cls, path=DEFAULT_WEIGHTS, device=None):
@@ -191,6 +209,8 @@ class MLPClosure:
         if "gain" in z.files and float(z["gain"]) != 1.0:
             c.gain = float(z["gain"])
             c.norm[40:46] *= c.gain
+        if "shell_w" in z.files:
+            c.shell_w = torch.from_numpy(z["shell_w"].astype(np.float64)).to(c.device)
         c.pack()
         return c
 
@@ -270,6 +290,35 @@ class FilteredSampler:
             zp, _l = _ptrs(zero)
             _lib.call("dd_les_samples", self.npts, gp, tp, zp, self.delta, dptr(raw_band), st)
 
+    def transfer(self, u_k, closures, nbins):
+        """Per-shell subgrid energy transfer (dd_les_transfer) at the filtered
+        DNS state u_k: the exact one, from tau = filt(u u) - filt(ub ub), and
+        that of the stress each closure predicts from the filtered velocity
+        (its band and shell weights are not applied).  Returns (exact [nbins],
+        {name: [nbins]}) as host float64 arrays."""
+        if getattr(self, '_raw1', None) is None:
+            self._raw1 = torch.empty((self.npts, 16), dtype=torch.float32, device=self.les.device)
+            self._tau = [torch.empty(self.les_shape, dtype=torch.float64, device=self.les.device) for _ in range(6)]
+        st = current_stream()
+        self.samples(u_k, self._raw1)
+        for c in range(6):
+            torch.sub(self._lx[3 + c], self._rp[c], out=self._tau[c])
+        up, _a = _ptrs(self._lk[:3])
+        tp, _b = _ptrs(self._tau)
+        out = torch.empty(nbins, dtype=torch.float64, device=self.les.device)
+        _lib.call("dd_les_transfer", self.les.handle, up, tp, int(nbins), dptr(out), dptr(self._ws),
+                  self._ws.numel(), st)
+        exact = out.cpu().numpy().copy()
+        models = {}
+        for name, cl in closures.items():
+            s = cl.struct()
+            _lib.call("dd_les_stress", self.les.handle, up, tp, ctypes.byref(s), _lib.DD_FP64, dptr(self._ws),
+                      self._ws.numel(), st)
+            _lib.call("dd_les_transfer", self.les.handle, up, tp, int(nbins), dptr(out), dptr(self._ws),
+                      self._ws.numel(), st)
+            models[name] = out.cpu().numpy().copy()
+        return exact, models
+
 
 def generate_dataset(n_seeds=50, n_snap=20, stride=50, dns_n=256, les_n=64, nu=5e-3, dt=2e-3, seed0=1000,
                      log=None, band=None):
@@ -321,6 +370,53 @@ def generate_dataset(n_seeds=50, n_snap=20, stride=50, dns_n=256, les_n=64, nu=5
         info["band"] = list(band)
         info["raw_band"] = raw_band
     return raw, np.array(seeds), info
+
+
+def shell_count(les_n):
+    """Bins of round(|k|) over the kept modes of an les_n^3 grid (2 pi box)."""
+    m = int(np.ceil(les_n / 3.0)) - 1
+    return int(np.floor(np.sqrt(3.0) * m + 0.5)) + 1
+
+
+def calibrate_shells(closure, n_seeds=4, n_snap=20, stride=50, dns_n=256, les_n=64, nu=5e-3, dt=2e-3, seed0=1000,
+                     wmax=8.0, log=None):
+    """Per-shell closure-term weights that make the network's mean subgrid
+    energy transfer equal the exact one over filtered DNS snapshots (the FP64
+    DNS of generate_dataset, seeds seed0 .. seed0 + n_seeds - 1):
+    w(k) = sum T_exact(k) / sum T_model(k) over the snapshots, 0 where the
+    model transfers nothing, clipped to [-wmax, wmax]; w(0) = w(1) (the mean
+    mode carries no force).  Returns (w, {"exact": sums, "model": sums})."""
+    from . import mods
+    from .init_cond import turbulence_3d
+    shape = (dns_n,) * 3
+    sampler = FilteredSampler(shape, (les_n,) * 3)
+    nb = shell_count(les_n)
+    RHS = mods.IncompressibleHydro(shape, mods.FourierRepresentation)
+    RHS.parameters['nu'] = nu
+    data = RHS.create_fields(0.)
+    ti = mods.RK4(RHS)
+    se = np.zeros(nb)
+    sm = np.zeros(nb)
+    t0 = time.time()
+    for s in range(n_seeds):
+        u0 = turbulence_3d(shape, seed=seed0 + s)
+        for i in range(3):
+            data['u'][i]['kspace'] = u0[i]
+        data.set_time(0.)
+        for j in range(n_snap):
+            for _ in range(stride):
+                ti.do_advance(data, dt)
+            e, m = sampler.transfer([data['u'][i].kdata for i in range(3)], {"m": closure}, nb)
+            se += e
+            sm += m["m"]
+        if log:
+            log("calibration seed %d done, %.1f s" % (seed0 + s, time.time() - t0))
+    tiny = 1e-6 * np.max(np.abs(sm))
+    w = np.where(np.abs(sm) > tiny, se / np.where(np.abs(sm) > tiny, sm, 1.0), 0.0)
+    w = np.clip(w, -wmax, wmax)
+    w[0] = w[1]
+    return w, {"exact": se.tolist(), "model": sm.tolist(), "seconds": time.time() - t0,
+               "snapshots": n_seeds * n_snap, "seed0": seed0}
 
 
 def fit_norm(raw, chunk=1 << 24):

@@ -143,11 +143,25 @@ __global__ void __launch_bounds__(32 * LES_WARPS) k_les_mlp(CPtrs gx, Ptrs tau, 
     }
 }
 
+// Closure-term weight at |k| = kk: the shell table sw[0..nsw) linearly
+// interpolated (entry i at |k| = i, the last entry beyond the table) when sw
+// is given, else the band ramp: 0 at |k| <= lo, 1 at |k| >= hi, linear between
+// (1 everywhere when hi <= 0).
+__device__ __forceinline__ double les_weight(double kk, const double* sw, int nsw, double lo, double hi) {
+    if (sw) {
+        const int i = (int)kk;
+        if (i >= nsw - 1) return sw[nsw - 1];
+        const double f = kk - (double)i;
+        return sw[i] + f * (sw[i + 1] - sw[i]);
+    }
+    if (hi > 0.) return kk <= lo ? 0. : (kk >= hi ? 1. : (kk - lo) / (hi - lo));
+    return 1.;
+}
+
 // nc_i -= w(|k|) i k_j tau_ij on the kept modes; tau spectra in full layout,
-// order xx, yy, zz, xy, xz, yz; nc compact complex128.  w ramps linearly from
-// 0 at |k| = lo to 1 at |k| = hi (w = 1 everywhere when hi <= 0).
+// order xx, yy, zz, xy, xz, yz; nc compact complex128; w from les_weight.
 __global__ void k_les_add(Geo3 g, const double* kx, const double* ky, const double* kz, CPtrs tk, Ptrs nc,
-                          double lo, double hi) {
+                          double lo, double hi, const double* sw, int nsw) {
     const int64_t n = (int64_t)g.Ky * g.Kz * g.Kx;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         int ky_i, kz_i, ix;
@@ -155,10 +169,7 @@ __global__ void k_les_add(Geo3 g, const double* kx, const double* ky, const doub
         les_kept(g, i, ky_i, kz_i, ix, o);
         const double k0 = kx[ix], k1 = ky[ky_i], k2 = kz[kz_i];
         double w = 1.;
-        if (hi > 0.) {
-            const double kk = sqrt(k0 * k0 + k1 * k1 + k2 * k2);
-            w = kk <= lo ? 0. : (kk >= hi ? 1. : (kk - lo) / (hi - lo));
-        }
+        if (sw || hi > 0.) w = les_weight(sqrt(k0 * k0 + k1 * k1 + k2 * k2), sw, nsw, lo, hi);
         if (w == 0.) continue;
         double2 t[6];
 #pragma unroll
@@ -242,6 +253,56 @@ __global__ void k_les_samples(int64_t npts, CPtrs gx, CPtrs f, CPtrs fr, double 
     }
 }
 
+// Subgrid transfer per kept mode: c[i] = m Re(conj(u_a) (-i k_j tau_ij)_a), m = 2
+// for 0 < kx < Nx/2 (the mode and its conjugate), else 1; bin[i] =
+// round(|k|) (as a double), -1 beyond the last bin.
+__global__ void k_les_transfer_modes(Geo3 g, const double* kx, const double* ky, const double* kz, CPtrs u, CPtrs tk,
+                                     int nbins, double* c, double* bin) {
+    const int64_t n = (int64_t)g.Ky * g.Kz * g.Kx;
+    const int rows[3][3] = {{0, 3, 4}, {3, 1, 5}, {4, 5, 2}};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        int ky_i, kz_i, ix;
+        int64_t o;
+        les_kept(g, i, ky_i, kz_i, ix, o);
+        const double kv[3] = {kx[ix], ky[ky_i], kz[kz_i]};
+        double t = 0.;
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            double fx = 0., fy = 0.;          // F_a = -i k_j tau_aj
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                const double2 tv = ((const double2*)tk.p[rows[a][j]])[o];
+                fx += kv[j] * tv.y;
+                fy -= kv[j] * tv.x;
+            }
+            const double2 ua = ((const double2*)u.p[a])[o];
+            t += ua.x * fx + ua.y * fy;
+        }
+        const double m = (ix > 0 && 2 * ix < g.Nx) ? 2. : 1.;
+        const double kk = sqrt(kv[0] * kv[0] + kv[1] * kv[1] + kv[2] * kv[2]);
+        const double b = floor(kk + 0.5);
+        c[i] = m * t;
+        bin[i] = b < (double)nbins ? b : -1.;
+    }
+}
+
+// out[b] = sum of c[i] over bin[i] == b, one block per bin, fixed order.
+__global__ void __launch_bounds__(256) k_les_transfer_bins(int64_t n, const double* c, const double* bin,
+                                                           double* out) {
+    __shared__ double red[256];
+    const double b = (double)blockIdx.x;
+    double s = 0.;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x)
+        if (bin[i] == b) s += c[i];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int h = 128; h > 0; h >>= 1) {
+        if (threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[blockIdx.x] = red[0];
+}
+
 // ------------------------------------------------------------- drivers
 struct LesWork {
     double2* gk[9];   // gradient spectra, later the stress spectra (0..5)
@@ -323,7 +384,8 @@ int les_closure_add(const dd_plan* p, const LesHook& h, int prec, bool compact, 
     for (int a = 0; a < 3; a++) n.p[a] = nc[a];
     DD_KT("les_add", st,
           k_les_add<<<les_grid((int64_t)g.Ky * g.Kz * g.Kx), 256, 0, st>>>(g, p->kx, p->ky, p->kz, tk, n,
-                                                                          h.cl->band_lo, h.cl->band_hi));
+                                                                          h.cl->band_lo, h.cl->band_hi,
+                                                                          h.cl->shell_w, h.cl->n_shell));
     DD_LAUNCH_CHECK();
     return DD_OK;
 }
@@ -434,6 +496,34 @@ int dd_les_stress(const dd_plan* p, const void* const* u, double* const* tau, co
     const LesWork w = les_carve(p, work);
     DD_TRY(les_grads(p, precision, false, u, w, st));
     return les_mlp(p, cl, w, tau, st);
+}
+
+int dd_les_transfer(const dd_plan* p, const void* const* u, const double* const* tau, int nbins, double* out,
+                    void* work, size_t work_bytes, void* stream) {
+    DD_TRY(les_check_plan(p));
+    DD_CHECK_ARG(u && tau && out && work, "dd_les_transfer: null pointer");
+    DD_CHECK_ARG(nbins >= 1 && nbins <= 4096, "nbins must be in [1, 4096]");
+    DD_CHECK_ARG(work_bytes >= les_work_bytes(p), "workspace too small: %zu < %zu", work_bytes, les_work_bytes(p));
+    for (int a = 0; a < 3; a++) DD_CHECK_ARG(u[a], "null velocity %d", a);
+    for (int c = 0; c < 6; c++) DD_CHECK_ARG(tau[c], "null stress %d", c);
+    cudaStream_t st = (cudaStream_t)stream;
+    const LesWork w = les_carve(p, work);
+    const Geo3& g = p->g3;
+    const double* xin[6];
+    void* kout[6];
+    for (int c = 0; c < 6; c++) { xin[c] = tau[c]; kout[c] = w.gk[c]; }
+    DD_TRY(fft_r2c<double>(p, 6, xin, kout, w.fw, w.fwb, st, false));
+    // per-mode terms and bins in two grid-point buffers (kept count <= grid points)
+    const int64_t n = (int64_t)g.Ky * g.Kz * g.Kx;
+    CPtrs uc{}, tk{};
+    for (int a = 0; a < 3; a++) uc.p[a] = u[a];
+    for (int c = 0; c < 6; c++) tk.p[c] = w.gk[c];
+    DD_KT("les_transfer_modes", st,
+          k_les_transfer_modes<<<les_grid(n), 256, 0, st>>>(g, p->kx, p->ky, p->kz, uc, tk, nbins, w.gx[6], w.gx[7]));
+    DD_LAUNCH_CHECK();
+    DD_KT("les_transfer_bins", st, k_les_transfer_bins<<<nbins, 256, 0, st>>>(n, w.gx[6], w.gx[7], out));
+    DD_LAUNCH_CHECK();
+    return DD_OK;
 }
 
 }  // extern "C"

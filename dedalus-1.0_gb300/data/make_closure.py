@@ -13,6 +13,24 @@ chooses among the candidate closures, ``--eval-seed`` (used for neither)
 measures the chosen one.  With ``--band-target lo hi`` a second network is
 trained on the stress restricted to that spectral band (the part of tau the
 banded closure term uses) and competes in the selection.
+
+The stored closure (les_closure_256to64.npz) was made by the command above.
+
+``--base FILE`` skips the dataset and the training and starts from a stored
+network (les_closure_256to64_base.npz is the all-mode network of a run of
+the command above without --band-target).  ``--calibrate-seeds N`` fits per-shell closure-term weights on
+training seeds seed0 .. seed0 + N - 1: the ratio of the exact to the
+network's subgrid energy transfer per wavenumber shell, summed over the
+filtered DNS snapshots (closure.calibrate_shells); the calibrated closure and
+its variants then compete in the selection:
+
+    python dedalus-1.0_gb300/data/make_closure.py \
+        --base dedalus-1.0_gb300/data/les_closure_256to64_base.npz \
+        --calibrate-seeds 4 --select-seed 11 --eval-seeds 7 13 17 \
+        --eval-steps 1000 --out calibrated.npz --report calibrated.json
+
+Its outcome is les_closure_calibration_report.json: the calibrated weights
+lost to the stored closure on the selection seed.
 """
 import argparse
 import json
@@ -47,6 +65,9 @@ def main(argv=None):
     ap.add_argument("--eval-steps", type=int, default=0)
     ap.add_argument("--eval-every", type=int, default=100)
     ap.add_argument("--eval-seed", type=int, default=7)
+    ap.add_argument("--eval-seeds", type=int, nargs="+", default=None, help="evaluate on each (overrides --eval-seed)")
+    ap.add_argument("--base", default=None, help="start from this stored network (no dataset, no training)")
+    ap.add_argument("--calibrate-seeds", type=int, default=0)
     ap.add_argument("--out", default=os.path.join(HERE, "les_closure_256to64.npz"))
     ap.add_argument("--report", default=None)
     ap.add_argument("--dump-samples", type=int, default=0, help="save this many random raw samples")
@@ -71,6 +92,11 @@ def main(argv=None):
                 json.dump(rep, f)
 
     band = tuple(a.band_target) if a.band_target else None
+    models = {}
+    if a.base:
+        models["stress"] = C.MLPClosure.load(a.base)
+        rep["base"] = {"file": os.path.basename(a.base), "meta": models["stress"].meta}
+        return finish(a, C, rep, models, band, log, write_report)
     raw, seeds, info = C.generate_dataset(a.seeds, a.snaps, a.stride, a.dns, a.les, a.nu, a.dt, a.seed0, log=log,
                                           band=band)
     raw_band = info.pop("raw_band", None)
@@ -105,7 +131,6 @@ def main(argv=None):
         torch.cuda.empty_cache()
         return cl, tinfo
 
-    models = {}
     models["stress"], rep["train"] = fit(raw, "stress")
     del raw
     if raw_band is not None:
@@ -113,8 +138,23 @@ def main(argv=None):
         del raw_band
     torch.cuda.empty_cache()
     write_report()
+    finish(a, C, rep, models, band, log, write_report)
 
+
+def finish(a, C, rep, models, band, log, write_report):
+    """Calibration, selection, storage and evaluation of the closure."""
+    import numpy as np
     chosen = models["stress"]
+    shells = None
+    if a.calibrate_seeds:
+        shells, cinfo = C.calibrate_shells(models["stress"], n_seeds=a.calibrate_seeds, n_snap=a.snaps,
+                                           stride=a.stride, dns_n=a.dns, les_n=a.les, nu=a.nu, dt=a.dt,
+                                           seed0=a.seed0, log=log)
+        cinfo["weights"] = shells.tolist()
+        rep["calibration"] = cinfo
+        log("shell weights %s" % np.round(shells, 3).tolist())
+        chosen = models["stress"].with_shells(shells)
+        write_report()
     if a.select_seed is not None:
         cands = {"stress_all_modes": models["stress"]}
         for lo, hi, gn in [(10.5, 21.0, 1.0), (10.5, 21.0, 2.0), (10.5, 15.75, 1.5)]:
@@ -122,6 +162,11 @@ def main(argv=None):
         if "band_stress" in models:
             for gn in (1.0, 1.5, 2.0, 3.0):
                 cands["band_stress_x%g" % gn] = models["band_stress"].with_band(band[0], band[1], gn)
+        if shells is not None:
+            cands["stress_shells"] = models["stress"].with_shells(shells)
+            cands["stress_shells_no_backscatter"] = models["stress"].with_shells(np.maximum(shells, 0.0))
+            for f in (0.8, 1.25):
+                cands["stress_shells_x%g" % f] = models["stress"].with_shells(f * shells)
         cands["no_model"] = None
         ev = C.evaluate(cands, seed=a.select_seed, dns_n=a.dns, les_n=a.les, nu=a.nu, dt=a.dt,
                         nsteps=a.eval_steps or 1000, every=a.eval_every, log=log)
@@ -129,22 +174,28 @@ def main(argv=None):
         rep["selection"] = {"seed": a.select_seed, "max_err_k_le_kmax_half": score}
         best = min((n for n in score if n != "no_model"), key=lambda n: score[n])
         chosen = cands[best]
-        rep["selection"]["chosen"] = {"name": best, "band": list(chosen.band), "gain": chosen.gain}
+        rep["selection"]["chosen"] = {"name": best, "band": list(chosen.band), "gain": chosen.gain,
+                                      "shells": None if chosen.shell_w is None else chosen.shell_w.cpu().tolist()}
         log("selected %s (%.4f) on seed %d" % (best, score[best], a.select_seed))
         write_report()
 
     chosen.meta["selection"] = rep.get("selection")
+    if "calibration" in rep:
+        chosen.meta["calibration"] = {k: v for k, v in rep["calibration"].items() if k in ("snapshots", "seed0")}
     chosen.save(a.out)
     log("saved %s" % a.out)
     if a.eval_steps:
         final = {"chosen": chosen, "stress_all_modes": models["stress"], "no_model": None}
-        ev = C.evaluate(final, seed=a.eval_seed, dns_n=a.dns, les_n=a.les, nu=a.nu, dt=a.dt, nsteps=a.eval_steps,
-                        every=a.eval_every, log=log)
-        rep["eval"] = ev
-        for name in ev["models"]:
-            r = ev[name]
-            log("%s: max E(k) err k<=kmax/2 %.4f, k<=kmax %.4f, final diss %.5f + sgs %.5f (DNS %.5f)" % (
-                name, max(r["err_half"]), max(r["err_full"]), r["diss"][-1], r["diss_sgs"][-1], ev["dns_diss"][-1]))
+        for seed in (a.eval_seeds or [a.eval_seed]):
+            ev = C.evaluate(final, seed=seed, dns_n=a.dns, les_n=a.les, nu=a.nu, dt=a.dt, nsteps=a.eval_steps,
+                            every=a.eval_every, log=log)
+            rep["eval" if seed == (a.eval_seeds or [a.eval_seed])[0] else "eval_%d" % seed] = ev
+            for name in ev["models"]:
+                r = ev[name]
+                log("seed %d %s: max E(k) err k<=kmax/2 %.4f, k<=kmax %.4f, final diss %.5f + sgs %.5f (DNS %.5f)" % (
+                    seed, name, max(r["err_half"]), max(r["err_full"]), r["diss"][-1], r["diss_sgs"][-1],
+                    ev["dns_diss"][-1]))
+            write_report()
     write_report()
 
 

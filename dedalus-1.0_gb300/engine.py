@@ -100,6 +100,33 @@ class Plan:
     def dealias(self, k):
         _lib.call("dd_dealias", self.handle, dptr(k), current_stream())
 
+    # ------------------------------------------------ shearing-box transforms
+    def _shear_ws(self, nfield):
+        n = ctypes.c_size_t()
+        _lib.call("dd_shear_workspace_size", self.handle, nfield, ctypes.byref(n))
+        return self.workspace(n.value, tag='shear')
+
+    def shear_r2c(self, xs, ks, kys, cut, pr, t):
+        """Shearing-box forward transforms at time t (kys: sheared k_y table,
+        pr: phase-rate table, both device float64)."""
+        ws = self._shear_ws(len(xs))
+        xp, _a = _lib.ptr_array([x.data_ptr() for x in xs])
+        kp, _b = _lib.ptr_array([k.data_ptr() for k in ks])
+        _lib.call("dd_shear_r2c", self.handle, len(xs), xp, kp, dptr(kys), float(cut), dptr(pr), float(t),
+                  dptr(ws), ws.numel(), current_stream())
+
+    def shear_c2r(self, ks, xs, kys, cut, pr, t):
+        """Shearing-box backward transforms at time t."""
+        ws = self._shear_ws(len(ks))
+        kp, _a = _lib.ptr_array([k.data_ptr() for k in ks])
+        xp, _b = _lib.ptr_array([x.data_ptr() for x in xs])
+        _lib.call("dd_shear_c2r", self.handle, len(ks), kp, xp, dptr(kys), float(cut), dptr(pr), float(t),
+                  dptr(ws), ws.numel(), current_stream())
+
+    def shear_dealias(self, ks, kys, cut):
+        kp, _a = _lib.ptr_array([k.data_ptr() for k in ks])
+        _lib.call("dd_shear_dealias", self.handle, len(ks), kp, dptr(kys), float(cut), current_stream())
+
 
 _PLANS = {}
 

@@ -140,7 +140,12 @@ class StateData:
         return self.__class__(self.time, self.shape, self.length, self._field_classes, params=self.parameters)
 
     def set_time(self, time):
+        # state_data.py:117-121: shearing-box components follow the time
         self.time = time
+        for name, field in self.fields.items():
+            if not field.representation._static_k:
+                for i, c in field:
+                    c._update_k()
 
     def add_field(self, name, fieldtype):
         if name in self.fields:

@@ -9,7 +9,8 @@ run script of the hot path uses:
         ti.advance(data, dt)
 """
 from .config import decfg
-from .representations import FourierRepresentation, GpuFourierRepresentation
+from .representations import (FourierRepresentation, GpuFourierRepresentation, FourierShearRepresentation,
+                              GpuFourierShearRepresentation)
 from .physics import Physics, IncompressibleHydro, BoussinesqHydro, IncompressibleMHD, LESHydro
 from .time_step import RK2mid, RK2trap, RK4
 from .fields import StateData, create_field_classes
@@ -17,6 +18,7 @@ from .kgrid import swap_indices
 from . import init_cond
 from .restart import restart
 
-__all__ = ["decfg", "FourierRepresentation", "GpuFourierRepresentation", "Physics", "IncompressibleHydro",
+__all__ = ["decfg", "FourierRepresentation", "GpuFourierRepresentation", "FourierShearRepresentation",
+           "GpuFourierShearRepresentation", "Physics", "IncompressibleHydro",
            "BoussinesqHydro", "IncompressibleMHD", "LESHydro", "RK2mid", "RK2trap", "RK4", "StateData",
            "create_field_classes", "swap_indices", "init_cond", "restart"]

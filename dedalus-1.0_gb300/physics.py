@@ -6,8 +6,9 @@ Same constructor ``Cls(shape, representation, length=None)``, the same
 ``RHS(data, deriv)`` (fills ``deriv[f][c]['kspace']`` and sets each
 component's ``integrating_factor`` on the first call, physics.py:504-522),
 ``compute_dt`` and the forcing setters.  The right-hand sides are computed by
-fused CUDA kernels (one C-ABI call per RHS).  The branches the fused kernels
-do not implement (shear, rotation, tracer, forcing functions) raise
+fused CUDA kernels (one C-ABI call per RHS); the shearing box, rotation, 3D
+Boussinesq and 2D MHD run the reference's operator sequence on CUDA kernels
+(generic.py).  The passive tracer and forcing functions raise
 NotImplementedError instead of running anywhere else.
 """
 import ctypes
@@ -19,6 +20,7 @@ from . import _lib
 from .config import decfg, precision_code
 from .engine import current_stream, dptr
 from .fields import create_field_classes, StateData
+from .generic import ReferenceOrderRHS
 
 
 def _ptrs(tensors):
@@ -109,7 +111,7 @@ class Physics:
         return t
 
 
-class IncompressibleHydro(Physics):
+class IncompressibleHydro(ReferenceOrderRHS, Physics):
     """physics.py:419-610."""
 
     def __init__(self, *args, **kwargs):
@@ -128,17 +130,30 @@ class IncompressibleHydro(Physics):
         self._first_rhs = True
 
     def _finalize(self):
+        # physics.py:484-502
         Physics._finalize(self)
-        if self.parameters['shear_rate'] != 0.:
-            raise NotImplementedError("shear (FourierShearRepresentation) is not in the CUDA path")
-        if self.parameters['Omega'] is not None:
-            raise NotImplementedError("rotation is not in the CUDA path")
         if self._tracer:
             raise NotImplementedError("the passive tracer is not in the CUDA path")
         if self.forcing_functions:
             raise NotImplementedError("forcing functions are not in the CUDA path")
-        self._shear = False
-        self._rotation = False
+        if self.parameters['shear_rate'] == 0.:
+            self._shear = False
+        else:
+            self._shear = True
+            if self._representation._static_k:
+                raise ValueError("A shearing representation must be used if shear_rate is nonzero.")
+        self._rotation = self.parameters['Omega'] is not None
+
+    def _generic(self):
+        """True when this RHS runs the reference-ordered operator sequence
+        (generic.py) instead of a fused kernel: shear, rotation, a shearing
+        representation, 3D Boussinesq, 2D MHD."""
+        if not self._is_finalized:
+            self._finalize()
+        return self._shear or self._rotation or not self._representation._static_k or self._generic_only()
+
+    def _generic_only(self):
+        return False
 
     def _diffusivities(self):
         """(field name, coefficient) pairs whose IF is coeff * k2**vo."""
@@ -188,7 +203,10 @@ class IncompressibleHydro(Physics):
         return ['u']
 
     def RHS(self, data, deriv):
-        """RHS(u) = P[-(u.grad)u] (physics.py:527-599), fused on the GPU."""
+        """RHS(u) = P[-(u.grad)u] (physics.py:527-599), fused on the GPU (the
+        shear / rotation branches in the reference's operator order)."""
+        if self._generic():
+            return self._generic_hydro(data, deriv, project=True)
         self._begin_rhs(data, deriv)
         plan = self.plan(data)
         if self.ndim != 3:
@@ -240,8 +258,8 @@ class IncompressibleHydro(Physics):
         returns False when this physics/grid has no fused step."""
         if self.ndim != 3 or not self._fused3d:
             return False
-        if not self._is_finalized:
-            self._finalize()
+        if self._generic():
+            return False
         plan, prec, vo, cf, ik2, th, tf, sp, keep = self._rk4_args(data, dt)
         n = ctypes.c_size_t()
         _lib.call("dd_rhs3d_workspace_size", plan.handle, self._phys3d, prec, ctypes.byref(n))
@@ -284,8 +302,8 @@ class IncompressibleHydro(Physics):
         hydro / Boussinesq; returns False when there is no fused step."""
         if self.ndim != 2 or type(self) not in (IncompressibleHydro, BoussinesqHydro):
             return False
-        if not self._is_finalized:
-            self._finalize()
+        if self._generic():
+            return False
         names = self._state_names()
         for f, c in names:
             data[f][c].require_space('kspace')
@@ -359,11 +377,15 @@ class BoussinesqHydro(IncompressibleHydro):
         return [float(self.parameters['g']), float(self.parameters['alpha_t']), float(self.parameters['beta']),
                 float(self._direction_index())]
 
+    def _generic_only(self):
+        return self.ndim == 3
+
     def RHS(self, data, deriv):
-        """physics.py:664-712, fused on the GPU (2D)."""
-        if self.ndim != 2:
-            raise NotImplementedError("3D Boussinesq is not in the CUDA path")
+        """physics.py:664-712, fused on the GPU (2D; 3D and the shear /
+        rotation branches in the reference's operator order)."""
         self._direction_index()
+        if self._generic():
+            return self._generic_boussinesq(data, deriv)
         self._begin_rhs(data, deriv)
         self._rhs2d(data, deriv, self.plan(data))
 
@@ -398,10 +420,14 @@ class IncompressibleMHD(IncompressibleHydro):
     def _groups3d(self):
         return ['u', 'B']
 
+    def _generic_only(self):
+        return self.ndim == 2
+
     def RHS(self, data, deriv):
-        """physics.py:770-819, fused on the GPU (3D)."""
-        if self.ndim != 3:
-            raise NotImplementedError("2D MHD is not in the CUDA path")
+        """physics.py:770-819, fused on the GPU (3D; 2D and the shear /
+        rotation branches in the reference's operator order)."""
+        if self._generic():
+            return self._generic_mhd(data, deriv)
         self._begin_rhs(data, deriv)
         self._rhs3d(data, deriv, self.plan(data))
 
@@ -438,6 +464,11 @@ class LESHydro(IncompressibleHydro):
         if self.precision is None:
             return IncompressibleHydro._precision(self)
         return self._PREC[self.precision]
+
+    def _finalize(self):
+        IncompressibleHydro._finalize(self)
+        if self._shear or self._rotation or not self._representation._static_k:
+            raise NotImplementedError("the LES closure runs without shear or rotation")
 
     def _les_ws(self, plan, prec):
         n = ctypes.c_size_t()

@@ -15,6 +15,7 @@ implements; ``numpy`` and ``fftw`` raise NotImplementedError like an unknown
 method does in the reference, representations.py:309-310).
 """
 import numpy as np
+import numpy.fft as npfft
 import torch
 
 from . import _lib
@@ -237,4 +238,74 @@ class FourierRepresentation(Representation):
         return self.length / self.global_shape['xspace']
 
 
+class FourierShearRepresentation(FourierRepresentation):
+    """Shearing-box component (representations.py:558-740): k['y'] is a
+    full-shape array that follows the shear, k_y(t) = k_y(0) - S k_x t
+    wrapped into (-kny, kny], and the transforms multiply the x-transformed
+    rows by exp(+-i S k_x y t) between the x and the y/z transforms.  The time
+    is that of the component's StateData.  FP64 transforms, '2/3' rules only."""
+
+    _static_k = False
+
+    def __init__(self, sd, shape, length):
+        FourierRepresentation.__init__(self, sd, shape, length)
+        if self.dealiasing not in ('2/3', '2/3 cython'):
+            raise NotImplementedError("the shearing box supports the 2/3 dealiasing rules only")
+        if decfg.get('FFT', 'precision', fallback='fp64') != 'fp64':
+            raise NotImplementedError("the shearing-box transforms run in FP64")
+        # representations.py:596-617
+        self._ky = self.k_host['y'].copy()
+        self.k_host['y'] = self.k_host['y'] * np.ones_like(self.k_host['x'])
+        ksize = self.global_shape['kspace'][self.ktrans['x']]
+        xsize = self.global_shape['xspace'][self.xtrans['x']]
+        xkx = npfft.fftfreq(xsize)[:ksize] * 2. * self.kny[self.ktrans['x']]
+        if xsize % 2 == 0:
+            xkx[-1] *= -1.
+        xkx = xkx.reshape((self.ndim - 1) * (1,) + (ksize,))
+        y = self.xspace_grid(open=True)[self.xtrans['y']]
+        self._phase_rate = self.sd.parameters['shear_rate'] * xkx * y
+        self._wave_rate = self.sd.parameters['shear_rate'] * self.k_host['x']
+        ny = int(self.global_shape['xspace'][self.xtrans['y']])
+        self._pr = torch.from_numpy(np.array(self._phase_rate, dtype=np.float64).reshape(ny, ksize)).to(self.device)
+        self._kny_y = float(self.kny[3 - self.ndim])
+        self._cut = 2. / 3. * self._kny_y
+        self._update_k()
+
+    def _update_k(self):
+        """representations.py:627-643: shift, wrap, upload, dealias."""
+        ky = self.k_host['y']
+        np.subtract(self._ky, self._wave_rate * self.sd.time, ky)
+        kny_y = self._kny_y
+        if ky.min() <= -kny_y:
+            ky[ky <= -kny_y] += 2 * kny_y
+        if ky.max() > kny_y:
+            ky[ky > kny_y] -= 2 * kny_y
+        self._kys = torch.from_numpy(np.ascontiguousarray(ky.reshape(-1))).to(self.device)
+        self.k['y'] = self._kys.view(ky.shape)
+        self.dealias()
+
+    def fwd_cuda(self):
+        self.plan.shear_r2c([self.xdata], [self.kdata], self._kys, self._cut, self._pr, self.sd.time)
+
+    def rev_cuda(self):
+        self.plan.shear_c2r([self.kdata], [self.xdata], self._kys, self._cut, self._pr, self.sd.time)
+
+    def dealias(self):
+        """2/3 rule with the sheared k_y (dealias_cy_{2d,3d}.pyx, full-shape ky branch)."""
+        self.require_space('kspace')
+        self.plan.shear_dealias([self.kdata], self._kys, self._cut)
+
+    dealias_23 = dealias
+    dealias_23_cython = dealias
+
+    def deriv(self, dim):
+        if dim != 'y':
+            return FourierRepresentation.deriv(self, dim)
+        self.require_space('kspace')
+        _lib.call("dd_shear_deriv_y", self.plan.handle, dptr(self._kys), dptr(self.kdata), dptr(self.deriv_data),
+                  current_stream())
+        return self.deriv_data
+
+
 GpuFourierRepresentation = FourierRepresentation
+GpuFourierShearRepresentation = FourierShearRepresentation

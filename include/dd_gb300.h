@@ -254,6 +254,9 @@ typedef struct dd_closure {
     double delta;          /* filter width fed to input 9 */
     double band_lo;        /* closure-term weight w(|k|): 0 for |k| <= band_lo, */
     double band_hi;        /* 1 for |k| >= band_hi, linear between; band_hi <= 0: w = 1 */
+    const double* shell_w; /* device table; when not NULL it replaces the band: w(|k|) is */
+    int n_shell;           /* shell_w linearly interpolated at |k| (entry i at |k| = i), */
+                           /* shell_w[n_shell - 1] beyond the table */
 } dd_closure;
 
 int dd_mlp_sizes(int* nparam, int* nbf16, int* nnorm, int* in_dim, int* out_dim);
@@ -301,7 +304,15 @@ int dd_les_band(const dd_plan* plan, int nfield, void* const* k, double lo, doub
 /* Grid-point subgrid stress predicted by the closure for velocity u. */
 int dd_les_stress(const dd_plan* plan, const void* const* u, double* const* tau, const dd_closure* cl,
                   int precision, void* work, size_t work_bytes, void* stream);
-/* Workspace of dd_les_gradients, dd_les_stress, dd_les_rhs3d and dd_les_rk4_step3d. */
+/* Subgrid energy transfer per wavenumber shell: out[b] = sum over the modes
+ * with round(|k|) = b of Re(conj(u_a) (-i k_j tau_ij)^_a), counted over the
+ * full spectrum (kx > 0 columns twice), for the velocity spectra u (3 full-layout
+ * k arrays) and the grid-point stresses tau (6 FP64 fields, order xx, yy, zz,
+ * xy, xz, yz); modes beyond bin nbins - 1 are left out.  Deterministic (fixed
+ * summation order).  out is device memory [nbins]. */
+int dd_les_transfer(const dd_plan* plan, const void* const* u, const double* const* tau, int nbins, double* out,
+                    void* work, size_t work_bytes, void* stream);
+/* Workspace of dd_les_gradients, dd_les_stress, dd_les_transfer, dd_les_rhs3d and dd_les_rk4_step3d. */
 int dd_les_workspace_size(const dd_plan* plan, int precision, size_t* bytes);
 /* RHS of the closed LES: dd_rhs3d (physics 0) plus -P[d_j tau_ij]. */
 int dd_les_rhs3d(const dd_plan* plan, const void* const* state, void* const* deriv, const double* inv_k2,
@@ -311,6 +322,36 @@ int dd_les_rhs3d(const dd_plan* plan, const void* const* state, void* const* der
 int dd_les_rk4_step3d(const dd_plan* plan, void* const* state, const double* inv_k2, const void* const* tab_half,
                       const void* const* tab_full, const double* coeff, int viscosity_order, double dt, int precision,
                       const int* nonkept_flag, const dd_closure* cl, void* work, size_t work_bytes, void* stream);
+
+/* ---- Shearing box (FourierShearRepresentation, representations.py:558-740) ----
+ * FP64 transforms of a shearing-box component at time t.  kys is the
+ * component's sheared, wrapped k['y'] (representations.py:627-643) as a device
+ * table, [ky][kx] (Ny x Nx/2+1) in 3D, [kx][ky] in 2D; cut = 2/3 of the y
+ * Nyquist wavenumber; pr = the phase rate S * kx * y of the x-transformed
+ * rows (representations.py:604-611), [y][kx] (Ny x Nx/2+1).
+ * Forward: x r2c, times exp(+i pr t), y (and z) DFTs, 1/N, then the 2/3 rule
+ * on (kx, k_y(t), kz) -- fwd_fftw + dealias (representations.py:676-691).
+ * Backward: the 2/3 rule applied to the input as read (the array is not
+ * modified), y (and z) inverse DFTs, times exp(-i pr t), x c2r -- rev_fftw
+ * (representations.py:693-704).  Lengths as dd_fft_r2c. */
+int dd_shear_workspace_size(const dd_plan* plan, int nfield, size_t* bytes);
+int dd_shear_r2c(const dd_plan* plan, int nfield, const double* const* x, void* const* k, const double* kys,
+                 double cut, const double* pr, double t, void* work, size_t work_bytes, void* stream);
+int dd_shear_c2r(const dd_plan* plan, int nfield, const void* const* k, double* const* x, const double* kys,
+                 double cut, const double* pr, double t, void* work, size_t work_bytes, void* stream);
+/* In-place 2/3 rule with the sheared k_y: dealias_cy_{2d,3d}.dealias_23 with a
+ * full-shape ky (dealias_cy_3d.pyx:39-45, dealias_cy_2d.pyx:36-40). */
+int dd_shear_dealias(const dd_plan* plan, int nfield, void* const* k, const double* kys, double cut, void* stream);
+/* k_out = 1j * k_y(t) * k_in (representations.py:419-425 with the sheared k['y']). */
+int dd_shear_deriv_y(const dd_plan* plan, const double* kys, const void* k_in, void* k_out, void* stream);
+/* Elementwise helpers of the shearing-box / rotating right-hand sides, each
+ * operation rounded as numpy's elementwise expressions are:
+ * k-space: out (+)= (in / r) * w (mode 0; numpy's complex-by-real division,
+ * a product with 1 / r) or (in * r) * w (mode 1), r real, n complex entries;
+ * grid points: out (+)= (a * b) * w (b may be NULL: a * w), n doubles. */
+int dd_kspace_real(int64_t n, const void* in, const double* r, double w, int mode, int accumulate, void* out,
+                   void* stream);
+int dd_xspace_fma(int64_t n, const double* a, const double* b, double w, int accumulate, double* out, void* stream);
 
 #ifdef __cplusplus
 }

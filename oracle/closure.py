@@ -212,9 +212,44 @@ def stress(u, shape, p, norm, delta, rounding=True):
     return [tau[:, c].astype(np.float64).reshape(shape) for c in range(NOUT)]
 
 
-def closure_term(u, shape, p, norm, delta, rounding=True, band=(0.0, 0.0)):
+def shell_weight(shape, table):
+    """w(|k|) on the k layout: table linearly interpolated at |k| (entry i at
+    |k| = i), the last entry beyond the table."""
+    kx, ky, kz = kvectors(shape)
+    kk = np.sqrt(kx ** 2 + ky ** 2 + kz ** 2)
+    t = np.asarray(table, dtype=np.float64)
+    i = np.floor(kk).astype(np.int64)
+    inside = i < t.size - 1
+    ic = np.where(inside, i, 0)
+    f = kk - i
+    return np.where(inside, t[ic] + f * (t[np.minimum(ic + 1, t.size - 1)] - t[ic]), t[-1])
+
+
+def transfer(u, tau, shape, nbins):
+    """Per-shell subgrid energy transfer: sum over the modes with round(|k|) =
+    b of Re(conj(u_a) (-i k_j tau_ij)^_a), over the full spectrum (kx > 0
+    columns twice); u: 3 k arrays, tau: 6 grid-point fields."""
+    th = [to_k(t) for t in tau]
+    kx, ky, kz = kvectors(shape)
+    kv = (kx, ky, kz)
+    rows = [(0, 3, 4), (3, 1, 5), (4, 5, 2)]
+    t = sum((np.conj(u[a]) * sum(-1j * kv[j] * th[rows[a][j]] for j in range(3))).real for a in range(3))
+    nx = shape[2]
+    ix = np.arange(nx // 2 + 1).reshape(1, 1, -1)
+    m = np.where((ix > 0) & (2 * ix < nx), 2.0, 1.0)
+    t = t * m * kept_mask(shape)
+    b = np.floor(np.sqrt(kx ** 2 + ky ** 2 + kz ** 2) + 0.5).astype(np.int64)
+    b = np.broadcast_to(b, t.shape)
+    out = np.zeros(nbins)
+    sel = b < nbins
+    np.add.at(out, b[sel], t[sel])
+    return out
+
+
+def closure_term(u, shape, p, norm, delta, rounding=True, band=(0.0, 0.0), shells=None):
     """-w(|k|) P[d_j tau_ij]^ (3 k arrays, kept modes) for velocity u; w ramps
-    linearly from 0 at |k| = band[0] to 1 at band[1] (w = 1 if band[1] <= 0)."""
+    linearly from 0 at |k| = band[0] to 1 at band[1] (w = 1 if band[1] <= 0),
+    or, with a shell table, is shell_weight(shape, shells)."""
     tau = [to_k(t) for t in stress(u, shape, p, norm, delta, rounding)]
     kx, ky, kz = kvectors(shape)
     kv = (kx, ky, kz)
@@ -225,13 +260,15 @@ def closure_term(u, shape, p, norm, delta, rounding=True, band=(0.0, 0.0)):
     div = sum(kv[a] * s[a] for a in range(3)) / k2
     keep = kept_mask(shape)
     w = 1.0
-    if band[1] > 0:
+    if shells is not None:
+        w = shell_weight(shape, shells)
+    elif band[1] > 0:
         kk = np.sqrt(kx ** 2 + ky ** 2 + kz ** 2)
         w = np.clip((kk - band[0]) / (band[1] - band[0]), 0.0, 1.0)
     return [-(s[a] - kv[a] * div) * keep * w for a in range(3)]
 
 
-def les_physics(shape, p, norm, delta, band=(0.0, 0.0)):
+def les_physics(shape, p, norm, delta, band=(0.0, 0.0), shells=None):
     """Oracle RHS object of the closed LES: the oracle IncompressibleHydro RHS
     with its pressure projection, plus closure_term()."""
     from .physics import IncompressibleHydro
@@ -242,7 +279,7 @@ def les_physics(shape, p, norm, delta, band=(0.0, 0.0)):
             IncompressibleHydro.RHS(self, data, deriv)
             self.pressure_projection(data, deriv)     # skipped by the base for subclasses
             u = [data['u'][i]['kspace'] for i in range(3)]
-            term = closure_term(u, shape, p, norm, delta, band=band)
+            term = closure_term(u, shape, p, norm, delta, band=band, shells=shells)
             for i in range(3):
                 deriv['u'][i]['kspace'] += term[i]
 

@@ -137,7 +137,12 @@ class StateData:
                               params=self.parameters)
 
     def set_time(self, time):
+        # state_data.py:117-121
         self.time = time
+        for name, field in self.fields.items():
+            if field.representation.__name__ == 'FourierShearRepresentation':
+                for i, c in field:
+                    c._update_k()
 
     def add_field(self, name, fieldtype):
         if name in self.fields:

@@ -155,12 +155,21 @@ class Physics:
             output[0]['kspace'] = X[0].deriv(self._trans[1])
             output[1]['kspace'] = -X[0].deriv(self._trans[0])
 
+    # physics.py:412-413 caches k^2 at the first call, which a shearing box
+    # then keeps using; 'current' (test use only) divides by the k^2 of the
+    # call's time instead.
+    laplace_k2 = 'cached'
+
     def laplace_solve(self, X, output):
         # physics.py:407-416
-        if self.k2 is None:
-            self.k2 = output.k2(no_zero=True)
+        if self.laplace_k2 == 'current':
+            k2 = output.k2(no_zero=True)
+        else:
+            if self.k2 is None:
+                self.k2 = output.k2(no_zero=True)
+            k2 = self.k2
         output['kspace'] = X['kspace']
-        output['kspace'] /= self.k2
+        output['kspace'] /= k2
         output['kspace'] *= -1.
 
 

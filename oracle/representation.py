@@ -283,3 +283,90 @@ class FourierRepresentation:
 
     def dx(self):
         return self.length / self.global_shape['xspace']
+
+
+class FourierShearRepresentation(FourierRepresentation):
+    """representations.py:558-740: shearing-box component.
+
+    k['y'] is a full-shape array that follows the shear (``_update_k``,
+    627-643).  The transforms follow the FFTW branch (``fwd_fftw`` /
+    ``rev_fftw``, 676-704): x transform, phase shift exp(+-i S kx y t) of the
+    x-transformed rows, y/z transforms, forward normalised by 1/N, backward
+    unnormalised.  The reference's numpy branch (``rev_np``, 721-737) ends by
+    scaling ``kdata`` instead of ``xdata`` by N, so its backward transform
+    comes out divided by N; the oracle does not restate that slip.  The 2/3
+    rule is the Cython kernel's sheared-ky branch (dealias_cy_3d.pyx:39-45,
+    dealias_cy_2d.pyx:36-40), written here in numpy."""
+
+    _static_k = False
+
+    def __init__(self, sd, shape, length):
+        FourierRepresentation.__init__(self, sd, shape, length)
+        # representations.py:596-617
+        self._ky = self.k['y'].copy()
+        self.k['y'] = self.k['y'] * np.ones_like(self.k['x'])
+        ksize = self.global_shape['kspace'][self.ktrans['x']]
+        xsize = self.global_shape['xspace'][self.xtrans['x']]
+        xkx = npfft.fftfreq(xsize)[:ksize] * 2. * self.kny[self.ktrans['x']]
+        if xsize % 2 == 0:
+            xkx[-1] *= -1.
+        xkx = xkx.reshape((self.ndim - 1) * (1,) + (ksize,))
+        y = self.xspace_grid(open=True)[self.xtrans['y']]
+        self._phase_rate = self.sd.parameters['shear_rate'] * xkx * y
+        self._wave_rate = self.sd.parameters['shear_rate'] * self.k['x']
+        self._update_k()
+
+    def _update_k(self):
+        # representations.py:627-643
+        np.subtract(self._ky, self._wave_rate * self.sd.time, self.k['y'])
+        kny_y = self.kny[3 - self.ndim]
+        if self.k['y'].min() <= -kny_y:
+            self.k['y'][self.k['y'] <= -kny_y] += 2 * kny_y
+        if self.k['y'].max() > kny_y:
+            self.k['y'][self.k['y'] > kny_y] -= 2 * kny_y
+        self.dealias()
+
+    def _sheared_mask(self):
+        if self.ndim == 2:
+            tx, ty = 2. / 3. * self.kny[0], 2. / 3. * self.kny[1]
+            return (((self.k['x'] >= tx) | (self.k['x'] <= -tx)) |
+                    ((self.k['y'] >= ty) | (self.k['y'] <= -ty)))
+        tx, ty, tz = 2. / 3. * self.kny[2], 2. / 3. * self.kny[0], 2. / 3. * self.kny[1]
+        return (((self.k['x'] >= tx) | (self.k['x'] <= -tx)) |
+                ((self.k['y'] >= ty) | (self.k['y'] <= -ty)) |
+                ((self.k['z'] >= tz) | (self.k['z'] <= -tz)))
+
+    def dealias_23(self):
+        self.require_space('kspace')
+        self.data[np.broadcast_to(self._sheared_mask(), self.data.shape)] = 0.
+
+    dealias_23_cython = dealias_23
+
+    def set_dealiasing(self, dealiasing):
+        if dealiasing not in ('2/3', '2/3 cython'):
+            raise NotImplementedError("the oracle's shearing box restates the 2/3 rules only")
+        self.dealias = self.dealias_23
+
+    def fwd_np(self):
+        # representations.py:676-691 (fwd_fftw)
+        m = npfft.rfft(self.xdata, axis=-1)
+        m = m * np.exp(1j * self._phase_rate * self.sd.time)
+        tr = [1, 0, 2][:self.ndim]
+        k = np.transpose(m, tr)
+        if self.ndim == 2:
+            k = npfft.fft(k, axis=1)
+        else:
+            k = npfft.fftn(k, axes=(0, 1))
+        self.kdata[:] = k / self.global_shape['xspace'].prod()
+
+    def rev_np(self):
+        # representations.py:693-704 (rev_fftw: unnormalised inverse)
+        gx = self.global_shape['xspace']
+        if self.ndim == 2:
+            k = npfft.ifft(self.kdata, axis=1) * gx[0]
+        else:
+            k = npfft.ifftn(self.kdata, axes=(0, 1)) * (gx[0] * gx[1])
+        tr = [1, 0, 2][:self.ndim]
+        m = np.transpose(k, tr)
+        m = m * np.exp(-1j * self._phase_rate * self.sd.time)
+        self.xdata[:] = npfft.irfft(m, n=int(gx[-1]), axis=-1) * gx[-1]

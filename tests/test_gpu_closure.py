@@ -206,13 +206,21 @@ def _norm_for(dd, shape, u, delta):
     return in_mean, in_scale, np.array([0.05, 0.04, 0.03, 0.0, 0.01, -0.01]), np.full(6, 0.02)
 
 
+# a shell table with negative entries (backscatter) and a ramp, shorter than
+# the largest |k| of a 32^3 kept set (18.2), so the last entry is used beyond it
+_SHELLS = [0.3, 0.3, -0.5, -0.8, -0.2, 0.4, 1.0, 1.7, 2.5, 3.1, 3.6, 4.0, 4.2, 4.3]
+
+
 @pytest.mark.gpu
-@pytest.mark.parametrize("shape,band", [((16, 16, 16), (0.0, 0.0)), ((32, 32, 32), (0.0, 0.0)),
-                                        ((32, 32, 32), (3.0, 7.5))])
-def test_les_closure_term_matches_oracle(dd, cuda, shape, band):
+@pytest.mark.parametrize("shape,band,shells", [((16, 16, 16), (0.0, 0.0), None), ((32, 32, 32), (0.0, 0.0), None),
+                                               ((32, 32, 32), (3.0, 7.5), None),
+                                               ((32, 32, 32), (0.0, 0.0), _SHELLS)])
+def test_les_closure_term_matches_oracle(dd, cuda, shape, band, shells):
     u = dd.init_cond.turbulence_3d(shape, seed=21)
     delta = np.pi / (np.ceil(shape[0] / 3) - 1)
     c = _closure(dd, _params(4), delta).with_band(*band)
+    if shells is not None:
+        c = c.with_shells(shells)
     c.set_norm(*_norm_for(dd, shape, u, delta))
     Rl, dl = _les_pair(dd, shape, c, u)
     Rp, dp = _les_pair(dd, shape, None, u)
@@ -220,10 +228,54 @@ def test_les_closure_term_matches_oracle(dd, cuda, shape, band):
     Rl.RHS(dl, kl)
     Rp.RHS(dp, kp)
     term = [kl['u'][i].to_numpy('kspace') - kp['u'][i].to_numpy('kspace') for i in range(3)]
-    ref = OC.closure_term(u, shape, c.params.cpu().numpy(), c.norm.cpu().numpy(), delta, band=band)
+    ref = OC.closure_term(u, shape, c.params.cpu().numpy(), c.norm.cpu().numpy(), delta, band=band, shells=shells)
     num = np.sqrt(sum(np.sum(np.abs(a - b) ** 2) for a, b in zip(term, ref)))
     den = np.sqrt(sum(np.sum(np.abs(b) ** 2) for b in ref))
     assert den > 0 and num / den < 2e-3, num / den
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape", [(16, 16, 16), (32, 32, 32)])
+def test_les_transfer_matches_oracle(dd, cuda, shape):
+    """dd_les_transfer (per-shell subgrid energy transfer) against the oracle
+    on a random velocity and random grid-point stresses, to 1e-12 of the
+    largest shell (FP64; the summation orders differ)."""
+    import torch
+    C = dd.closure
+    u = dd.init_cond.turbulence_3d(shape, seed=31)
+    rng = np.random.Generator(np.random.PCG64(32))
+    tau = [rng.normal(0, 1, shape) for _ in range(6)]
+    nb = C.shell_count(shape[0])
+    plan = dd.engine.get_plan(shape, (2 * np.pi,) * 3)
+    n = ctypes.c_size_t()
+    dd._lib.call("dd_les_workspace_size", plan.handle, dd._lib.DD_FP64, ctypes.byref(n))
+    ws = torch.empty(n.value, dtype=torch.uint8, device="cuda")
+    ud = [_dev(c) for c in u]
+    td = [_dev(t) for t in tau]
+    up, _a = C._ptrs(ud)
+    tp, _b = C._ptrs(td)
+    out = torch.empty(nb, dtype=torch.float64, device="cuda")
+    dd._lib.call("dd_les_transfer", plan.handle, up, tp, nb, dd.engine.dptr(out), dd.engine.dptr(ws), ws.numel(),
+                 dd.engine.current_stream())
+    got = out.cpu().numpy()
+    ref = OC.transfer(u, tau, shape, nb)
+    assert np.max(np.abs(got - ref)) <= 1e-12 * np.max(np.abs(ref)), (got, ref)
+    # fewer bins: the tail is left out, the head unchanged
+    out2 = torch.empty(5, dtype=torch.float64, device="cuda")
+    dd._lib.call("dd_les_transfer", plan.handle, up, tp, 5, dd.engine.dptr(out2), dd.engine.dptr(ws), ws.numel(),
+                 dd.engine.current_stream())
+    assert np.array_equal(out2.cpu().numpy(), got[:5])
+
+
+@pytest.mark.gpu
+def test_shell_table_survives_save_and_load(dd, cuda, tmp_path):
+    c = _closure(dd, _params(9), 0.15).with_shells(_SHELLS)
+    path = str(tmp_path / "c.npz")
+    c.save(path)
+    d = dd.closure.MLPClosure.load(path)
+    assert np.array_equal(d.shell_w.cpu().numpy(), np.array(_SHELLS))
+    s = d.struct()
+    assert s.n_shell == len(_SHELLS) and s.shell_w == d.shell_w.data_ptr()
 
 
 @pytest.mark.gpu

@@ -96,3 +96,45 @@ def test_constant_stress_gives_no_closure_term():
     norm[32:38] = [0.3, 0.2, 0.1, 0.05, 0.0, -0.1]
     t = OC.closure_term(u, shape, OC.pack(w), norm, 0.1)
     assert max(np.max(np.abs(c)) for c in t) < 1e-14
+
+
+def _solenoidal(shape, seed):
+    """Random kept-mode solenoidal velocity (3 k arrays)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    u = [OC.to_k(rng.normal(size=shape)) for _ in range(3)]
+    kx, ky, kz = OC.kvectors(shape)
+    k2 = kx ** 2 + ky ** 2 + kz ** 2
+    d = (kx * u[0] + ky * u[1] + kz * u[2]) / np.where(k2 == 0, 1.0, k2)
+    return [u[0] - kx * d, u[1] - ky * d, u[2] - kz * d]
+
+
+def test_transfer_sums_to_stress_strain_product():
+    """Parseval: the per-shell transfers of a solenoidal velocity add up to
+    <tau_ij S_ij> over the grid (all shells kept)."""
+    shape = (16, 16, 16)
+    u = _solenoidal(shape, 5)
+    rng = np.random.Generator(np.random.PCG64(6))
+    tau = [OC.to_x(OC.to_k(rng.normal(size=shape)), shape) for _ in range(6)]
+    T = OC.transfer(u, tau, shape, 64)
+    G = OC.gradients(u, shape)           # G[3 a + j] = d_j u_a
+    ts = 0.0
+    for c, (a, b) in enumerate(OC.PAIRS):
+        s = 0.5 * (G[3 * a + b] + G[3 * b + a])
+        ts += (1.0 if a == b else 2.0) * np.mean(tau[c] * s)
+    assert abs(T.sum() - ts) <= 1e-12 * max(abs(ts), np.max(np.abs(T)))
+
+
+def test_shell_table_interpolates_and_reproduces_a_ramp():
+    shape = (16, 16, 16)
+    lo, hi = 2.0, 6.0
+    table = np.clip((np.arange(8.0) - lo) / (hi - lo), 0.0, 1.0)
+    w = OC.shell_weight(shape, table)
+    kx, ky, kz = OC.kvectors(shape)
+    kk = np.sqrt(kx ** 2 + ky ** 2 + kz ** 2)
+    ramp = np.clip((kk - lo) / (hi - lo), 0.0, 1.0)
+    assert np.allclose(w, ramp, rtol=0, atol=1e-15)
+    # beyond the table: its last entry
+    w2 = OC.shell_weight(shape, [0.5, 1.5, 2.5])
+    assert np.all(w2[kk >= 2.0] == 2.5)
+    sel = kk < 2.0
+    assert np.allclose(w2[sel], (0.5 + kk)[sel], atol=1e-15)
