@@ -68,6 +68,8 @@ def main(argv=None):
     ap.add_argument("--eval-seeds", type=int, nargs="+", default=None, help="evaluate on each (overrides --eval-seed)")
     ap.add_argument("--base", default=None, help="start from this stored network (no dataset, no training)")
     ap.add_argument("--calibrate-seeds", type=int, default=0)
+    ap.add_argument("--backscatter", type=float, nargs="+", default=None, metavar="B",
+                    help="also select among shell tables gain * ramp(10.5, 21) - B below 10.5 (gain 2)")
     ap.add_argument("--out", default=os.path.join(HERE, "les_closure_256to64.npz"))
     ap.add_argument("--report", default=None)
     ap.add_argument("--dump-samples", type=int, default=0, help="save this many random raw samples")
@@ -162,6 +164,13 @@ def finish(a, C, rep, models, band, log, write_report):
         if "band_stress" in models:
             for gn in (1.0, 1.5, 2.0, 3.0):
                 cands["band_stress_x%g" % gn] = models["band_stress"].with_band(band[0], band[1], gn)
+        if a.backscatter:
+            kk = np.arange(C.shell_count(a.les), dtype=np.float64)
+            ramp = 2.0 * np.clip((kk - 10.5) / 10.5, 0.0, 1.0)
+            for b in a.backscatter:
+                w = np.where(kk < 10.5, -b, ramp)
+                w[0] = 0.0
+                cands["stress_band_x2_backscatter_%g" % b] = models["stress"].with_shells(w)
         if shells is not None:
             cands["stress_shells"] = models["stress"].with_shells(shells)
             cands["stress_shells_no_backscatter"] = models["stress"].with_shells(np.maximum(shells, 0.0))
