@@ -50,6 +50,8 @@ WORKLOADS = {
     "hydro3d-256-df64": dict(kind="hydro3d", shape=(256,) * 3, nu=5e-3, dt=2e-3, precision="df64"),
     "hydro3d-256-fp32": dict(kind="hydro3d", shape=(256,) * 3, nu=5e-3, dt=2e-3, precision="fp32"),
     "hydro3d-128-fp64": dict(kind="hydro3d", shape=(128,) * 3, nu=5e-3, dt=2e-3, precision="fp64"),
+    # 256-point x rows on a grid small enough for a full ncu capture, larger than L2
+    "hydro3d-128x128x256-fp64": dict(kind="hydro3d", shape=(128, 128, 256), nu=5e-3, dt=2e-3, precision="fp64"),
     "hydro3d-128-df64": dict(kind="hydro3d", shape=(128,) * 3, nu=5e-3, dt=2e-3, precision="df64"),
     "mhd3d-256-fp32": dict(kind="mhd3d", shape=(256,) * 3, nu=5e-3, dt=1e-3, precision="fp32"),
     "mhd3d-256-fp64": dict(kind="mhd3d", shape=(256,) * 3, nu=5e-3, dt=1e-3, precision="fp64"),
@@ -71,6 +73,9 @@ TRAFFIC = {
     ("hydro3d-256-fp64", "x_cross_256_f64"): (
         8 * (67.76e6 + 18.20e6),
         "ncu capture of the same kernel on 128^3 FP64 (67.76 MB read + 18.20 MB written), x8 for 256^3"),
+    ("hydro3d-256-fp64", "x_div_256_f64"): (
+        4 * (67.74e6 + 92.44e6),
+        "ncu capture of the same kernel on 128x128x256 FP64 (67.74 MB read + 92.44 MB written), x4 rows for 256^3"),
     ("les64-closure", "les_mlp"): (
         18.92e6 + 0.0, "ncu capture at full size (18.92 MB read, stresses still in L2 at kernel end)"),
 }
@@ -82,6 +87,16 @@ def B3(N):
 
 def C3(N):
     return 16 * N ** 2 * (N // 2 + 1)
+
+
+def B3s(shape):
+    nz, ny, nx = shape
+    return 8 * nz * ny * nx + 16 * nz * ny * (nx // 2 + 1)
+
+
+def C3s(shape):
+    nz, ny, nx = shape
+    return 16 * nz * ny * (nx // 2 + 1)
 
 
 def B2(N):
@@ -181,17 +196,41 @@ class Hydro3Runner:
     def state(self):
         return [self.data[f][c].kdata for f, c in self.names]
 
+    def divergence_form(self):
+        """True when the fused steps ran the divergence form (3 + 5
+        transforms per RHS; chosen per step for a solenoidal state)."""
+        return getattr(self.rhs, "last_phys3d", 0) == 2
+
+    def transforms_per_rhs(self):
+        return 18 if self.mhd else (8 if self.divergence_form() else 9)
+
     def bytes_per_step(self):
-        N = self.wl["shape"][0]
+        """Algorithmic bytes: every transform reads and writes one real and one
+        complex field (B3), every stage reads/writes three complex passes per
+        component (C3); the divergence form's stages read two more product
+        fields."""
+        sh = self.wl["shape"]
         if self.mhd:
-            return 4 * 18 * B3(N) + 4 * 6 * 3 * C3(N)
-        return 4 * 9 * B3(N) + 4 * 3 * 3 * C3(N)
+            return 4 * 18 * B3s(sh) + 4 * 6 * 3 * C3s(sh)
+        extra = 4 * 2 * C3s(sh) if self.divergence_form() else 0
+        return 4 * self.transforms_per_rhs() * B3s(sh) + 4 * 3 * 3 * C3s(sh) + extra
+
+    def canonical_bytes_per_step(self):
+        """The rotational-form count (4 RHS x 9 transforms) for comparison."""
+        sh = self.wl["shape"]
+        return 4 * 9 * B3s(sh) + 4 * 3 * 3 * C3s(sh)
 
     def point_stages(self):
         return float(np.prod(self.wl["shape"])) * 4
 
     def flops_per_step(self):
-        return 4 * (18 if self.mhd else 9) * fft_flops(self.wl["shape"])
+        return 4 * self.transforms_per_rhs() * fft_flops(self.wl["shape"])
+
+    def _nio(self):
+        g = 2 if self.mhd else 1
+        if self.divergence_form():
+            return 3, 5
+        return 6 * g, 3 * g
 
     def kernel_flops(self, label):
         """Canonical transform flops of one launch (5 L log2 L per complex
@@ -199,13 +238,14 @@ class Hydro3Runner:
         Nz, Ny, Nx = self.wl["shape"]
         Mx, My, Mz = (Nx - 1) // 3, (Ny - 1) // 3, (Nz - 1) // 3
         Kx, Ky = Mx + 1, 2 * My + 1
-        g = 2 if self.mhd else 1
-        ni, no = 6 * g, 3 * g
+        ni, no = self._nio()
         cf = lambda L: 5.0 * L * np.log2(L)
         if label.startswith("z_inv_curl"):
             return ni * Kx * Ky * cf(Nz)
         if label.startswith("y_inv"):
             return ni * Kx * Nz * cf(Ny)
+        if label.startswith("x_div"):
+            return Nz * Ny * ((ni + no) * 0.5 * cf(Nx) + Nx * 7)
         if label.startswith("x_cross"):
             return Nz * Ny * ((ni + no) * 0.5 * cf(Nx) + Nx * (9 if not self.mhd else 30))
         if label.startswith("y_fwd"):
@@ -224,19 +264,21 @@ class Hydro3Runner:
         kc = Ky * Kz * Kx * 16
         w1, w2 = Ky * Nz * Kx * cs, Nz * Ny * Kx * cs
         g = 2 if self.mhd else 1           # vector fields in the state
-        ni, no = 6 * g, 3 * g
+        ni, no = self._nio()
         if label.startswith("z_inv_curl"):
             return 3 * g * kc + ni * w1
         if label.startswith("y_inv"):
             return ni * (w1 + w2)
-        if label.startswith("x_cross"):
+        if label.startswith("x_cross") or label.startswith("x_div"):
             return (ni + no) * w2
         if label.startswith("y_fwd"):
             return no * (w2 + w1)
         if label.startswith("z_fwd_compact"):
             return no * (w1 + kc)
         if label.startswith("rk4_stage3"):
-            return 3 * g * kc * 5
+            return 3 * g * kc * 5 + (2 * kc if self.divergence_form() else 0)
+        if label.startswith("div_sums3"):
+            return 3 * kc
         return None
 
     def config(self, ws):
@@ -245,7 +287,10 @@ class Hydro3Runner:
                             % ("3D incompressible MHD" if self.mhd else "3D incompressible hydro", *w["shape"], w["dt"],
                                w["nu"], ", eta=%g" % w["nu"] if self.mhd else "", w["precision"]),
                 "grid": list(w["shape"]), "integrator": "RK4", "dt": w["dt"], "precision": w["precision"],
-                "parallelism": "replicas x%d" % ws, "l2": "inputs larger than L2 (state + intermediates), no flush"}
+                "parallelism": "replicas x%d" % ws, "l2": "inputs larger than L2 (state + intermediates), no flush",
+                "nonlinear_form": ("curl form (6 + 12 transforms per RHS)" if self.mhd else
+                                   "divergence form, 3 + 5 transforms per RHS (solenoidal state, checked every step)"
+                                   if self.divergence_form() else "rotational form, 6 + 3 transforms per RHS")}
 
     def metric(self):
         if self.mhd:
@@ -830,6 +875,13 @@ def main():
                              "DGEMM" if wl["precision"] == "fp64" else "SGEMM (no TF32)"),
                          "t_flops_ms": t_f * 1e3, "combined_bound": "hbm" if t_b >= t_f else "flops",
                          "combined_frac": max(t_b, t_f) / (ms_per_step / 1e3)})
+        if hasattr(run, "transforms_per_rhs"):
+            step_hbm["transforms_per_rhs"] = run.transforms_per_rhs()
+            if run.transforms_per_rhs() != 9 and not getattr(run, "mhd", False):
+                # the same step measured against the rotational form's 9-transform count
+                F9, B9 = F * 9 / run.transforms_per_rhs(), run.canonical_bytes_per_step()
+                step_hbm["combined_frac_vs_9_transform_count"] = max(B9 / (hbm_peak * 1e9), F9 / (P * 1e12)) / (
+                    ms_per_step / 1e3)
 
     # end to end through the public API: the state in from pinned host memory,
     # one step, the state back out, every step

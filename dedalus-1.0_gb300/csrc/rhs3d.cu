@@ -70,12 +70,36 @@ __device__ __forceinline__ double inv_k2_of(const ProjArgs& a, double k2, int& q
     return rdiv(1., k2 == 0. ? 1. : k2);
 }
 
+// N_i = -i k_j T_ij from the five divergence-form products at entry i (order
+// xx - zz, yy - zz, xy, xz, yz; T_zz = 0).  -i s = (s.y, -s.x).
+__device__ __forceinline__ void div_form(const CPtrs& nc, int64_t i, double kxv, double kyv, double kzv, double2* k) {
+    const double2 a = ((const double2*)nc.p[0])[i], b = ((const double2*)nc.p[1])[i];
+    const double2 c = ((const double2*)nc.p[2])[i], d = ((const double2*)nc.p[3])[i];
+    const double2 e = ((const double2*)nc.p[4])[i];
+    const double sxr = fma(kzv, d.x, fma(kyv, c.x, kxv * a.x)), sxi = fma(kzv, d.y, fma(kyv, c.y, kxv * a.y));
+    const double syr = fma(kzv, e.x, fma(kyv, b.x, kxv * c.x)), syi = fma(kzv, e.y, fma(kyv, b.y, kxv * c.y));
+    const double szr = fma(kyv, e.x, kxv * d.x), szi = fma(kyv, e.y, kxv * d.y);
+    k[0] = make_double2(sxi, -sxr);
+    k[1] = make_double2(syi, -syr);
+    k[2] = make_double2(szi, -szr);
+}
+
+// Unprojected nonlinear term of every state component at kept entry i.
+template <int PH>
+__device__ __forceinline__ void load_nc(const CPtrs& nc, int64_t i, double kxv, double kyv, double kzv, double2* k) {
+    if constexpr (PH == P3_HYDRO_DIV) {
+        div_form(nc, i, kxv, kyv, kzv, k);
+    } else {
+#pragma unroll
+        for (int c = 0; c < Phys3<PH>::NO; c++) k[c] = ((const double2*)nc.p[c])[i];
+    }
+}
+
 // RHS of every state component at one kept entry from the compact products.
 template <int PH>
 __device__ __forceinline__ void rhs_at(const CPtrs& nc, int64_t i, double kxv, double kyv, double kzv, double s,
                                        double2* k) {
-#pragma unroll
-    for (int c = 0; c < Phys3<PH>::NO; c++) k[c] = ((const double2*)nc.p[c])[i];
+    load_nc<PH>(nc, i, kxv, kyv, kzv, k);
     project(k[0], k[1], k[2], kxv, kyv, kzv, s);
     if constexpr (PH == P3_MHD) curl_k(k[3], k[4], k[5], kxv, kyv, kzv);
 }
@@ -144,8 +168,7 @@ __global__ void k_rk4_stage3(RK4Args a) {
         int q;
         const double s = inv_k2_of(a.pa, k2, q);
         double2 k[6];
-#pragma unroll
-        for (int c = 0; c < Phys3<PH>::NO; c++) k[c] = ((const double2*)a.nc.p[c])[i];
+        load_nc<PH>(a.nc, i, kxv, kyv, kzv, k);
         project_fma(k[0], k[1], k[2], kxv, kyv, kzv, s);
         if constexpr (PH == P3_MHD) curl_k(k[3], k[4], k[5], kxv, kyv, kzv);
         double f0[NG], f1h[NG];
@@ -229,6 +252,40 @@ __global__ void k_dealias3_all(Geo3 g, Ptrs k) {
     }
 }
 
+// Sums over the kept modes of a full-layout velocity: out[0] += |k . u|^2,
+// out[1] += |k|^2 |u|^2 (block partials, then one atomic add per block).
+__global__ void __launch_bounds__(256) k_div_sums3(Geo3 g, const double* kx, const double* ky, const double* kz,
+                                                    CPtrs u, double* out) {
+    __shared__ double r0[256], r1[256];
+    const int n = g.Ky * g.Kz * g.Kx;      // < 2^31 for every supported grid
+    double s0 = 0., s1 = 0.;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int ix = i % g.Kx, r = i / g.Kx;
+        const int kzc = r % g.Kz, kyc = r / g.Kz;
+        const int ky_i = compact_to_full(kyc, g.Ny, g.Ky), kz_i = compact_to_full(kzc, g.Nz, g.Kz);
+        const int64_t o = ((int64_t)ky_i * g.Nz + kz_i) * g.Nh + ix;
+        const double kv[3] = {kx[ix], ky[ky_i], kz[kz_i]};
+        double dr = 0., di = 0., uu = 0.;
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            const double2 v = ((const double2*)u.p[a])[o];
+            dr += kv[a] * v.x;
+            di += kv[a] * v.y;
+            uu += v.x * v.x + v.y * v.y;
+        }
+        s0 += dr * dr + di * di;
+        s1 += (kv[0] * kv[0] + kv[1] * kv[1] + kv[2] * kv[2]) * uu;
+    }
+    r0[threadIdx.x] = s0;
+    r1[threadIdx.x] = s1;
+    __syncthreads();
+    for (int h = 128; h > 0; h >>= 1) {
+        if (threadIdx.x < h) { r0[threadIdx.x] += r0[threadIdx.x + h]; r1[threadIdx.x] += r1[threadIdx.x + h]; }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) { atomicAdd(out, r0[0]); atomicAdd(out + 1, r1[0]); }
+}
+
 static unsigned ew_grid(int64_t n) {
     int64_t b = (n + 255) / 256;
     if (b > 152 * 16) b = 152 * 16;
@@ -246,7 +303,7 @@ static int nonlinear3_any(const dd_plan* pl, int prec, bool compact, const void*
         return compact ? nonlinear3<df64, true, PH>(pl, u, inv_fpr, w, st)
                        : nonlinear3<df64, false, PH>(pl, u, inv_fpr, w, st);
     }
-    set_error("double-float arithmetic is implemented for 3D hydro only");
+    set_error("double-float arithmetic is implemented for 3D hydro in rotational form only");
     return DD_ERR_UNSUPPORTED;
 }
 
@@ -358,9 +415,10 @@ using namespace dd;
 static int check3(const dd_plan* p, int phys, const double* params, const void* const* a, const void* const* b) {
     DD_CHECK_ARG(p, "null plan");
     DD_CHECK_ARG(p->ndim == 3, "plan is not 3D");
-    DD_CHECK_ARG(phys == P3_HYDRO || phys == P3_MHD, "physics must be 0 (hydro) or 1 (MHD)");
-    DD_CHECK_ARG(phys == P3_HYDRO || (params && params[0] > 0.), "MHD needs params = {rho0 > 0}");
-    const int nf = phys == P3_HYDRO ? 3 : 6;
+    DD_CHECK_ARG(phys == P3_HYDRO || phys == P3_MHD || phys == P3_HYDRO_DIV,
+                 "physics must be 0 (hydro), 1 (MHD) or 2 (hydro, divergence form)");
+    DD_CHECK_ARG(phys != P3_MHD || (params && params[0] > 0.), "MHD needs params = {rho0 > 0}");
+    const int nf = phys == P3_MHD ? 6 : 3;
     DD_CHECK_ARG(a, "null field array");
     for (int c = 0; c < nf; c++) {
         DD_CHECK_ARG(a[c], "null field pointer %d", c);
@@ -373,10 +431,12 @@ extern "C" {
 
 int dd_rhs3d_workspace_size(const dd_plan* p, int physics, int precision, size_t* bytes) {
     DD_CHECK_ARG(p && bytes && p->ndim == 3, "dd_rhs3d_workspace_size: bad arguments");
-    DD_CHECK_ARG(physics == P3_HYDRO || physics == P3_MHD, "physics must be 0 (hydro) or 1 (MHD)");
-    const int ni = physics == P3_HYDRO ? 6 : 12, no = ni / 2, nf = no;
+    DD_CHECK_ARG(physics == P3_HYDRO || physics == P3_MHD || physics == P3_HYDRO_DIV,
+                 "physics must be 0 (hydro), 1 (MHD) or 2 (hydro, divergence form)");
     DD_CHECK_ARG(precision >= DD_FP64 && precision <= DD_DF64, "bad precision");
-    *bytes = work3_bytes(precision, p->g3, ni, no, nf, true);
+    if (physics == P3_HYDRO) *bytes = work3_bytes(precision, p->g3, 6, 3, 3, true);
+    else if (physics == P3_MHD) *bytes = work3_bytes(precision, p->g3, 12, 6, 6, true);
+    else *bytes = work3_bytes(precision, p->g3, 5, 5, 3, true);
     return DD_OK;
 }
 
@@ -388,6 +448,8 @@ int dd_rhs3d(const dd_plan* p, int physics, const double* params, const void* co
     cudaStream_t st = (cudaStream_t)stream;
     if (physics == P3_HYDRO)
         return rhs3<P3_HYDRO>(p, params, state, deriv, inv_k2, precision, zero_nonkept, work, work_bytes, st);
+    if (physics == P3_HYDRO_DIV)
+        return rhs3<P3_HYDRO_DIV>(p, params, state, deriv, inv_k2, precision, zero_nonkept, work, work_bytes, st);
     return rhs3<P3_MHD>(p, params, state, deriv, inv_k2, precision, zero_nonkept, work, work_bytes, st);
 }
 
@@ -403,6 +465,9 @@ int dd_rk4_step3d(const dd_plan* p, int physics, const double* params, void* con
     if (physics == P3_HYDRO)
         return rk4_3<P3_HYDRO>(p, params, state, inv_k2, tab_half, tab_full, coeff, viscosity_order, dt, precision,
                                nonkept_flag, work, work_bytes, st);
+    if (physics == P3_HYDRO_DIV)
+        return rk4_3<P3_HYDRO_DIV>(p, params, state, inv_k2, tab_half, tab_full, coeff, viscosity_order, dt,
+                                   precision, nonkept_flag, work, work_bytes, st);
     return rk4_3<P3_MHD>(p, params, state, inv_k2, tab_half, tab_full, coeff, viscosity_order, dt, precision,
                          nonkept_flag, work, work_bytes, st);
 }
@@ -473,6 +538,21 @@ int dd_hydro3d_rk4_step(const dd_plan* p, void* const* u, const double* inv_k2, 
     const double c[1] = {nu};
     return dd_rk4_step3d(p, P3_HYDRO, nullptr, u, inv_k2, th, tf, c, viscosity_order, dt, precision, nonkept_flag,
                          work, work_bytes, stream);
+}
+
+int dd_divergence_sums(const dd_plan* p, const void* const* u, double* out, void* stream) {
+    DD_CHECK_ARG(p && u && out, "dd_divergence_sums: null pointer");
+    DD_CHECK_ARG(p->ndim == 3, "dd_divergence_sums: 3D plans only");
+    CPtrs uc{};
+    for (int a = 0; a < 3; a++) { DD_CHECK_ARG(u[a], "null velocity %d", a); uc.p[a] = u[a]; }
+    cudaStream_t st = (cudaStream_t)stream;
+    DD_CUDA(cudaMemsetAsync(out, 0, 2 * sizeof(double), st));
+    const Geo3& g = p->g3;
+    const int64_t nk = (int64_t)g.Ky * g.Kz * g.Kx;
+    const unsigned nb = (unsigned)std::min<int64_t>((nk + 255) / 256, 152 * 4);
+    DD_KT("div_sums3", st, k_div_sums3<<<nb, 256, 0, st>>>(g, p->kx, p->ky, p->kz, uc, out));
+    DD_LAUNCH_CHECK();
+    return DD_OK;
 }
 
 int dd_any_nonkept(const dd_plan* p, int ncomp, const void* const* k, int* dflag, void* stream) {

@@ -2,6 +2,7 @@
 // Fused 3D right-hand sides and RK4 step for incompressible hydro and MHD.
 //
 //   hydro: RHS(u) = P[u x w]^, w = curl u                  (physics.py:527-599)
+//          or, for a solenoidal state, P[-i k_j T_ij] (ProdDiv3 below)
 //   MHD:   RHS(u) = P[u x w + (J x B) / (4 pi rho0)]^, J = curl B,
 //          RHS(B) = curl (u x B)^                            (physics.py:770-819)
 // The rotational form u x w equals the reference's -(u.grad)u on the kept
@@ -24,10 +25,14 @@
 
 namespace dd {
 
-enum { P3_HYDRO = 0, P3_MHD = 1 };
+// P3_HYDRO_DIV: hydro with the nonlinear term in divergence form, valid for a
+// solenoidal state (below).  NI = transform buffers, NINV = inverse-transformed
+// fields, NO = forward-transformed products.
+enum { P3_HYDRO = 0, P3_MHD = 1, P3_HYDRO_DIV = 2 };
 template <int PH> struct Phys3;
-template <> struct Phys3<P3_HYDRO> { static constexpr int NG = 1, NF = 3, NI = 6, NO = 3; };
-template <> struct Phys3<P3_MHD>   { static constexpr int NG = 2, NF = 6, NI = 12, NO = 6; };
+template <> struct Phys3<P3_HYDRO>     { static constexpr int NG = 1, NF = 3, NI = 6, NINV = 6, NO = 3; };
+template <> struct Phys3<P3_MHD>       { static constexpr int NG = 2, NF = 6, NI = 12, NINV = 12, NO = 6; };
+template <> struct Phys3<P3_HYDRO_DIV> { static constexpr int NG = 1, NF = 3, NI = 5, NINV = 3, NO = 5; };
 static_assert(Phys3<P3_MHD>::NI <= DD_MAXF, "too many transform fields for Ptrs");
 
 // a * (1j * k) as numpy computes it (representations.py:423)
@@ -106,6 +111,27 @@ struct ProdMHD3 {
     }
 };
 
+// Divergence form (Basdevant's five products): for a solenoidal u,
+// -(u.grad)u = -d_j (u_i u_j) = -d_j T_ij - grad(u_z u_z) with T = u u^T - u_z^2 I,
+// whose diagonal (xx - zz, yy - zz, 0) leaves five independent entries.  The
+// gradient is removed by the projection, so P[-i k_j T_ij] is the reference's
+// RHS whenever div u = 0: 3 inverse and 5 forward transforms per RHS instead of
+// 6 + 3.  out: xx - zz, yy - zz, xy, xz, yz.
+template <typename T>
+struct ProdDiv3 {
+    static constexpr int NI = 3, NO = 5;
+    static constexpr int lmin = 16, lmax = 512;
+    __device__ void operator()(const T* in, T* out, int) const {
+        const T ux = in[0], uy = in[1], uz = in[2];
+        const T zz = uz * uz;
+        out[0] = ux * ux - zz;
+        out[1] = uy * uy - zz;
+        out[2] = ux * uy;
+        out[3] = ux * uz;
+        out[4] = uy * uz;
+    }
+};
+
 // ------------------------------------------------------------------ pass 5
 template <typename T>
 struct OpZFwdCompact3 {
@@ -169,11 +195,14 @@ int nonlinear3(const dd_plan* pl, const void* const* u, double inv_fpr, const Wo
         w2.p[f] = w.W2<T>(f); w2c.p[f] = w2.p[f];
     }
     OpZInvCurl3<T, COMPACT, P::NG> a{g, uin, w1, TwSel<T>::z(pl), pl->kx, pl->ky, pl->kz};
-    DD_TRY((launch_pass_len<T, true, false, false>(g.Nz, a, g.Kx, g.Ky, P::NI, st)));
+    DD_TRY((launch_pass_len<T, true, false, false>(g.Nz, a, g.Kx, g.Ky, P::NINV, st)));
     OpYInv3<T> b{g, w1c, w2, TwSel<T>::y(pl)};
-    DD_TRY((launch_pass_len<T, true, false, false>(g.Ny, b, g.Kx, g.Nz, P::NI, st)));
+    DD_TRY((launch_pass_len<T, true, false, false>(g.Ny, b, g.Kx, g.Nz, P::NINV, st)));
     // products overwrite fields 0..NO-1 of W2 row by row (each block reads its rows first)
-    if constexpr (PH == P3_HYDRO) {
+    if constexpr (PH == P3_HYDRO_DIV) {
+        DD_TRY((launch_x_prod_len<T>("x_div", g.Nx, g.Nz * g.Ny, g.Kx, w2c, w2, 1, 0, 0, TwSel<T>::x(pl),
+                                     (T)pl->inv_n, ProdDiv3<T>{}, st)));
+    } else if constexpr (PH == P3_HYDRO) {
         DD_TRY((launch_x_prod_len<T>("x_cross", g.Nx, g.Nz * g.Ny, g.Kx, w2c, w2, 1, 0, 0, TwSel<T>::x(pl),
                                      (T)pl->inv_n, ProdHydro3<T>{}, st)));
     } else {
@@ -194,6 +223,7 @@ int nonlinear3(const dd_plan* pl, const void* const* u, double inv_fpr, const Wo
                                               cudaStream_t);                                            \
     EXT template int nonlinear3<T, true, PH>(const dd_plan*, const void* const*, double, const Work3&,      \
                                              cudaStream_t);
-#define DD_RHS3D_INSTANTIATE(EXT, T) DD_RHS3D_INSTANTIATE_PH(EXT, T, P3_HYDRO) DD_RHS3D_INSTANTIATE_PH(EXT, T, P3_MHD)
+#define DD_RHS3D_INSTANTIATE(EXT, T) DD_RHS3D_INSTANTIATE_PH(EXT, T, P3_HYDRO) DD_RHS3D_INSTANTIATE_PH(EXT, T, P3_MHD) \
+    DD_RHS3D_INSTANTIATE_PH(EXT, T, P3_HYDRO_DIV)
 
 }  // namespace dd

@@ -42,6 +42,13 @@ template <> struct ProdCfg<512, 6, 3> {
     using SI = Sched<512, 6, 192, 8, 8, 8>;  using SF = Sched<512, 3, 192, 8, 8, 8>;
     static constexpr int Q = 2, NT = 192;
 };
+// Hydro in divergence form (3 -> 5): the forward side has 5/3 of the inverse
+// pencils; 4 rows per block fill 6 inverse pencils (32 threads each) and 10
+// forward pencils (16 threads each).
+template <> struct ProdCfg<256, 3, 5> {
+    using SI = Sched<256, 6, 192, 8, 8, 4>;  using SF = Sched<256, 10, 160, 16, 16, 1>;
+    static constexpr int Q = 4, NT = 192;
+};
 template <> struct ProdCfg<64, 12, 6> {
     using SI = Sched<64, 24, 192, 8, 8, 1>;  using SF = Sched<64, 12, 192, 4, 4, 4>;
     static constexpr int Q = 4, NT = 192;

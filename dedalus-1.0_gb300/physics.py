@@ -253,6 +253,27 @@ class IncompressibleHydro(ReferenceOrderRHS, Physics):
         cf = (ctypes.c_double * len(coeffs))(*coeffs)
         return plan, self._precision(), vo, cf, ik2, th, tf, sp, keep
 
+    # 'auto': the fused 3D hydro step uses the divergence form of the
+    # nonlinear term (physics 2 of dd_rk4_step3d: 3 + 5 transforms per RHS
+    # instead of 6 + 3) whenever the state is solenoidal to |k.u| <= 1e-12 |k||u|
+    # (checked before every step with dd_divergence_sums), and the rotational
+    # form otherwise; both equal the reference's -(u.grad)u to roundoff on
+    # such states.  'rotational' always uses the rotational form, and so does
+    # a step captured into a CUDA graph (the check reads back to the host).
+    nonlinear_form = 'auto'
+    DIV_TOL2 = 1e-24
+
+    def _step_phys3d(self, plan, prec, sp):
+        if (self._phys3d != 0 or self.nonlinear_form != 'auto' or prec == _lib.DD_DF64
+                or torch.cuda.is_current_stream_capturing()):
+            return self._phys3d
+        buf = self._tables.get('div_sums')
+        if buf is None:
+            buf = self._tables['div_sums'] = torch.empty(2, dtype=torch.float64, device=plan.device)
+        _lib.call("dd_divergence_sums", plan.handle, sp, dptr(buf), current_stream())
+        num, den = buf.tolist()
+        return 2 if num <= self.DIV_TOL2 * den else self._phys3d
+
     def fused_rk4(self, data, dt):
         """One fused RK4 step on the device (dd_rk4_step3d) for 3D hydro / MHD;
         returns False when this physics/grid has no fused step."""
@@ -261,12 +282,14 @@ class IncompressibleHydro(ReferenceOrderRHS, Physics):
         if self._generic():
             return False
         plan, prec, vo, cf, ik2, th, tf, sp, keep = self._rk4_args(data, dt)
+        phys = self._step_phys3d(plan, prec, sp)
+        self.last_phys3d = phys
         n = ctypes.c_size_t()
-        _lib.call("dd_rhs3d_workspace_size", plan.handle, self._phys3d, prec, ctypes.byref(n))
+        _lib.call("dd_rhs3d_workspace_size", plan.handle, phys, prec, ctypes.byref(n))
         ws = self.workspace(n.value)
         pp = self._params3d()
         ppa = None if pp is None else (ctypes.c_double * len(pp))(*pp)
-        _lib.call("dd_rk4_step3d", plan.handle, self._phys3d, ppa, sp, None if ik2 is None else dptr(ik2), th, tf,
+        _lib.call("dd_rk4_step3d", plan.handle, phys, ppa, sp, None if ik2 is None else dptr(ik2), th, tf,
                   cf, vo, float(dt), prec, None, dptr(ws), ws.numel(), current_stream())
         return True
 

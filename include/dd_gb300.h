@@ -191,8 +191,11 @@ int dd_rk2mid_step2d(const dd_plan* plan, int physics, const double* params, int
 /* ------------------------------------------------------ fused 3D physics
  * physics 0 = IncompressibleHydro (state u_x, u_y, u_z; physics.py:527-599),
  * physics 1 = IncompressibleMHD (state u_x, u_y, u_z, B_x, B_y, B_z;
- * physics.py:770-819) with params = {rho0}.  Shear, rotation, tracer and
- * forcing are not implemented.  dd_rhs3d writes the dealiased RHS of every
+ * physics.py:770-819) with params = {rho0}, physics 2 = IncompressibleHydro
+ * with the nonlinear term in divergence form (five products, 3 + 5 transforms
+ * per RHS instead of 6 + 3; FP64 and FP32): equal to physics 0 to roundoff
+ * when the state is solenoidal, which the caller checks (dd_divergence_sums).
+ * Shear, rotation, tracer and forcing are not in these kernels.  dd_rhs3d writes the dealiased RHS of every
  * state component into deriv (full layout); dd_rk4_step3d advances the state
  * in place by one RK4 step (definition as for dd_hydro3d_rk4_step) with one
  * diffusivity per vector field, coeff = {nu} or {nu, eta}, and one pair of
@@ -227,6 +230,11 @@ int dd_volume_average(const dd_plan* plan, int kind, int ncomp, const void* cons
 int dd_spectrum(const dd_plan* plan, int ncomp, const void* const* comps, double norm, int nbins, const double* kbottom,
                 const double* ktop, double dk, double* out_sum, double* out_count, void* work, size_t work_bytes,
                 void* stream);
+
+/* out[0] = sum |k . u|^2, out[1] = sum |k|^2 |u|^2 over the kept modes of a
+ * 3D velocity (3 full-layout k arrays); out is device memory [2], overwritten.
+ * out[0] / out[1] is the squared relative divergence of the state. */
+int dd_divergence_sums(const dd_plan* plan, const void* const* u, double* out, void* stream);
 
 /* Sets *dflag (device int) to 1 if any of the ncomp k arrays has a non-zero
  * entry outside the kept (dealiased) modes; does not clear it. */

@@ -195,3 +195,84 @@ def test_rk4_step_matches_oracle_at_256(dd, cuda):
     dd.mods.RK4(rg).do_advance(dg, 2e-3)
     err = rel_l2(host_u(dg), [do['u'][i]['kspace'] for i in range(3)])
     assert err < 1e-12, err
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape", [(32, 32, 32), (16, 32, 64), (256, 256, 256)])
+def test_divergence_form_step_matches_oracle_and_rotational(dd, cuda, shape):
+    """A solenoidal state takes the divergence form (physics 2: 3 + 5
+    transforms per RHS); its RK4 step equals the oracle's and the rotational
+    form's to 1e-12 relative L2."""
+    u0 = dd.init_cond.turbulence_3d(shape, seed=7)
+    rg, dg = gpu_hydro(dd, shape, 5e-3, u0)
+    dd.mods.RK4(rg).do_advance(dg, 2e-3)
+    assert rg.last_phys3d == 2
+    rr, dr = gpu_hydro(dd, shape, 5e-3, u0)
+    rr.nonlinear_form = 'rotational'
+    dd.mods.RK4(rr).do_advance(dr, 2e-3)
+    assert rr.last_phys3d == 0
+    assert rel_l2(host_u(dg), host_u(dr)) < 1e-12
+    if shape[0] <= 64:
+        ro, do = oracle_hydro(shape, 5e-3, u0)
+        OT.RK4(ro).do_advance(do, 2e-3)
+        ref = [do['u'][i]['kspace'] for i in range(3)]
+        assert rel_l2(host_u(dg), ref) < 1e-12
+
+
+@pytest.mark.gpu
+def test_non_solenoidal_state_takes_the_rotational_form(dd, cuda):
+    """A state with a divergent part keeps the rotational form (equal to the
+    reference's advective form for any state) and matches the oracle."""
+    shape = (32, 32, 32)
+    rng = np.random.Generator(np.random.PCG64(8))
+    u0 = dd.init_cond.turbulence_3d(shape, seed=8)
+    kx, ky, kz = dd.kgrid.k_tables(shape, (2 * np.pi,) * 3)
+    grad = [kx[None, None, :], ky[:, None, None], kz[None, :, None]]
+    phi = np.zeros_like(u0[0])
+    phi[1:4, 1:4, 1:4] = rng.normal(size=(3, 3, 3)) * 0.05
+    u1 = [u0[i] + 1j * grad[i] * phi for i in range(3)]
+    rg, dg = gpu_hydro(dd, shape, 5e-3, u1)
+    dd.mods.RK4(rg).do_advance(dg, 2e-3)
+    assert rg.last_phys3d == 0
+    ro, do = oracle_hydro(shape, 5e-3, u1)
+    OT.RK4(ro).do_advance(do, 2e-3)
+    assert rel_l2(host_u(dg), [do['u'][i]['kspace'] for i in range(3)]) < 1e-12
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", [0, 1])
+def test_divergence_form_rhs_matches_rotational(dd, cuda, prec):
+    """dd_rhs3d physics 2 against physics 0 on a solenoidal state (FP64 to
+    1e-12, FP32 to 1e-5), and dd_divergence_sums against numpy."""
+    import ctypes
+    import torch
+    shape = (32, 32, 32)
+    u0 = dd.init_cond.turbulence_3d(shape, seed=9)
+    plan = dd.engine.get_plan(shape, (2 * np.pi,) * 3)
+    u = [torch.from_numpy(c).cuda() for c in u0]
+    up, _a = dd._lib.ptr_array([c.data_ptr() for c in u])
+    ik2 = dd.mods.IncompressibleHydro(shape, dd.mods.FourierRepresentation).inv_k2_table(plan)
+    outs = []
+    for phys in (0, 2):
+        n = ctypes.c_size_t()
+        dd._lib.call("dd_rhs3d_workspace_size", plan.handle, phys, prec, ctypes.byref(n))
+        ws = torch.empty(n.value, dtype=torch.uint8, device="cuda")
+        d = [torch.empty_like(c) for c in u]
+        dp, _b = dd._lib.ptr_array([c.data_ptr() for c in d])
+        dd._lib.call("dd_rhs3d", plan.handle, phys, None, up, dp, dd.engine.dptr(ik2), prec, 1,
+                     dd.engine.dptr(ws), ws.numel(), dd.engine.current_stream())
+        outs.append([c.cpu().numpy() for c in d])
+    assert rel_l2(outs[1], outs[0]) < (1e-12 if prec == 0 else 1e-5)
+    sums = torch.empty(2, dtype=torch.float64, device="cuda")
+    dd._lib.call("dd_divergence_sums", plan.handle, up, dd.engine.dptr(sums), dd.engine.current_stream())
+    kx, ky, kz = dd.kgrid.k_tables(shape, (2 * np.pi,) * 3)
+    K = [kx[None, None, :], ky[:, None, None], kz[None, :, None]]
+    mx, my, mz = plan.mx, plan.my, plan.mz
+    keep = ((np.abs(K[0]) <= mx) & (np.abs(K[1]) <= my) & (np.abs(K[2]) <= mz))
+    div = sum(K[i] * u0[i] for i in range(3))
+    k2 = K[0] ** 2 + K[1] ** 2 + K[2] ** 2
+    ref0 = np.sum(np.abs(div) ** 2 * keep)
+    ref1 = np.sum(k2 * sum(np.abs(c) ** 2 for c in u0) * keep)
+    got = sums.cpu().numpy()
+    assert abs(got[1] - ref1) <= 1e-12 * ref1
+    assert got[0] <= 1e-24 * ref1 and ref0 <= 1e-24 * ref1
