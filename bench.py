@@ -197,28 +197,33 @@ class Hydro3Runner:
         return [self.data[f][c].kdata for f, c in self.names]
 
     def divergence_form(self):
-        """True when the fused steps ran the divergence form (3 + 5
-        transforms per RHS; chosen per step for a solenoidal state)."""
-        return getattr(self.rhs, "last_phys3d", 0) == 2
+        """True when the fused steps ran the divergence form (hydro 3 + 5,
+        MHD 6 + 8 transforms per RHS; chosen per step for a solenoidal state)."""
+        return getattr(self.rhs, "last_phys3d", 0) in (2, 3)
 
     def transforms_per_rhs(self):
-        return 18 if self.mhd else (8 if self.divergence_form() else 9)
+        if self.mhd:
+            return 14 if self.divergence_form() else 18
+        return 8 if self.divergence_form() else 9
+
+    def canonical_transforms_per_rhs(self):
+        return 18 if self.mhd else 9
 
     def bytes_per_step(self):
         """Algorithmic bytes: every transform reads and writes one real and one
         complex field (B3), every stage reads/writes three complex passes per
-        component (C3); the divergence form's stages read two more product
+        component (C3); the divergence forms' stages read two more product
         fields."""
         sh = self.wl["shape"]
-        if self.mhd:
-            return 4 * 18 * B3s(sh) + 4 * 6 * 3 * C3s(sh)
+        nc = 6 if self.mhd else 3
         extra = 4 * 2 * C3s(sh) if self.divergence_form() else 0
-        return 4 * self.transforms_per_rhs() * B3s(sh) + 4 * 3 * 3 * C3s(sh) + extra
+        return 4 * self.transforms_per_rhs() * B3s(sh) + 4 * nc * 3 * C3s(sh) + extra
 
     def canonical_bytes_per_step(self):
-        """The rotational-form count (4 RHS x 9 transforms) for comparison."""
+        """The curl forms' count (4 RHS x 9 or 18 transforms) for comparison."""
         sh = self.wl["shape"]
-        return 4 * 9 * B3s(sh) + 4 * 3 * 3 * C3s(sh)
+        nc = 6 if self.mhd else 3
+        return 4 * self.canonical_transforms_per_rhs() * B3s(sh) + 4 * nc * 3 * C3s(sh)
 
     def point_stages(self):
         return float(np.prod(self.wl["shape"])) * 4
@@ -229,7 +234,7 @@ class Hydro3Runner:
     def _nio(self):
         g = 2 if self.mhd else 1
         if self.divergence_form():
-            return 3, 5
+            return (6, 8) if self.mhd else (3, 5)
         return 6 * g, 3 * g
 
     def kernel_flops(self, label):
@@ -240,12 +245,12 @@ class Hydro3Runner:
         Kx, Ky = Mx + 1, 2 * My + 1
         ni, no = self._nio()
         cf = lambda L: 5.0 * L * np.log2(L)
-        if label.startswith("z_inv_curl"):
+        if label.startswith("z_inv"):
             return ni * Kx * Ky * cf(Nz)
         if label.startswith("y_inv"):
             return ni * Kx * Nz * cf(Ny)
         if label.startswith("x_div"):
-            return Nz * Ny * ((ni + no) * 0.5 * cf(Nx) + Nx * 7)
+            return Nz * Ny * ((ni + no) * 0.5 * cf(Nx) + Nx * (24 if self.mhd else 7))
         if label.startswith("x_cross"):
             return Nz * Ny * ((ni + no) * 0.5 * cf(Nx) + Nx * (9 if not self.mhd else 30))
         if label.startswith("y_fwd"):
@@ -265,7 +270,7 @@ class Hydro3Runner:
         w1, w2 = Ky * Nz * Kx * cs, Nz * Ny * Kx * cs
         g = 2 if self.mhd else 1           # vector fields in the state
         ni, no = self._nio()
-        if label.startswith("z_inv_curl"):
+        if label.startswith("z_inv"):
             return 3 * g * kc + ni * w1
         if label.startswith("y_inv"):
             return ni * (w1 + w2)
@@ -288,9 +293,9 @@ class Hydro3Runner:
                                w["nu"], ", eta=%g" % w["nu"] if self.mhd else "", w["precision"]),
                 "grid": list(w["shape"]), "integrator": "RK4", "dt": w["dt"], "precision": w["precision"],
                 "parallelism": "replicas x%d" % ws, "l2": "inputs larger than L2 (state + intermediates), no flush",
-                "nonlinear_form": ("curl form (6 + 12 transforms per RHS)" if self.mhd else
-                                   "divergence form, 3 + 5 transforms per RHS (solenoidal state, checked every step)"
-                                   if self.divergence_form() else "rotational form, 6 + 3 transforms per RHS")}
+                "nonlinear_form": ("divergence form, %s transforms per RHS (solenoidal state, checked every step)"
+                                   % ("6 + 8" if self.mhd else "3 + 5") if self.divergence_form() else
+                                   "curl forms, %s transforms per RHS" % ("12 + 6" if self.mhd else "6 + 3"))}
 
     def metric(self):
         if self.mhd:
@@ -877,11 +882,12 @@ def main():
                          "combined_frac": max(t_b, t_f) / (ms_per_step / 1e3)})
         if hasattr(run, "transforms_per_rhs"):
             step_hbm["transforms_per_rhs"] = run.transforms_per_rhs()
-            if run.transforms_per_rhs() != 9 and not getattr(run, "mhd", False):
-                # the same step measured against the rotational form's 9-transform count
-                F9, B9 = F * 9 / run.transforms_per_rhs(), run.canonical_bytes_per_step()
-                step_hbm["combined_frac_vs_9_transform_count"] = max(B9 / (hbm_peak * 1e9), F9 / (P * 1e12)) / (
-                    ms_per_step / 1e3)
+            nt0 = run.canonical_transforms_per_rhs()
+            if run.transforms_per_rhs() != nt0:
+                # the same step measured against the curl forms' transform count
+                F0, B0 = F * nt0 / run.transforms_per_rhs(), run.canonical_bytes_per_step()
+                step_hbm["combined_frac_vs_%d_transform_count" % nt0] = max(
+                    B0 / (hbm_peak * 1e9), F0 / (P * 1e12)) / (ms_per_step / 1e3)
 
     # end to end through the public API: the state in from pinned host memory,
     # one step, the state back out, every step

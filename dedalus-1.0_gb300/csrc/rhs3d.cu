@@ -89,6 +89,10 @@ template <int PH>
 __device__ __forceinline__ void load_nc(const CPtrs& nc, int64_t i, double kxv, double kyv, double kzv, double2* k) {
     if constexpr (PH == P3_HYDRO_DIV) {
         div_form(nc, i, kxv, kyv, kzv, k);
+    } else if constexpr (PH == P3_MHD_DIV) {
+        div_form(nc, i, kxv, kyv, kzv, k);      // momentum from products 0..4
+#pragma unroll
+        for (int c = 3; c < 6; c++) k[c] = ((const double2*)nc.p[c + 2])[i];   // u x B
     } else {
 #pragma unroll
         for (int c = 0; c < Phys3<PH>::NO; c++) k[c] = ((const double2*)nc.p[c])[i];
@@ -101,7 +105,7 @@ __device__ __forceinline__ void rhs_at(const CPtrs& nc, int64_t i, double kxv, d
                                        double2* k) {
     load_nc<PH>(nc, i, kxv, kyv, kzv, k);
     project(k[0], k[1], k[2], kxv, kyv, kzv, s);
-    if constexpr (PH == P3_MHD) curl_k(k[3], k[4], k[5], kxv, kyv, kzv);
+    if constexpr (p3_mhd(PH)) curl_k(k[3], k[4], k[5], kxv, kyv, kzv);
 }
 
 template <int PH>
@@ -170,7 +174,7 @@ __global__ void k_rk4_stage3(RK4Args a) {
         double2 k[6];
         load_nc<PH>(a.nc, i, kxv, kyv, kzv, k);
         project_fma(k[0], k[1], k[2], kxv, kyv, kzv, s);
-        if constexpr (PH == P3_MHD) curl_k(k[3], k[4], k[5], kxv, kyv, kzv);
+        if constexpr (p3_mhd(PH)) curl_k(k[3], k[4], k[5], kxv, kyv, kzv);
         double f0[NG], f1h[NG];
 #pragma unroll
         for (int grp = 0; grp < NG; grp++) {
@@ -341,7 +345,7 @@ static int rhs3(const dd_plan* p, const double* params, const void* const* u, vo
     const Geo3& g = p->g3;
     const size_t need = work3_bytes(prec, g, P::NI, P::NO, P::NF, false);
     DD_CHECK_ARG(wb >= need, "workspace too small: %zu < %zu", wb, need);
-    const double inv_fpr = PH == P3_MHD ? inv_fpr_of(params) : 0.;
+    const double inv_fpr = p3_mhd(PH) ? inv_fpr_of(params) : 0.;
     Work3 w = make_work<PH>(g, work);
     DD_TRY(nonlinear3_any<PH>(p, prec, false, u, inv_fpr, w, st));
     ProjArgs pa{g, p->kx, p->ky, p->kz, inv_k2, inv_k2 != nullptr};
@@ -372,7 +376,7 @@ static int rk4_3(const dd_plan* p, const double* params, void* const* u, const d
     DD_CHECK_ARG(wb >= need, "workspace too small: %zu < %zu", wb, need);
     const bool intk = inv_k2 != nullptr;
     DD_CHECK_ARG(!intk || (tab_half && tab_full), "phi tables required with integer wavenumbers");
-    const double inv_fpr = PH == P3_MHD ? inv_fpr_of(params) : 0.;
+    const double inv_fpr = p3_mhd(PH) ? inv_fpr_of(params) : 0.;
     Work3 w = make_work<PH>(g, work);
     RK4Args a{};
     a.pa = ProjArgs{g, p->kx, p->ky, p->kz, inv_k2, intk};
@@ -415,10 +419,10 @@ using namespace dd;
 static int check3(const dd_plan* p, int phys, const double* params, const void* const* a, const void* const* b) {
     DD_CHECK_ARG(p, "null plan");
     DD_CHECK_ARG(p->ndim == 3, "plan is not 3D");
-    DD_CHECK_ARG(phys == P3_HYDRO || phys == P3_MHD || phys == P3_HYDRO_DIV,
-                 "physics must be 0 (hydro), 1 (MHD) or 2 (hydro, divergence form)");
-    DD_CHECK_ARG(phys != P3_MHD || (params && params[0] > 0.), "MHD needs params = {rho0 > 0}");
-    const int nf = phys == P3_MHD ? 6 : 3;
+    DD_CHECK_ARG(phys >= P3_HYDRO && phys <= P3_MHD_DIV,
+                 "physics must be 0 (hydro), 1 (MHD), 2 (hydro, divergence form) or 3 (MHD, divergence form)");
+    DD_CHECK_ARG(!p3_mhd(phys) || (params && params[0] > 0.), "MHD needs params = {rho0 > 0}");
+    const int nf = p3_mhd(phys) ? 6 : 3;
     DD_CHECK_ARG(a, "null field array");
     for (int c = 0; c < nf; c++) {
         DD_CHECK_ARG(a[c], "null field pointer %d", c);
@@ -431,12 +435,13 @@ extern "C" {
 
 int dd_rhs3d_workspace_size(const dd_plan* p, int physics, int precision, size_t* bytes) {
     DD_CHECK_ARG(p && bytes && p->ndim == 3, "dd_rhs3d_workspace_size: bad arguments");
-    DD_CHECK_ARG(physics == P3_HYDRO || physics == P3_MHD || physics == P3_HYDRO_DIV,
-                 "physics must be 0 (hydro), 1 (MHD) or 2 (hydro, divergence form)");
+    DD_CHECK_ARG(physics >= P3_HYDRO && physics <= P3_MHD_DIV,
+                 "physics must be 0 (hydro), 1 (MHD), 2 (hydro, divergence form) or 3 (MHD, divergence form)");
     DD_CHECK_ARG(precision >= DD_FP64 && precision <= DD_DF64, "bad precision");
     if (physics == P3_HYDRO) *bytes = work3_bytes(precision, p->g3, 6, 3, 3, true);
     else if (physics == P3_MHD) *bytes = work3_bytes(precision, p->g3, 12, 6, 6, true);
-    else *bytes = work3_bytes(precision, p->g3, 5, 5, 3, true);
+    else if (physics == P3_HYDRO_DIV) *bytes = work3_bytes(precision, p->g3, 5, 5, 3, true);
+    else *bytes = work3_bytes(precision, p->g3, 8, 8, 6, true);
     return DD_OK;
 }
 
@@ -450,6 +455,8 @@ int dd_rhs3d(const dd_plan* p, int physics, const double* params, const void* co
         return rhs3<P3_HYDRO>(p, params, state, deriv, inv_k2, precision, zero_nonkept, work, work_bytes, st);
     if (physics == P3_HYDRO_DIV)
         return rhs3<P3_HYDRO_DIV>(p, params, state, deriv, inv_k2, precision, zero_nonkept, work, work_bytes, st);
+    if (physics == P3_MHD_DIV)
+        return rhs3<P3_MHD_DIV>(p, params, state, deriv, inv_k2, precision, zero_nonkept, work, work_bytes, st);
     return rhs3<P3_MHD>(p, params, state, deriv, inv_k2, precision, zero_nonkept, work, work_bytes, st);
 }
 
@@ -468,6 +475,9 @@ int dd_rk4_step3d(const dd_plan* p, int physics, const double* params, void* con
     if (physics == P3_HYDRO_DIV)
         return rk4_3<P3_HYDRO_DIV>(p, params, state, inv_k2, tab_half, tab_full, coeff, viscosity_order, dt,
                                    precision, nonkept_flag, work, work_bytes, st);
+    if (physics == P3_MHD_DIV)
+        return rk4_3<P3_MHD_DIV>(p, params, state, inv_k2, tab_half, tab_full, coeff, viscosity_order, dt,
+                                 precision, nonkept_flag, work, work_bytes, st);
     return rk4_3<P3_MHD>(p, params, state, inv_k2, tab_half, tab_full, coeff, viscosity_order, dt, precision,
                          nonkept_flag, work, work_bytes, st);
 }

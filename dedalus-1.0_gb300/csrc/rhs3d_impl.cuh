@@ -28,11 +28,14 @@ namespace dd {
 // P3_HYDRO_DIV: hydro with the nonlinear term in divergence form, valid for a
 // solenoidal state (below).  NI = transform buffers, NINV = inverse-transformed
 // fields, NO = forward-transformed products.
-enum { P3_HYDRO = 0, P3_MHD = 1, P3_HYDRO_DIV = 2 };
+enum { P3_HYDRO = 0, P3_MHD = 1, P3_HYDRO_DIV = 2, P3_MHD_DIV = 3 };
 template <int PH> struct Phys3;
 template <> struct Phys3<P3_HYDRO>     { static constexpr int NG = 1, NF = 3, NI = 6, NINV = 6, NO = 3; };
 template <> struct Phys3<P3_MHD>       { static constexpr int NG = 2, NF = 6, NI = 12, NINV = 12, NO = 6; };
 template <> struct Phys3<P3_HYDRO_DIV> { static constexpr int NG = 1, NF = 3, NI = 5, NINV = 3, NO = 5; };
+template <> struct Phys3<P3_MHD_DIV>   { static constexpr int NG = 2, NF = 6, NI = 8, NINV = 6, NO = 8; };
+__host__ __device__ constexpr bool p3_curl_inputs(int ph) { return ph == P3_HYDRO || ph == P3_MHD; }
+__host__ __device__ constexpr bool p3_mhd(int ph) { return ph == P3_MHD || ph == P3_MHD_DIV; }
 static_assert(Phys3<P3_MHD>::NI <= DD_MAXF, "too many transform fields for Ptrs");
 
 // a * (1j * k) as numpy computes it (representations.py:423)
@@ -44,10 +47,10 @@ __device__ __forceinline__ double2 ideriv(double2 a, double k) { return make_dou
 // physics.py:394-396: (d_y X_z - d_z X_y, d_z X_x - d_x X_z, d_x X_y - d_y X_x)).
 // The state is read from the full reference layout [ky][kz][kx] or from the
 // compact kept layout [kyc][kzc][kx] used for RK stage states.
-template <typename T, bool COMPACT, int NG>
+template <typename T, bool COMPACT, int NG, bool CURL = true>
 struct OpZInvCurl3 {
     using V = typename Vec2<T>::type;
-    static constexpr const char* name = NG == 1 ? "z_inv_curl" : "z_inv_curl_mhd";
+    static constexpr const char* name = NG == 1 ? "z_inv_curl" : (CURL ? "z_inv_curl_mhd" : "z_inv_mhd");
     static constexpr int lmin = 16, lmax = 512;
     Geo3 g; CPtrs u; Ptrs out; const V* tw;
     const double* kx; const double* ky; const double* kz;
@@ -61,6 +64,10 @@ struct OpZInvCurl3 {
     __device__ C<T> load(int fld, int kyc, int e, int ix) const {
         if (!kept_full(e, g.Nz, g.Mz)) return zero<T>();
         const int ky_i = compact_to_full(kyc, g.Ny, g.Ky);
+        if constexpr (!CURL) {     // state components only (fld = component)
+            const double2 v = get(fld, kyc, ky_i, e, ix);
+            return mk<T>((T)v.x, (T)v.y);
+        }
         const int grp = fld / 6, j = fld % 6, c0 = 3 * grp;
         double2 r;
         if (j < 3) {
@@ -132,6 +139,30 @@ struct ProdDiv3 {
     }
 };
 
+// MHD in divergence form, for solenoidal u and B: the momentum products
+// M = u u^T - B B^T / (4 pi rho0) (J x B = (B.grad)B - grad(B^2/2) and
+// (B.grad)B = d_j(B_i B_j) when div B = 0) in Basdevant's five entries, and the
+// induction products u x B (its curl needs no divergence assumption).
+// in: u, B;  out: Mxx - Mzz, Myy - Mzz, Mxy, Mxz, Myz, (u x B)_x, _y, _z.
+template <typename T>
+struct ProdMHDDiv3 {
+    static constexpr int NI = 6, NO = 8;
+    static constexpr int lmin = 16, lmax = 512;
+    T inv_fpr;
+    __device__ void operator()(const T* in, T* out, int) const {
+        const T ux = in[0], uy = in[1], uz = in[2], bx = in[3], by = in[4], bz = in[5];
+        const T mzz = uz * uz - bz * bz * inv_fpr;
+        out[0] = (ux * ux - bx * bx * inv_fpr) - mzz;
+        out[1] = (uy * uy - by * by * inv_fpr) - mzz;
+        out[2] = ux * uy - bx * by * inv_fpr;
+        out[3] = ux * uz - bx * bz * inv_fpr;
+        out[4] = uy * uz - by * bz * inv_fpr;
+        out[5] = uy * bz - uz * by;
+        out[6] = uz * bx - ux * bz;
+        out[7] = ux * by - uy * bx;
+    }
+};
+
 // ------------------------------------------------------------------ pass 5
 template <typename T>
 struct OpZFwdCompact3 {
@@ -194,7 +225,7 @@ int nonlinear3(const dd_plan* pl, const void* const* u, double inv_fpr, const Wo
         w1.p[f] = w.W1<T>(f); w1c.p[f] = w1.p[f];
         w2.p[f] = w.W2<T>(f); w2c.p[f] = w2.p[f];
     }
-    OpZInvCurl3<T, COMPACT, P::NG> a{g, uin, w1, TwSel<T>::z(pl), pl->kx, pl->ky, pl->kz};
+    OpZInvCurl3<T, COMPACT, P::NG, p3_curl_inputs(PH)> a{g, uin, w1, TwSel<T>::z(pl), pl->kx, pl->ky, pl->kz};
     DD_TRY((launch_pass_len<T, true, false, false>(g.Nz, a, g.Kx, g.Ky, P::NINV, st)));
     OpYInv3<T> b{g, w1c, w2, TwSel<T>::y(pl)};
     DD_TRY((launch_pass_len<T, true, false, false>(g.Ny, b, g.Kx, g.Nz, P::NINV, st)));
@@ -202,6 +233,9 @@ int nonlinear3(const dd_plan* pl, const void* const* u, double inv_fpr, const Wo
     if constexpr (PH == P3_HYDRO_DIV) {
         DD_TRY((launch_x_prod_len<T>("x_div", g.Nx, g.Nz * g.Ny, g.Kx, w2c, w2, 1, 0, 0, TwSel<T>::x(pl),
                                      (T)pl->inv_n, ProdDiv3<T>{}, st)));
+    } else if constexpr (PH == P3_MHD_DIV) {
+        DD_TRY((launch_x_prod_len<T>("x_div_mhd", g.Nx, g.Nz * g.Ny, g.Kx, w2c, w2, 1, 0, 0, TwSel<T>::x(pl),
+                                     (T)pl->inv_n, ProdMHDDiv3<T>{(T)inv_fpr}, st)));
     } else if constexpr (PH == P3_HYDRO) {
         DD_TRY((launch_x_prod_len<T>("x_cross", g.Nx, g.Nz * g.Ny, g.Kx, w2c, w2, 1, 0, 0, TwSel<T>::x(pl),
                                      (T)pl->inv_n, ProdHydro3<T>{}, st)));
@@ -224,6 +258,6 @@ int nonlinear3(const dd_plan* pl, const void* const* u, double inv_fpr, const Wo
     EXT template int nonlinear3<T, true, PH>(const dd_plan*, const void* const*, double, const Work3&,      \
                                              cudaStream_t);
 #define DD_RHS3D_INSTANTIATE(EXT, T) DD_RHS3D_INSTANTIATE_PH(EXT, T, P3_HYDRO) DD_RHS3D_INSTANTIATE_PH(EXT, T, P3_MHD) \
-    DD_RHS3D_INSTANTIATE_PH(EXT, T, P3_HYDRO_DIV)
+    DD_RHS3D_INSTANTIATE_PH(EXT, T, P3_HYDRO_DIV) DD_RHS3D_INSTANTIATE_PH(EXT, T, P3_MHD_DIV)
 
 }  // namespace dd

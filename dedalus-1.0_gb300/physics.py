@@ -253,26 +253,36 @@ class IncompressibleHydro(ReferenceOrderRHS, Physics):
         cf = (ctypes.c_double * len(coeffs))(*coeffs)
         return plan, self._precision(), vo, cf, ik2, th, tf, sp, keep
 
-    # 'auto': the fused 3D hydro step uses the divergence form of the
-    # nonlinear term (physics 2 of dd_rk4_step3d: 3 + 5 transforms per RHS
-    # instead of 6 + 3) whenever the state is solenoidal to |k.u| <= 1e-12 |k||u|
-    # (checked before every step with dd_divergence_sums), and the rotational
-    # form otherwise; both equal the reference's -(u.grad)u to roundoff on
-    # such states.  'rotational' always uses the rotational form, and so does
+    # 'auto': the fused 3D step uses the divergence form of the nonlinear
+    # terms (dd_rk4_step3d physics 2 for hydro: 3 + 5 transforms per RHS
+    # instead of 6 + 3; physics 3 for MHD: 6 + 8 instead of 12 + 6) whenever
+    # every vector field of the state is solenoidal to |k.u| <= 1e-12 |k||u|
+    # (checked before every step with dd_divergence_sums), and the curl forms
+    # otherwise; both equal the reference's terms to roundoff on such states.  'rotational' always uses the rotational form, and so does
     # a step captured into a CUDA graph (the check reads back to the host).
     nonlinear_form = 'auto'
     DIV_TOL2 = 1e-24
 
     def _step_phys3d(self, plan, prec, sp):
-        if (self._phys3d != 0 or self.nonlinear_form != 'auto' or prec == _lib.DD_DF64
+        """Physics code of dd_rk4_step3d for this step: the divergence form
+        (hydro 0 -> 2, MHD 1 -> 3) when every vector field of the state is
+        solenoidal to the tolerance."""
+        if (self._phys3d not in (0, 1) or self.nonlinear_form != 'auto' or prec == _lib.DD_DF64
                 or torch.cuda.is_current_stream_capturing()):
             return self._phys3d
+        ngroups = len(self._groups3d())
         buf = self._tables.get('div_sums')
-        if buf is None:
-            buf = self._tables['div_sums'] = torch.empty(2, dtype=torch.float64, device=plan.device)
-        _lib.call("dd_divergence_sums", plan.handle, sp, dptr(buf), current_stream())
-        num, den = buf.tolist()
-        return 2 if num <= self.DIV_TOL2 * den else self._phys3d
+        if buf is None or buf.numel() < 2 * ngroups:
+            buf = self._tables['div_sums'] = torch.empty(2 * ngroups, dtype=torch.float64, device=plan.device)
+        base = ctypes.cast(sp, ctypes.c_void_p).value      # the pointer array (kept alive by the caller)
+        for g in range(ngroups):
+            gp = ctypes.cast(ctypes.c_void_p(base + 3 * g * ctypes.sizeof(ctypes.c_void_p)),
+                             ctypes.POINTER(ctypes.c_void_p))
+            _lib.call("dd_divergence_sums", plan.handle, gp, ctypes.c_void_p(buf.data_ptr() + 16 * g),
+                      current_stream())
+        v = buf.tolist()
+        ok = all(v[2 * g] <= self.DIV_TOL2 * v[2 * g + 1] for g in range(ngroups))
+        return self._phys3d + 2 if ok else self._phys3d
 
     def fused_rk4(self, data, dt):
         """One fused RK4 step on the device (dd_rk4_step3d) for 3D hydro / MHD;

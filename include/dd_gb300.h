@@ -194,7 +194,11 @@ int dd_rk2mid_step2d(const dd_plan* plan, int physics, const double* params, int
  * physics.py:770-819) with params = {rho0}, physics 2 = IncompressibleHydro
  * with the nonlinear term in divergence form (five products, 3 + 5 transforms
  * per RHS instead of 6 + 3; FP64 and FP32): equal to physics 0 to roundoff
- * when the state is solenoidal, which the caller checks (dd_divergence_sums).
+ * when the state is solenoidal, which the caller checks (dd_divergence_sums);
+ * physics 3 = IncompressibleMHD with the momentum term in divergence form
+ * (five products of u u - B B / (4 pi rho0)) and the induction products u x B,
+ * 6 + 8 transforms per RHS instead of 12 + 6: equal to physics 1 to roundoff
+ * when u and B are solenoidal.
  * Shear, rotation, tracer and forcing are not in these kernels.  dd_rhs3d writes the dealiased RHS of every
  * state component into deriv (full layout); dd_rk4_step3d advances the state
  * in place by one RK4 step (definition as for dd_hydro3d_rk4_step) with one

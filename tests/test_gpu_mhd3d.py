@@ -121,3 +121,53 @@ def test_alfven_wave_known_answer(dd, cuda):
         assert abs(got - want) < 1e-6 * abs(hostU[c][idx]) + 1e-14, (c, got, want)
         gotb = data['B'][c].to_numpy('kspace')[idx]
         assert abs(gotb - hostB[c][idx] * phase) < 1e-6 * abs(hostB[c][idx]) + 1e-14
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape,rho0", [((32, 32, 32), 1.0), ((16, 32, 64), 2.5), ((256, 256, 256), 1.0)])
+def test_mhd_divergence_form_step(dd, cuda, shape, rho0):
+    """Solenoidal u and B take the divergence form (physics 3: 6 + 8
+    transforms per RHS); two RK4 steps equal the curl form's and the oracle's
+    to 1e-12 relative L2."""
+    params = {'nu': 5e-3, 'eta': 5e-3, 'rho0': rho0}
+    comps = fields(dd, shape, 5)
+    M = dd.mods
+    runs = []
+    for form in ('auto', 'rotational'):
+        rg = M.IncompressibleMHD(shape, M.FourierRepresentation)
+        rg.parameters.update(params)
+        rg.nonlinear_form = form
+        dg = rg.create_fields(0.)
+        for (f, c), a in zip(NAMES, comps):
+            dg[f][c]['kspace'] = a
+        ti = M.RK4(rg)
+        for _ in range(2):
+            ti.do_advance(dg, 1e-3)
+        runs.append((rg.last_phys3d, host(dg, True)))
+    assert runs[0][0] == 3 and runs[1][0] == 1
+    assert rel_l2(runs[0][1], runs[1][1]) < 1e-12
+    if shape[0] <= 64:
+        ro, do, _rg, _dg = setup(dd, shape, params, comps)
+        to = OT.RK4(ro)
+        for _ in range(2):
+            to.do_advance(do, 1e-3)
+        assert rel_l2(runs[0][1], host(do, False)) < 1e-12
+
+
+@pytest.mark.gpu
+def test_mhd_divergent_field_takes_the_curl_form(dd, cuda):
+    """A magnetic field with a divergent part keeps the curl forms (which the
+    reference computes for any field) and matches the oracle."""
+    shape = (32, 32, 32)
+    comps = fields(dd, shape, 6)
+    kx, ky, kz = dd.kgrid.k_tables(shape, (2 * np.pi,) * 3)
+    grad = [kx[None, None, :], ky[:, None, None], kz[None, :, None]]
+    phi = np.zeros_like(comps[0])
+    phi[1:3, 1:3, 1:3] = 0.05
+    comps = comps[:3] + [comps[3 + i] + 1j * grad[i] * phi for i in range(3)]
+    params = {'nu': 5e-3, 'eta': 5e-3, 'rho0': 1.0}
+    ro, do, rg, dg = setup(dd, shape, params, comps)
+    dd.mods.RK4(rg).do_advance(dg, 1e-3)
+    OT.RK4(ro).do_advance(do, 1e-3)
+    assert rg.last_phys3d == 1
+    assert rel_l2(host(dg, True), host(do, False)) < 1e-12
