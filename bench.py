@@ -119,7 +119,7 @@ def bytes_2d(label, runs, cs, ni, no, nf):
         M = (N - 1) // 3
         Kx, Ky = M + 1, 2 * M + 1
         w, kc = N * Kx * cs, Kx * Ky * 16
-        if label.startswith("x_prod"):
+        if label.startswith("x_prod") or label.startswith("x_div"):
             b = (ni + no) * w
         elif label.startswith("y_inv"):
             b = nf * kc + ni * w
@@ -406,11 +406,16 @@ class EnsembleRunner:
         return float(self.ens.grid_point_stages())
 
     def flops_per_step(self):
-        return sum(2 * 8 * fft_flops((n, n)) for n in self.sizes)
+        return sum(2 * self.ens.transforms_per_rhs(n) * fft_flops((n, n)) for n in self.sizes)
 
     def kernel_bytes(self, label):
         cs = 16 if self.wl["precision"] == "fp64" else 8
-        return bytes_2d(label, {n: self.sizes.count(n) for n in self.wl["sizes"]}, cs, 5, 3, 3)
+        div = all(c.phys == 3 for c in self.ens.classes)     # divergence form: 3 inverse, 4 forward fields
+        ni, no = (3, 4) if div else (5, 3)
+        b = bytes_2d(label, {n: self.sizes.count(n) for n in self.wl["sizes"]}, cs, ni, no, 3)
+        if b is not None and label.startswith("rk2mid_stage2d") and div:
+            b *= 16.0 / 15.0                                  # one more product field read per stage
+        return b
 
     def config(self, ws):
         w = self.wl
@@ -419,7 +424,9 @@ class EnsembleRunner:
                             "N^2=1, RK2mid, dt=%g, %s, one CUDA graph per ensemble step"
                             % (w["nrun"], list(w["sizes"]), counts, w["nu"], w["dt"], w["precision"]),
                 "runs_per_size": counts, "schedule": self.sched, "dt": w["dt"], "precision": w["precision"],
-                "parallelism": "replicas x%d" % ws, "l2": "ensemble state (> 1 GB) larger than L2, no flush"}
+                "parallelism": "replicas x%d" % ws, "l2": "ensemble state (> 1 GB) larger than L2, no flush",
+                "nonlinear_form": "divergence form, 3 + 4 transforms per RHS (solenoidal u, checked at capture)"
+                if all(c.phys == 3 for c in self.ens.classes) else "curl form, 5 + 3 transforms per RHS"}
 
     def metric(self):
         return "512-run 2D Boussinesq ensemble steps/s", "ensemble steps/s"

@@ -79,6 +79,7 @@ SIGNATURES = {
     "dd_les_band": [P, I, PP, D, D, P],
     "dd_les_transfer": [P, PP, PP, I, P, P, SZ, P],
     "dd_divergence_sums": [P, PP, P, P],
+    "dd_divergence_sums2d": [P, I, P, P, I64, P, P],
     "dd_shear_workspace_size": [P, I, ctypes.POINTER(SZ)],
     "dd_shear_r2c": [P, I, PP, PP, P, D, P, D, P, SZ, P],
     "dd_shear_c2r": [P, I, PP, PP, P, D, P, D, P, SZ, P],

@@ -62,7 +62,7 @@ __device__ __forceinline__ void phis2(const Stage2Args& a, int c, int q, double 
 // One thread per kept entry of every run.  NF (2 hydro, 3 Boussinesq) and
 // MODE (0 = write deriv, 1 = RK2mid stage 1, 2 = stage 2) are template
 // parameters so that the per-field loop unrolls with static indices.
-template <int NF, int MODE>
+template <int NF, int MODE, bool DIV>
 __global__ void k_stage2(Stage2Args a) {
     const Geo2& g = a.g;
     const int per = g.Kx * g.Ky;
@@ -80,8 +80,17 @@ __global__ void k_stage2(Stage2Args a) {
         if (a.intk && a.inv_k2) s = a.inv_k2[q];
         else s = rdiv(1., k2 == 0. ? 1. : k2);
         double2 N[NF];
-        N[0] = ((const double2*)a.nc.p[0])[run * a.nc_rs + j];
-        N[1] = ((const double2*)a.nc.p[1])[run * a.nc_rs + j];
+        const int64_t ni = run * a.nc_rs + j;
+        if constexpr (DIV) {
+            // N = -i k_j T_ij with T_xx = u_x^2 - u_y^2, T_xy = u_x u_y, T_yy = 0; -i s = (s.y, -s.x)
+            const double2 p0 = ((const double2*)a.nc.p[0])[ni], p1 = ((const double2*)a.nc.p[1])[ni];
+            const double sxr = fma(kyv, p1.x, kxv * p0.x), sxi = fma(kyv, p1.y, kxv * p0.y);
+            N[0] = make_double2(sxi, -sxr);
+            N[1] = make_double2(kxv * p1.y, -(kxv * p1.x));
+        } else {
+            N[0] = ((const double2*)a.nc.p[0])[ni];
+            N[1] = ((const double2*)a.nc.p[1])[ni];
+        }
         if constexpr (NF == 3) {
             const int64_t ri = a.rin_compact ? run * a.rin_rs + j : run * a.rin_rs + (int64_t)ix * g.Ny + ky_i;
             const double2 T = ((const double2*)a.rin.p[2])[ri];
@@ -90,8 +99,16 @@ __global__ void k_stage2(Stage2Args a) {
             const double2 b = make_double2(rmul(rmul(T.x, a.pp.g), a.pp.alpha_t), rmul(rmul(T.y, a.pp.g), a.pp.alpha_t));
             if (a.pp.dir == 0) N[0] = make_double2(radd(N[0].x, b.x), radd(N[0].y, b.y));
             else N[1] = make_double2(radd(N[1].x, b.x), radd(N[1].y, b.y));
-            // temperature: (-(u.grad T)) - (u_dir * beta) (physics.py:702-708)
-            const double2 adv = ((const double2*)a.nc.p[2])[run * a.nc_rs + j];
+            // temperature: (-(u.grad T)) - (u_dir * beta) (physics.py:702-708); in divergence
+            // form u.grad T = i k . (u T)^, i s = (-s.y, s.x)
+            double2 adv;
+            if constexpr (DIV) {
+                const double2 fx = ((const double2*)a.nc.p[2])[ni], fy = ((const double2*)a.nc.p[3])[ni];
+                const double sr = fma(kyv, fy.x, kxv * fx.x), si = fma(kyv, fy.y, kxv * fx.y);
+                adv = make_double2(-si, sr);
+            } else {
+                adv = ((const double2*)a.nc.p[2])[ni];
+            }
             N[2] = make_double2(rsub(-adv.x, rmul(ud.x, a.pp.beta)), rsub(-adv.y, rmul(ud.y, a.pp.beta)));
         }
         if constexpr (MODE == 0) project2(N[0], N[1], kxv, kyv, s);
@@ -120,8 +137,10 @@ __global__ void k_stage2(Stage2Args a) {
 
 template <int MODE>
 static int launch_stage2(const Stage2Args& a, unsigned nb, const char* label, cudaStream_t st) {
-    if (a.phys == PHYS_HYDRO) DD_KT(label, st, k_stage2<2, MODE><<<nb, 256, 0, st>>>(a));
-    else DD_KT(label, st, k_stage2<3, MODE><<<nb, 256, 0, st>>>(a));
+    if (a.phys == PHYS_HYDRO) DD_KT(label, st, k_stage2<2, MODE, false><<<nb, 256, 0, st>>>(a));
+    else if (a.phys == PHYS_BOUSS) DD_KT(label, st, k_stage2<3, MODE, false><<<nb, 256, 0, st>>>(a));
+    else if (a.phys == PHYS_HYDRO_DIV) DD_KT(label, st, k_stage2<2, MODE, true><<<nb, 256, 0, st>>>(a));
+    else DD_KT(label, st, k_stage2<3, MODE, true><<<nb, 256, 0, st>>>(a));
     DD_LAUNCH_CHECK();
     return DD_OK;
 }
@@ -160,6 +179,36 @@ __global__ void k_zero_nonkept2_all(Geo2 g, Ptrs k, int64_t rs, int nrun) {
     }
 }
 
+// Sums over the kept modes of nrun 2D velocities (run r at offset r * rs):
+// out[0] += |k . u|^2, out[1] += |k|^2 |u|^2 (block partials, one atomic per block).
+__global__ void __launch_bounds__(256) k_div_sums2(Geo2 g, const double* kx, const double* ky, const double2* ux,
+                                                    const double2* uy, int64_t rs, int nrun, double* out) {
+    __shared__ double r0[256], r1[256];
+    const int per = g.Kx * g.Ky;
+    const int64_t n = (int64_t)per * nrun;
+    double s0 = 0., s1 = 0.;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int run = (int)(i / per);
+        const int j = (int)(i - (int64_t)run * per);
+        const int kyc = j % g.Ky, ix = j / g.Ky;
+        const int ky_i = compact_to_full(kyc, g.Ny, g.Ky);
+        const int64_t o = run * rs + (int64_t)ix * g.Ny + ky_i;
+        const double a = kx[ix], b = ky[ky_i];
+        const double2 u = ux[o], v = uy[o];
+        const double dr = a * u.x + b * v.x, di = a * u.y + b * v.y;
+        s0 += dr * dr + di * di;
+        s1 += (a * a + b * b) * (u.x * u.x + u.y * u.y + v.x * v.x + v.y * v.y);
+    }
+    r0[threadIdx.x] = s0;
+    r1[threadIdx.x] = s1;
+    __syncthreads();
+    for (int h = 128; h > 0; h >>= 1) {
+        if (threadIdx.x < h) { r0[threadIdx.x] += r0[threadIdx.x + h]; r1[threadIdx.x] += r1[threadIdx.x + h]; }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) { atomicAdd(out, r0[0]); atomicAdd(out + 1, r1[0]); }
+}
+
 static unsigned ew_grid2(int64_t n) {
     int64_t b = (n + 255) / 256;
     if (b > 152 * 16) b = 152 * 16;
@@ -186,6 +235,8 @@ static size_t work2_bytes(int prec, const Geo2& g, int nrun) {
 static int nonlinear2_phys(int phys, const dd_plan* pl, int prec, bool compact, const Work2& w,
                            const void* const* st, int64_t st_rs, cudaStream_t s) {
     if (phys == PHYS_HYDRO) return nonlinear2_any<PHYS_HYDRO>(pl, prec, compact, w, st, st_rs, s);
+    if (phys == PHYS_HYDRO_DIV) return nonlinear2_any<PHYS_HYDRO_DIV>(pl, prec, compact, w, st, st_rs, s);
+    if (phys == PHYS_BOUSS_DIV) return nonlinear2_any<PHYS_BOUSS_DIV>(pl, prec, compact, w, st, st_rs, s);
     return nonlinear2_any<PHYS_BOUSS>(pl, prec, compact, w, st, st_rs, s);
 }
 
@@ -194,7 +245,7 @@ static void fill_common(Stage2Args& a, const dd_plan* p, int phys, const double*
     a.g = p->g2; a.kx = p->kx; a.ky = p->ky; a.inv_k2 = inv_k2; a.intk = inv_k2 != nullptr;
     a.phys = phys; a.nrun = nrun;
     if (pp) { a.pp.g = pp[0]; a.pp.alpha_t = pp[1]; a.pp.beta = pp[2]; a.pp.dir = (int)pp[3]; }
-    const int no = phys == PHYS_HYDRO ? 2 : 3;
+    const int no = phys == PHYS_HYDRO || phys == PHYS_HYDRO_DIV ? 2 : (phys == PHYS_BOUSS ? 3 : 4);
     for (int f = 0; f < no; f++)
         DD_PREC_DISPATCH(prec, T, a.nc.p[f] = (void*)w.NC<T>(f));
     a.nc_rs = (int64_t)w.kc; a.c_rs = (int64_t)w.kc;
@@ -202,9 +253,10 @@ static void fill_common(Stage2Args& a, const dd_plan* p, int phys, const double*
 
 static int check2(const dd_plan* p, int phys, int nrun, const double* pp) {
     DD_CHECK_ARG(p && p->ndim == 2, "plan must be 2D");
-    DD_CHECK_ARG(phys == PHYS_HYDRO || phys == PHYS_BOUSS, "physics must be 0 (hydro) or 1 (Boussinesq)");
+    DD_CHECK_ARG(phys >= PHYS_HYDRO && phys <= PHYS_BOUSS_DIV,
+                 "physics must be 0 (hydro), 1 (Boussinesq), 2 or 3 (the same in divergence form)");
     DD_CHECK_ARG(nrun >= 1 && nrun <= 65535, "nrun must be in [1, 65535]");
-    if (phys == PHYS_BOUSS) {
+    if (p2_bouss(phys)) {
         DD_CHECK_ARG(pp, "Boussinesq parameters required");
         DD_CHECK_ARG(pp[3] == 0. || pp[3] == 1., "boussinesq direction must be 0 (x) or 1 (y) in 2D");
     }
@@ -229,7 +281,7 @@ int dd_rhs2d(const dd_plan* p, int phys, const double* params, int nrun, const v
              size_t work_bytes, void* stream) {
     DD_TRY(check2(p, phys, nrun, params));
     DD_CHECK_ARG(state && deriv && work, "dd_rhs2d: null pointer");
-    const int nf = phys == PHYS_HYDRO ? 2 : 3;
+    const int nf = p2_bouss(phys) ? 3 : 2;
     for (int c = 0; c < nf; c++) DD_CHECK_ARG(state[c] && deriv[c], "dd_rhs2d: null field pointer %d", c);
     DD_CHECK_ARG(precision >= DD_FP64 && precision <= DD_DF64, "bad precision");
     const size_t need = work2_bytes(precision, p->g2, nrun);
@@ -258,7 +310,7 @@ int dd_rk2mid_step2d(const dd_plan* p, int phys, const double* params, int nrun,
     DD_TRY(check2(p, phys, nrun, params));
     DD_CHECK_ARG(state && work && nu, "dd_rk2mid_step2d: null pointer");
     DD_CHECK_ARG(viscosity_order >= 1, "viscosity_order must be >= 1");
-    const int nf = phys == PHYS_HYDRO ? 2 : 3;
+    const int nf = p2_bouss(phys) ? 3 : 2;
     for (int c = 0; c < nf; c++) DD_CHECK_ARG(state[c], "dd_rk2mid_step2d: null field pointer %d", c);
     DD_CHECK_ARG(precision >= DD_FP64 && precision <= DD_DF64, "bad precision");
     const bool intk = inv_k2 != nullptr;
@@ -293,6 +345,21 @@ int dd_rk2mid_step2d(const dd_plan* p, int phys, const double* params, int nrun,
                                         p->g2, a.y, state_rs, nf, nrun, p->kx, p->ky, a));
         DD_LAUNCH_CHECK();
     }
+    return DD_OK;
+}
+
+int dd_divergence_sums2d(const dd_plan* p, int nrun, const void* ux, const void* uy, int64_t run_stride, double* out,
+                         void* stream) {
+    DD_CHECK_ARG(p && p->ndim == 2, "dd_divergence_sums2d: plan must be 2D");
+    DD_CHECK_ARG(ux && uy && out && nrun >= 1, "dd_divergence_sums2d: bad arguments");
+    cudaStream_t st = (cudaStream_t)stream;
+    DD_CUDA(cudaMemsetAsync(out, 0, 2 * sizeof(double), st));
+    const Geo2& g = p->g2;
+    const int64_t n = (int64_t)g.Kx * g.Ky * nrun;
+    const unsigned nb = (unsigned)std::min<int64_t>((n + 255) / 256, 152 * 4);
+    DD_KT("div_sums2", st, k_div_sums2<<<nb, 256, 0, st>>>(g, p->kx, p->ky, (const double2*)ux, (const double2*)uy,
+                                                          run_stride, nrun, out));
+    DD_LAUNCH_CHECK();
     return DD_OK;
 }
 

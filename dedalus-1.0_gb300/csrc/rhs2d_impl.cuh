@@ -24,18 +24,29 @@ namespace dd {
 
 __device__ __forceinline__ double2 ideriv2(double2 a, double k) { return make_double2(-(a.y * k), a.x * k); }
 
-enum { PHYS_HYDRO = 0, PHYS_BOUSS = 1 };
+// PHYS_*_DIV: the same physics with the nonlinear terms in divergence form,
+// valid for a solenoidal u: -(u.grad)u = -d_j (u_i u_j) and u.grad T =
+// div(u T).  Basdevant's trick leaves two momentum products (u_x^2 - u_y^2,
+// u_x u_y; the dropped u_y^2 I is a gradient the projection removes) and two
+// temperature fluxes (u_x T, u_y T): 2 or 3 inverse transforms (u, T) and 2 or
+// 4 forward ones per RHS instead of 3 + 2 (hydro) and 5 + 3 (Boussinesq).
+enum { PHYS_HYDRO = 0, PHYS_BOUSS = 1, PHYS_HYDRO_DIV = 2, PHYS_BOUSS_DIV = 3 };
+__host__ __device__ constexpr bool p2_div(int ph) { return ph == PHYS_HYDRO_DIV || ph == PHYS_BOUSS_DIV; }
+__host__ __device__ constexpr bool p2_bouss(int ph) { return ph == PHYS_BOUSS || ph == PHYS_BOUSS_DIV; }
 
 template <int PHYS> struct Phys2;
 template <> struct Phys2<PHYS_HYDRO> { static constexpr int NF = 2, NI = 3, NO = 2; };
 template <> struct Phys2<PHYS_BOUSS> { static constexpr int NF = 3, NI = 5, NO = 3; };
+template <> struct Phys2<PHYS_HYDRO_DIV> { static constexpr int NF = 2, NI = 2, NO = 2; };
+template <> struct Phys2<PHYS_BOUSS_DIV> { static constexpr int NF = 3, NI = 3, NO = 4; };
 static_assert(Phys2<PHYS_BOUSS>::NI <= DD_MAXF, "too many transform fields for Ptrs");
 
 // ------------------------------------------------------------------ pass 1
 template <typename T, bool COMPACT, int PHYS>
 struct OpYInvPhys2 {
     using V = typename Vec2<T>::type;
-    static constexpr const char* name = PHYS == PHYS_HYDRO ? "y_inv_hydro2d" : "y_inv_bouss2d";
+    static constexpr const char* name = PHYS == PHYS_HYDRO ? "y_inv_hydro2d" : PHYS == PHYS_BOUSS ? "y_inv_bouss2d"
+                                        : PHYS == PHYS_HYDRO_DIV ? "y_inv_hydro2d_div" : "y_inv_bouss2d_div";
     static constexpr int lmin = 32, lmax = 512;
     Geo2 g; CPtrs st; int64_t st_rs; Ptrs out; int64_t w_rs; const V* tw;
     const double* kx; const double* ky;
@@ -49,7 +60,7 @@ struct OpYInvPhys2 {
     __device__ C<T> load(int fld, int run, int e, int ix) const {
         if (!kept_full(e, g.Ny, g.My)) return zero<T>();
         double2 r;
-        if (fld < 2) r = get(fld, run, ix, e);
+        if (p2_div(PHYS) || fld < 2) r = get(fld, run, ix, e);   // divergence forms: the state itself
         else if (fld == 2) {  // curlX, N == 2: X[1].deriv(x) - X[0].deriv(y)  (physics.py:400)
             const double2 a = ideriv2(get(1, run, ix, e), kx[ix]), b = ideriv2(get(0, run, ix, e), ky[e]);
             r = make_double2(a.x - b.x, a.y - b.y);
@@ -83,6 +94,27 @@ struct ProdBouss2 {
     }
 };
 
+template <typename T>
+struct ProdHydroDiv2 {
+    static constexpr int NI = 2, NO = 2;
+    static constexpr int lmin = 32, lmax = 512;
+    __device__ void operator()(const T* in, T* out, int) const {
+        out[0] = in[0] * in[0] - in[1] * in[1];   // u_x^2 - u_y^2
+        out[1] = in[0] * in[1];                   // u_x u_y
+    }
+};
+template <typename T>
+struct ProdBoussDiv2 {
+    static constexpr int NI = 3, NO = 4;
+    static constexpr int lmin = 32, lmax = 512;
+    __device__ void operator()(const T* in, T* out, int) const {
+        out[0] = in[0] * in[0] - in[1] * in[1];
+        out[1] = in[0] * in[1];
+        out[2] = in[0] * in[2];                   // u_x T
+        out[3] = in[1] * in[2];                   // u_y T
+    }
+};
+
 // ------------------------------------------------------------------ pass 3
 template <typename T>
 struct OpYFwdCompact2 {
@@ -113,10 +145,11 @@ struct Work2 {
     template <typename T> double2* NC(int f) const {
         return (double2*)((char*)base + up256(sizeof(C<T>) * 5 * nrun * w)) + (size_t)f * nrun * kc;
     }
-    template <typename T> double2* K1(int f) const { return NC<T>(3) + (size_t)f * nrun * kc; }
-    template <typename T> double2* YS(int f) const { return NC<T>(6) + (size_t)f * nrun * kc; }
+    // compact regions: products NC (up to 4), then K1 (3) and YS (3)
+    template <typename T> double2* K1(int f) const { return NC<T>(4) + (size_t)f * nrun * kc; }
+    template <typename T> double2* YS(int f) const { return NC<T>(7) + (size_t)f * nrun * kc; }
     template <typename T> static size_t bytes(const Geo2& g, int nrun) {
-        return up256(sizeof(C<T>) * 5 * (size_t)nrun * g.wcount()) + sizeof(double2) * 9 * (size_t)nrun * g.Kx * g.Ky;
+        return up256(sizeof(C<T>) * 5 * (size_t)nrun * g.wcount()) + sizeof(double2) * 10 * (size_t)nrun * g.Kx * g.Ky;
     }
 };
 
@@ -126,11 +159,21 @@ int nonlinear2(const dd_plan* pl, const Work2& w, const void* const* st, int64_t
     using PH = Phys2<PHYS>;
     CPtrs sin{}; Ptrs wo{}; CPtrs wi{}; Ptrs nc{};
     for (int c = 0; c < PH::NF; c++) sin.p[c] = st[c];
-    for (int f = 0; f < PH::NI; f++) { wo.p[f] = w.W<T>(f); wi.p[f] = wo.p[f]; }
+    // W buffers: the inverse-transformed fields, then (in place, row by row) the
+    // products; the divergence form has more products (4) than inputs (3)
+    constexpr int NW = PH::NI > PH::NO ? PH::NI : PH::NO;
+    static_assert(NW <= 5, "Work2 holds 5 transform buffers");
+    for (int f = 0; f < NW; f++) { wo.p[f] = w.W<T>(f); wi.p[f] = wo.p[f]; }
     for (int f = 0; f < PH::NO; f++) nc.p[f] = w.NC<T>(f);
     OpYInvPhys2<T, COMPACT, PHYS> a{g, sin, st_rs, wo, (int64_t)w.w, TwSel<T>::y(pl), pl->kx, pl->ky};
     DD_TRY((launch_pass_len<T, true, true, false>(g.Ny, a, g.Kx, w.nrun, PH::NI, s)));
-    if (PHYS == PHYS_HYDRO) {
+    if constexpr (PHYS == PHYS_HYDRO_DIV) {
+        DD_TRY((launch_x_prod_len<T>("x_div_hydro2d", g.Nx, g.Ny, g.Kx, wi, wo, w.nrun, (int64_t)w.w, (int64_t)w.w,
+                                     TwSel<T>::x(pl), (T)pl->inv_n, ProdHydroDiv2<T>{}, s)));
+    } else if constexpr (PHYS == PHYS_BOUSS_DIV) {
+        DD_TRY((launch_x_prod_len<T>("x_div_bouss2d", g.Nx, g.Ny, g.Kx, wi, wo, w.nrun, (int64_t)w.w, (int64_t)w.w,
+                                     TwSel<T>::x(pl), (T)pl->inv_n, ProdBoussDiv2<T>{}, s)));
+    } else if constexpr (PHYS == PHYS_HYDRO) {
         DD_TRY((launch_x_prod_len<T>("x_prod_hydro2d", g.Nx, g.Ny, g.Kx, wi, wo, w.nrun, (int64_t)w.w, (int64_t)w.w,
                                      TwSel<T>::x(pl), (T)pl->inv_n, ProdHydro2<T>{}, s)));
     } else {
@@ -150,6 +193,14 @@ int nonlinear2(const dd_plan* pl, const Work2& w, const void* const* st, int64_t
     EXT template int nonlinear2<T, false, PHYS_BOUSS>(const dd_plan*, const Work2&, const void* const*, int64_t, \
                                                       cudaStream_t);                                         \
     EXT template int nonlinear2<T, true, PHYS_BOUSS>(const dd_plan*, const Work2&, const void* const*, int64_t,  \
-                                                     cudaStream_t);
+                                                     cudaStream_t);                                          \
+    EXT template int nonlinear2<T, false, PHYS_HYDRO_DIV>(const dd_plan*, const Work2&, const void* const*,     \
+                                                          int64_t, cudaStream_t);                            \
+    EXT template int nonlinear2<T, true, PHYS_HYDRO_DIV>(const dd_plan*, const Work2&, const void* const*,      \
+                                                         int64_t, cudaStream_t);                             \
+    EXT template int nonlinear2<T, false, PHYS_BOUSS_DIV>(const dd_plan*, const Work2&, const void* const*,     \
+                                                          int64_t, cudaStream_t);                            \
+    EXT template int nonlinear2<T, true, PHYS_BOUSS_DIV>(const dd_plan*, const Work2&, const void* const*,      \
+                                                         int64_t, cudaStream_t);
 
 }  // namespace dd

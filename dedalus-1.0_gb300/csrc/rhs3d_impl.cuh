@@ -219,6 +219,7 @@ int nonlinear3(const dd_plan* pl, const void* const* u, double inv_fpr, const Wo
     using P = Phys3<PH>;
     const Geo3& g = pl->g3;
     CPtrs uin{}; Ptrs w1{}, w2{}, nc{}; CPtrs w1c{}, w2c{};
+    static_assert(P::NI >= P::NO && P::NI >= P::NINV, "transform buffers must hold inputs and products");
     for (int c = 0; c < P::NF; c++) uin.p[c] = u[c];
     for (int c = 0; c < P::NO; c++) nc.p[c] = w.NC<T>(c);
     for (int f = 0; f < P::NI; f++) {

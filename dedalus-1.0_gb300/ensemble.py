@@ -27,6 +27,8 @@ from .engine import get_plan, dptr
 from . import init_cond
 
 PHYS_BOUSS = 1
+PHYS_BOUSS_DIV = 3            # divergence form, for solenoidal velocities
+DIV_TOL2 = 1e-24
 _TUNE_ENV = "DD_TUNE_CACHE"
 
 
@@ -49,6 +51,7 @@ class _SizeClass:
         self.chunk = self.nrun
         self.ws = None
         self.stream = torch.cuda.Stream(device=device)
+        self.phys = PHYS_BOUSS
 
     def workspace(self, chunk):
         n = ctypes.c_size_t()
@@ -165,7 +168,7 @@ class BoussinesqEnsemble2D:
             ws = c.workspace(c.chunk)
             base = c.slab[j0]
             fp, _f = _lib.ptr_array([base[f].data_ptr() for f in range(3)])
-            _lib.call("dd_rk2mid_step2d", c.plan.handle, PHYS_BOUSS, self.params, nr, fp, rs, dptr(ik2), thp, tfp,
+            _lib.call("dd_rk2mid_step2d", c.plan.handle, c.phys, self.params, nr, fp, rs, dptr(ik2), thp, tfp,
                       nus, self.vo, float(dt), self.prec, ctypes.byref(self._nonkept[c.n]), dptr(ws), ws.numel(),
                       st)
 
@@ -183,6 +186,22 @@ class BoussinesqEnsemble2D:
             e.record(self.classes[ci].stream)
             main.wait_event(e)
 
+    def _update_forms(self):
+        """Per size class: the divergence form of the nonlinear terms when every
+        run's velocity is solenoidal (dd_divergence_sums2d), else the curl form.
+        The dynamics keep a solenoidal state solenoidal, so the choice holds
+        until the state is set again (which drops the captured graph)."""
+        buf = torch.empty(2, dtype=torch.float64, device=self.device)
+        st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        for c in self.classes:
+            base = c.slab[0]
+            _lib.call("dd_divergence_sums2d", c.plan.handle, c.nrun, dptr(base[0]), dptr(base[1]), 3 * c.fsize,
+                      dptr(buf), st)
+            num, den = buf.tolist()
+            c.phys = PHYS_BOUSS_DIV if self.nonlinear_form == 'auto' and num <= DIV_TOL2 * den else PHYS_BOUSS
+
+    nonlinear_form = 'auto'
+
     def step(self, dt, graph=True):
         """Advance every run by one RK2mid step (one graph replay when graph=True)."""
         if graph:
@@ -190,6 +209,7 @@ class BoussinesqEnsemble2D:
                 self.capture(dt)
             self._graph.replay()
         else:
+            self._update_forms()
             self._issue_step(dt)
         self.time += dt
         self.iteration += 1
@@ -198,6 +218,7 @@ class BoussinesqEnsemble2D:
         """Capture one ensemble step into a CUDA graph.  The schedule (chunks,
         order) and every table and workspace are prepared by an eager step on a
         scratch copy first, so nothing allocates or configures inside capture."""
+        self._update_forms()
         saved = [c.slab.clone() for c in self.classes]
         self._issue_step(dt)                      # warm-up: tables, workspaces, kernel attributes
         torch.cuda.synchronize()
@@ -214,15 +235,24 @@ class BoussinesqEnsemble2D:
         self._graph, self._graph_dt = g, dt
 
     # ---------------------------------------------------------------- metrics
-    def algorithmic_bytes_per_step(self):
-        """Canonical bytes of one ensemble step: per run, 2 RHS x 8 transforms x
-        (one real + one complex 2D field pass) + 2 stages x 3 fields x 3 complex
-        passes (B2(N) = 8 N^2 + 16 N (N/2 + 1))."""
+    def transforms_per_rhs(self, n):
+        """Transforms per RHS of a run of size n: 5 + 3 (curl form) or 3 + 4
+        (divergence form)."""
+        c = next(c for c in self.classes if c.n == n)
+        return 7 if c.phys == PHYS_BOUSS_DIV else 8
+
+    def algorithmic_bytes_per_step(self, canonical=False):
+        """Algorithmic bytes of one ensemble step: per run, 2 RHS x 8 (or 7)
+        transforms x (one real + one complex 2D field pass) + 2 stages x 3 fields
+        x 3 complex passes (B2(N) = 8 N^2 + 16 N (N/2 + 1)); the divergence
+        form's stages read one more product field.  canonical: the curl form's
+        count."""
         tot = 0
         for n in self.sizes:
             b2 = 8 * n * n + 16 * n * (n // 2 + 1)
             c2 = 16 * n * (n // 2 + 1)
-            tot += 2 * 8 * b2 + 2 * 3 * 3 * c2
+            nt = 8 if canonical else self.transforms_per_rhs(n)
+            tot += 2 * nt * b2 + 2 * 3 * 3 * c2 + (2 * c2 if nt == 7 else 0)
         return tot
 
     def grid_point_stages(self):

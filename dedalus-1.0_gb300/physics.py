@@ -361,7 +361,21 @@ class IncompressibleHydro(ReferenceOrderRHS, Physics):
         pp = self._params2d()
         ppa = None if pp is None else (ctypes.c_double * 4)(*pp)
         nus = (ctypes.c_double * 3)(*(coeffs + [0.] * (3 - len(coeffs))))
-        _lib.call("dd_rk2mid_step2d", plan.handle, self._phys2d, ppa, 1, sp, 0,
+        phys = self._phys2d
+        # below 256^2 points a step is launch/latency bound: the check's host
+        # read would cost more than the transform it saves
+        if (self.nonlinear_form == 'auto' and not torch.cuda.is_current_stream_capturing()
+                and int(np.prod(plan.xshape)) >= 256 * 256):
+            buf = self._tables.get('div_sums')
+            if buf is None:
+                buf = self._tables['div_sums'] = torch.empty(2, dtype=torch.float64, device=plan.device)
+            _lib.call("dd_divergence_sums2d", plan.handle, 1, dptr(data['u'][0].kdata), dptr(data['u'][1].kdata), 0,
+                      dptr(buf), current_stream())
+            num, den = buf.tolist()
+            if num <= self.DIV_TOL2 * den:
+                phys += 2
+        self.last_phys2d = phys
+        _lib.call("dd_rk2mid_step2d", plan.handle, phys, ppa, 1, sp, 0,
                   None if ik2 is None else dptr(ik2), th, tf, nus, vo, float(dt), prec, None,
                   dptr(ws), ws.numel(), current_stream())
         return True

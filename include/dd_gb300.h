@@ -169,7 +169,11 @@ int dd_hydro3d_rk4_step(const dd_plan* plan, void* const* u, const double* inv_k
  * physics 1 = BoussinesqHydro (physics.py:664-712), state (u_x, u_y, T) with
  * params = {g, alpha_t, beta, direction} (direction 0 = x, 1 = y; the
  * reference's default 'z' has no 2D component, physics.py:646, fields.py:148).
- * Shear, rotation, tracer and forcing are not implemented.  A call covers
+ * physics 2 / 3 = the same with the nonlinear terms in divergence form (the
+ * momentum products u_x^2 - u_y^2, u_x u_y and the fluxes u_x T, u_y T: 2 + 2
+ * and 3 + 4 transforms per RHS instead of 3 + 2 and 5 + 3), equal to physics
+ * 0 / 1 to roundoff when every run's u is solenoidal (dd_divergence_sums2d).
+ * Shear, rotation, tracer and forcing are not in these kernels.  A call covers
  * nrun independent runs of the plan's grid: run b's field c is at
  * state[c] + b * state_rs complex entries (state_rs = 0 and nrun = 1 for one
  * run).  dd_rhs2d writes the dealiased RHS into deriv (zero_nonkept != 0 also
@@ -239,6 +243,10 @@ int dd_spectrum(const dd_plan* plan, int ncomp, const void* const* comps, double
  * 3D velocity (3 full-layout k arrays); out is device memory [2], overwritten.
  * out[0] / out[1] is the squared relative divergence of the state. */
 int dd_divergence_sums(const dd_plan* plan, const void* const* u, double* out, void* stream);
+/* The same for nrun 2D velocities (u_x, u_y full-layout k arrays; run r at
+ * offset r * run_stride complex entries), summed over all runs. */
+int dd_divergence_sums2d(const dd_plan* plan, int nrun, const void* ux, const void* uy, int64_t run_stride,
+                         double* out, void* stream);
 
 /* Sets *dflag (device int) to 1 if any of the ncomp k arrays has a non-zero
  * entry outside the kept (dealiased) modes; does not clear it. */

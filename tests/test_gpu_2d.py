@@ -156,3 +156,52 @@ def test_gravity_wave_known_answer(dd, cuda):
     for (f, c), v in init.items():
         got = data[f][c].to_numpy('kspace')[mode]
         assert abs(got - v * phase) < 1e-5 * abs(v), (f, c, got, v * phase)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("cls,shape", [("IncompressibleHydro", (256, 256)), ("BoussinesqHydro", (256, 256)),
+                                       ("BoussinesqHydro", (256, 512))])
+def test_divergence_form_2d_steps(dd, cuda, cls, shape):
+    """On grids of 256^2 points and more a solenoidal u takes the divergence
+    form (physics 2 / 3); five RK2mid steps equal the curl form's and the
+    oracle's to 1e-12 relative L2."""
+    hydro = cls == "IncompressibleHydro"
+    names = HYD if hydro else BOU
+    params = {'nu': 1e-3} if hydro else BPAR
+    fields = hydro_fields(dd, shape, 4) if hydro else bouss_fields(dd, shape, 5)
+    ro, do, rg, dg = setup(dd, cls, shape, params, fields)
+    _r2, _d2, rc, dc = setup(dd, cls, shape, params, fields)
+    rc.nonlinear_form = 'rotational'
+    to, tg, tc = OT.RK2mid(ro), dd.mods.RK2mid(rg), dd.mods.RK2mid(rc)
+    for _ in range(5):
+        to.do_advance(do, 1e-2 if not hydro else 1e-3)
+        tg.do_advance(dg, 1e-2 if not hydro else 1e-3)
+        tc.do_advance(dc, 1e-2 if not hydro else 1e-3)
+    assert rg.last_phys2d == (2 if hydro else 3) and rc.last_phys2d == (0 if hydro else 1)
+    assert rel_l2(state(dg, names, True), state(dc, names, True)) < 1e-12
+    assert rel_l2(state(dg, names, True), state(do, names, False)) < 1e-12
+
+
+@pytest.mark.gpu
+def test_divergence_sums_2d(dd, cuda):
+    import torch
+    shape = (64, 128)
+    u = dd.init_cond.turbulence_2d(shape, seed=6)
+    rng = np.random.Generator(np.random.PCG64(7))
+    v = [u[0] + 0.01 * rng.normal(size=u[0].shape), u[1]]        # a divergent copy as run 1
+    slab = torch.from_numpy(np.stack([np.stack([u[0], u[1], u[0]]), np.stack([v[0], v[1], v[0]])])).cuda()
+    plan = dd.engine.get_plan(shape, (2 * np.pi,) * 2)
+    out = torch.empty(2, dtype=torch.float64, device="cuda")
+    fs = slab[0, 0].numel()
+    for nrun, runs in ((1, [u]), (2, [u, v])):
+        dd._lib.call("dd_divergence_sums2d", plan.handle, nrun, dd.engine.dptr(slab[0, 0]), dd.engine.dptr(slab[0, 1]),
+                     3 * fs, dd.engine.dptr(out), dd.engine.current_stream())
+        kx, ky, _ = dd.kgrid.k_tables(shape, (2 * np.pi,) * 2)
+        KX, KY = kx[:, None], ky[None, :]
+        keep = (np.abs(KX) <= plan.mx) & ((np.arange(len(ky)) <= plan.my) | (np.arange(len(ky)) >= len(ky) - plan.my))[None, :]
+        r0 = sum(np.sum(np.abs(KX * w[0] + KY * w[1]) ** 2 * keep) for w in runs)
+        r1 = sum(np.sum((KX ** 2 + KY ** 2) * (np.abs(w[0]) ** 2 + np.abs(w[1]) ** 2) * keep) for w in runs)
+        got = out.cpu().numpy()
+        assert abs(got[1] - r1) <= 1e-12 * r1
+        assert abs(got[0] - r0) <= 1e-12 * r1
+    assert got[0] > 1e-6 * got[1]          # the divergent run shows

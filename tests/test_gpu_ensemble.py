@@ -77,3 +77,24 @@ def test_ensemble_autotune_caches_schedule(dd, cuda, tmp_path):
         ref.step(1e-2, graph=False)
     for r in range(len(sizes)):
         np.testing.assert_array_equal(np.stack(ens2.run_state(r)), np.stack(ref.run_state(r)))
+
+
+@pytest.mark.gpu
+def test_ensemble_divergence_form_equals_curl_form(dd, cuda):
+    """The ensemble's runs start with u = 0 (solenoidal): every class takes
+    the divergence form (physics 3), and ten steps equal the curl form's to
+    1e-12 relative L2 per run."""
+    sizes = [64, 128, 64, 256, 128]
+    res = []
+    for form in ("auto", "rotational"):
+        ens = dd.ensemble.BoussinesqEnsemble2D(sizes, nu=2e-3, kappa=2e-3)
+        ens.nonlinear_form = form
+        ens.load_initial_conditions(seed=3)
+        for _ in range(10):
+            ens.step(1e-2, graph=False)
+        res.append(([c.phys for c in ens.classes], [ens.run_state(r) for r in range(len(sizes))]))
+    assert all(p == 3 for p in res[0][0]) and all(p == 1 for p in res[1][0])
+    for a, b in zip(res[0][1], res[1][1]):
+        num = sum(np.sum(np.abs(x - y) ** 2) for x, y in zip(a, b))
+        den = sum(np.sum(np.abs(y) ** 2) for y in b)
+        assert np.sqrt(num / den) < 1e-12
