@@ -65,6 +65,67 @@ int launch_pass(const Op& op, int npencil, int nslow, int nfield, cudaStream_t s
     return DD_OK;
 }
 
+// The same pass with an explicit schedule S (pencils per tile, threads, radix
+// sequence): small tiles give a small single-run grid enough blocks to fill
+// the GPU (a 128-point y pass of 43 kx pencils is 2 tiles of the default 32
+// pencils, but 11 tiles of 4).
+template <typename T, class S, bool INV, bool LD_E, bool ST_E, class Op>
+__global__ void __launch_bounds__(S::NT) k_pass_sched(const Op op, int nfield) {
+    extern __shared__ __align__(16) unsigned char dd_smem[];
+    constexpr int L = S::L, P = S::P, PS = S::PS, NT = S::NT;
+    C<T>* tile = reinterpret_cast<C<T>*>(dd_smem);
+    C<T>* tw = tile + L * PS;
+    load_twiddles<T, L>(tw, op.tw);
+    const int fld = blockIdx.x % nfield;
+    const int f0 = (blockIdx.x / nfield) * P;
+    const int s = blockIdx.y + 65535 * blockIdx.z;
+    const int npen = op.npencil();
+    for (int idx = threadIdx.x; idx < L * P; idx += NT) {
+        const int e = LD_E ? idx % L : idx / P;
+        const int p = LD_E ? idx / L : idx % P;
+        const int f = f0 + p;
+        tile[e * PS + p] = (f < npen) ? op.load(fld, s, e, f) : zero<T>();
+    }
+    __syncthreads();
+    pencil_fft_s<T, S, INV>(tile, tw);
+    const int nst = op.nstore();
+    for (int idx = threadIdx.x; idx < nst * P; idx += NT) {
+        const int e = ST_E ? idx % nst : idx / P;
+        const int p = ST_E ? idx / nst : idx % P;
+        const int f = f0 + p;
+        if (f < npen) op.store(fld, s, e, f, tile + p, PS);
+    }
+}
+
+template <typename T, class S, bool INV, bool LD_E, bool ST_E, class Op>
+int launch_pass_sched(const Op& op, int npencil, int nslow, int nfield, cudaStream_t st) {
+    const size_t smem = S::template smem_bytes<T>();
+    auto kern = k_pass_sched<T, S, INV, LD_E, ST_E, Op>;
+    static std::atomic<unsigned long long> configured{0};
+    DD_TRY(ensure_smem((const void*)kern, smem, configured));
+    if (npencil <= 0 || nslow <= 0 || nfield <= 0) return DD_OK;
+    DD_CHECK_ARG(nslow <= 65535, "pass: slow extent %d must be <= 65535", nslow);
+    dim3 grid(cdiv(npencil, S::P) * nfield, nslow, 1);
+    static const std::string label = std::string(Op::name) + "_" + std::to_string(S::L) + "s" + PrecName<T>::s;
+    DD_KT(label.c_str(), st, kern<<<grid, S::NT, smem, st>>>(op, nfield));
+    DD_LAUNCH_CHECK();
+    return DD_OK;
+}
+
+// Small-tile schedules (4 pencils, 16 threads each) for single-run 2D grids.
+template <int L> struct SmallSched;
+template <> struct SmallSched<64> { using S = Sched<64, 4, 64, 4, 4, 4>; };
+template <> struct SmallSched<128> { using S = Sched<128, 4, 64, 8, 4, 4>; };
+
+// Launch a pass with the small-tile schedule when one exists for length L;
+// returns 1 (not launched) otherwise.
+template <typename T, bool INV, bool LD_E, bool ST_E, class Op>
+int launch_pass_small(int L, const Op& op, int npencil, int nslow, int nfield, cudaStream_t st) {
+    if (L == 64) return launch_pass_sched<T, typename SmallSched<64>::S, INV, LD_E, ST_E>(op, npencil, nslow, nfield, st);
+    if (L == 128) return launch_pass_sched<T, typename SmallSched<128>::S, INV, LD_E, ST_E>(op, npencil, nslow, nfield, st);
+    return 1;
+}
+
 // ============================================================ 3D operators
 // Inverse along kz: K[ky][kz][kx] (kept entries) -> W1[kyc][z][kxc].
 template <typename T, typename KT>

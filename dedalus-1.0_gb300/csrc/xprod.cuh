@@ -49,6 +49,16 @@ template <> struct ProdCfg<256, 3, 5> {
     using SI = Sched<256, 6, 192, 8, 8, 4>;  using SF = Sched<256, 10, 160, 16, 16, 1>;
     static constexpr int Q = 4, NT = 192;
 };
+// 2D hydro (3 -> 2) on 64- and 128-point rows: 2 rows per block (3 inverse
+// and 2 forward pencils of 16 threads), so that one 128^2 run has 64 blocks.
+template <> struct ProdCfg<64, 3, 2> {
+    using SI = Sched<64, 3, 48, 4, 4, 4>;  using SF = Sched<64, 2, 32, 4, 4, 4>;
+    static constexpr int Q = 2, NT = 48;
+};
+template <> struct ProdCfg<128, 3, 2> {
+    using SI = Sched<128, 3, 48, 8, 4, 4>;  using SF = Sched<128, 2, 32, 8, 4, 4>;
+    static constexpr int Q = 2, NT = 48;
+};
 template <> struct ProdCfg<64, 12, 6> {
     using SI = Sched<64, 24, 192, 8, 8, 1>;  using SF = Sched<64, 12, 192, 4, 4, 4>;
     static constexpr int Q = 4, NT = 192;
