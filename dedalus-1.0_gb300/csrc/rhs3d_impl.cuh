@@ -5,6 +5,7 @@
 //          or, for a solenoidal state, P[-i k_j T_ij] (ProdDiv3 below)
 //   MHD:   RHS(u) = P[u x w + (J x B) / (4 pi rho0)]^, J = curl B,
 //          RHS(B) = curl (u x B)^                            (physics.py:770-819)
+//          or, for solenoidal u and B, RHS(u) = P[-i k_j M_ij] (ProdMHDDiv3)
 // The rotational form u x w equals the reference's -(u.grad)u on the kept
 // modes to roundoff: the difference is a gradient, which the projection
 // removes, and products of dealiased fields alias only onto non-kept modes.
@@ -12,13 +13,15 @@
 // transform per component instead of two; equal by linearity).
 //
 // Passes (all pruned to the kept modes; T = FP64 or FP32 arithmetic):
-//   1  Z^-1 of each vector field and its curl (formed while loading)
+//   1  Z^-1 of each vector field and its curl (formed while loading); the
+//      divergence forms load the state fields only
 //   2  Y^-1
 //   3  X c2r -> pointwise products -> X r2c, scaled by 1/N   (k_x_prod)
 //   4  Y forward, kept ky only
 //   5  Z forward, kept kz only, into a compact [kyc][kzc][kx] buffer
-//   6  projection (physics.py:588-599, laplace_solve 407-416) and, for B,
-//      the spectral curl (physics.py:394-396), fused with the RK4 stage.
+//   6  (divergence forms: -i k_j T_ij from the product spectra) projection
+//      (physics.py:588-599, laplace_solve 407-416) and, for B, the spectral
+//      curl (physics.py:394-396), fused with the RK4 stage.
 #include "launch_len.cuh"
 #include "xprod.cuh"
 #include "etd.cuh"
