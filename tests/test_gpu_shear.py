@@ -102,6 +102,9 @@ _CASES = [
     ("BoussinesqHydro", (16, 16, 16), {"nu": 2e-3, "kappa": 2e-3, "boussinesq_direction": "z"}, False),
     ("IncompressibleMHD", (16, 16, 16), {"shear_rate": 1.0, "nu": 5e-3, "eta": 5e-3}, True),
     ("IncompressibleMHD", (32, 32), {"nu": 5e-3, "eta": 5e-3}, False),
+    ("IncompressibleMHD", (32, 32), {"shear_rate": 0.8, "nu": 5e-3, "eta": 5e-3}, True),
+    ("BoussinesqHydro", (16, 16, 16), {"shear_rate": 1.2, "nu": 2e-3, "kappa": 2e-3, "Omega": np.array([1.0, 0.0, 0.0]),
+                                       "boussinesq_direction": "z"}, True),
 ]
 
 
