@@ -1,7 +1,8 @@
 """GB300-native drop-in for the pseudospectral RHS / timestepping hot path of
-dedalus-1.0 (Fourier representation, IncompressibleHydro / BoussinesqHydro /
-IncompressibleMHD physics, RK2mid / RK2trap / RK4 integrators), plus a learned
-subgrid closure for 64^3 LES (``closure``, ``physics.LESHydro``).
+dedalus-1.0 (Fourier and shearing-box Fourier representations,
+IncompressibleHydro / BoussinesqHydro / IncompressibleMHD physics with shear
+and rotation, RK2mid / RK2trap / RK4 integrators), plus a learned subgrid
+closure for 64^3 LES (``closure``, ``physics.LESHydro``).
 
 Import name ``dedalus_gb300`` (the directory name is not a Python identifier;
 ``__graft_entry__.load_package()`` registers it).  All compute runs in
@@ -24,9 +25,10 @@ try:  # the device layers need torch; host helpers (kgrid, init_cond) do not
     from . import ensemble
     from . import closure
     from . import restart
+    from . import generic
 except ImportError as e:  # pragma: no cover
     if "torch" not in str(e):
         raise
 
 __all__ = ["_lib", "kgrid", "config", "init_cond", "engine", "representations", "fields", "physics",
-           "time_step", "mods", "diagnostics", "ensemble", "closure", "restart"]
+           "time_step", "mods", "diagnostics", "ensemble", "closure", "restart", "generic"]
