@@ -138,3 +138,16 @@ def test_shell_table_interpolates_and_reproduces_a_ramp():
     assert np.all(w2[kk >= 2.0] == 2.5)
     sel = kk < 2.0
     assert np.allclose(w2[sel], (0.5 + kk)[sel], atol=1e-15)
+
+
+def test_shell_count_covers_the_kept_modes():
+    """closure.shell_count bins round(|k|) over the kept cube |m_i| <= ceil(N/3) - 1."""
+    pytest.importorskip("torch")
+    import __graft_entry__
+    dd = __graft_entry__.load_package()
+    for n in (16, 32, 64):
+        shape = (n, n, n)
+        kx, ky, kz = OC.kvectors(shape)
+        kk = np.sqrt(kx ** 2 + ky ** 2 + kz ** 2)
+        top = int(np.max(np.floor(kk[np.broadcast_to(OC.kept_mask(shape), kk.shape)] + 0.5)))
+        assert dd.closure.shell_count(n) == top + 1
