@@ -46,6 +46,7 @@ SIGNATURES = {
     "dd_dealias": [P, P, P],
     "dd_deriv": [P, I, P, P, P],
     "dd_scale_add": [P, P, D, I, I64, P],
+    "dd_max_square": [I, PP, I64, P, P],
     "dd_euler": [P, P, P, D, I64, P],
     "dd_etd1": [I, P, P, P, P, D, I64, P],
     "dd_etd2rk1": [I, P, P, P, P, P, D, I64, P],

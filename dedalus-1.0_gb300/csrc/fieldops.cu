@@ -1,5 +1,6 @@
-// Small k-space field operations behind the representation's user API:
-// spectral derivative (representations.py:419-425) and scaled copies.
+// Small field operations behind the representation's user API: spectral
+// derivative (representations.py:419-425), scaled copies, and the largest
+// squared grid value of a vector field (fields.py:153-157, for the CFL step).
 #include "dd_common.cuh"
 #include "geometry.cuh"
 #include "plan.cuh"
@@ -39,6 +40,29 @@ __global__ void k_scale_add(const double2* x, double2* y, double w, int accumula
     }
 }
 
+// out = max over components c and grid points i of x_c[i]^2.  The squares are
+// non-negative, so their IEEE bit patterns order like the values and one
+// 64-bit atomicMax per warp merges them; the result is exact and
+// independent of the launch shape (a NaN anywhere wins, as with numpy's max).
+// *out must hold +0.0 (all-zero bits) on entry.
+__global__ void k_max_square(CPtrs x, int ncomp, int64_t n, unsigned long long* out) {
+    double m = 0.0;
+    for (int c = 0; c < ncomp; c++) {
+        const double* xc = (const double*)x.p[c];
+        for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+            const double v = xc[i];
+            const double q = v * v;
+            m = (q > m || q != q) ? q : m;
+        }
+    }
+    unsigned long long b = (unsigned long long)__double_as_longlong(m);
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long t = __shfl_xor_sync(0xffffffffu, b, o);
+        b = t > b ? t : b;
+    }
+    if ((threadIdx.x & 31) == 0 && b != 0ull) atomicMax(out, b);
+}
+
 static unsigned grid_for(int64_t n) {
     int64_t b = (n + 255) / 256;
     if (b > 152 * 16) b = 152 * 16;
@@ -70,6 +94,23 @@ int dd_scale_add(const void* x, void* y, double w, int accumulate, int64_t n, vo
     if (n == 0) return DD_OK;
     DD_KT("scale_add", (cudaStream_t)stream,
           k_scale_add<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>((const double2*)x, (double2*)y, w, accumulate, n));
+    DD_LAUNCH_CHECK();
+    return DD_OK;
+}
+
+int dd_max_square(int ncomp, const double* const* x, int64_t n, double* out, void* stream) {
+    DD_CHECK_ARG(x && out && n >= 0, "dd_max_square: bad arguments");
+    DD_CHECK_ARG(ncomp >= 1 && ncomp <= DD_MAXF, "dd_max_square: ncomp %d out of range", ncomp);
+    CPtrs xs{};
+    for (int c = 0; c < ncomp; c++) {
+        DD_CHECK_ARG(x[c], "dd_max_square: null component pointer %d", c);
+        xs.p[c] = x[c];
+    }
+    const cudaStream_t st = (cudaStream_t)stream;
+    DD_CUDA(cudaMemsetAsync(out, 0, sizeof(double), st));
+    if (n == 0) return DD_OK;
+    DD_KT("max_square", st,
+          k_max_square<<<grid_for(n), 256, 0, st>>>(xs, ncomp, n, (unsigned long long*)out));
     DD_LAUNCH_CHECK();
     return DD_OK;
 }

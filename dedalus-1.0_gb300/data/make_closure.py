@@ -17,20 +17,19 @@ banded closure term uses) and competes in the selection.
 The stored closure (les_closure_256to64.npz) was made by the command above.
 
 ``--base FILE`` skips the dataset and the training and starts from a stored
-network (les_closure_256to64_base.npz is the all-mode network of a run of
-the command above without --band-target).  ``--calibrate-seeds N`` fits per-shell closure-term weights on
-training seeds seed0 .. seed0 + N - 1: the ratio of the exact to the
-network's subgrid energy transfer per wavenumber shell, summed over the
-filtered DNS snapshots (closure.calibrate_shells); the calibrated closure and
-its variants then compete in the selection:
+network (any weights file written by this script).  ``--calibrate-seeds N``
+fits per-shell closure-term weights on training seeds seed0 .. seed0 + N - 1:
+the ratio of the exact to the network's subgrid energy transfer per
+wavenumber shell, summed over the filtered DNS snapshots
+(closure.calibrate_shells); the calibrated closure and its variants then
+compete in the selection:
 
-    python dedalus-1.0_gb300/data/make_closure.py \
-        --base dedalus-1.0_gb300/data/les_closure_256to64_base.npz \
+    python dedalus-1.0_gb300/data/make_closure.py --base weights.npz \
         --calibrate-seeds 4 --select-seed 11 --eval-seeds 7 13 17 \
         --eval-steps 1000 --out calibrated.npz --report calibrated.json
 
-Its outcome is les_closure_calibration_report.json: the calibrated weights
-lost to the stored closure on the selection seed.
+(On the stored network's all-mode sibling the calibrated weights lost to the
+banded closure on the selection seed.)
 """
 import argparse
 import json

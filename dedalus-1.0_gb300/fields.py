@@ -66,8 +66,18 @@ class VectorFieldBase(BaseField):
             self.ctrans = {'x': 0, 0: 'x', 'y': 1, 1: 'y', 'z': 2, 2: 'z'}
 
     def max_square(self):
-        """fields.py:153-157 (single device: no reduction across ranks)."""
-        return max(float((c['xspace'] ** 2).max()) for i, c in self)
+        """fields.py:153-157 (single device: no reduction across ranks).  As
+        in the reference, reading c['xspace'] leaves every component in grid
+        space; the maximum is one device reduction (dd_max_square)."""
+        from . import _lib
+        from .engine import current_stream, dptr
+        comps = [c for i, c in self]
+        for c in comps:
+            c.require_space('xspace')
+        out = torch.empty((), dtype=torch.float64, device=comps[0].device)
+        xp, _keep = _lib.ptr_array([c.xdata.data_ptr() for c in comps])
+        _lib.call("dd_max_square", len(comps), xp, comps[0].xdata.numel(), dptr(out), current_stream())
+        return float(out.item())
 
     def div_free(self):
         """Project off the irrotational part (fields.py:169-195)."""

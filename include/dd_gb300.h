@@ -96,11 +96,20 @@ int dd_fft_c2r(const dd_plan* plan, int nfield, const void* const* k, double* co
  * synchronisation are not allowed, or the caller's host language has no
  * device allocator).  Intermediates live in a 4 MiB static device buffer in
  * the library image (held on every GPU that loads the library): grids up to
- * 64^3 (3D) and 512^2 (2D); larger ones return DD_ERR_UNSUPPORTED.  The first
- * call on a device looks the buffer up (cudaGetSymbolAddress) and should come
- * before any stream capture.  All calls share the buffer: calls whose GPU
- * work overlaps race, so issue them in order on one stream. */
+ * 64^3 (3D) and 512^2 (2D), with or without 2/3 dealiasing (Nyquist modes are
+ * never kept); larger ones return DD_ERR_UNSUPPORTED.  Each call looks the buffer
+ * up on the current device (cudaGetSymbolAddress); the first call on a device
+ * should come before any stream capture.  The plan must belong to the current
+ * device (DD_ERR_INVALID otherwise).  All calls share the buffer: calls whose
+ * GPU work overlaps race, so issue them in order on one stream. */
 int dd_fft_c2r_noalloc(const dd_plan* plan, const void* k, double* x, void* stream);
+
+/* *out (device double) = max over the ncomp grid-space arrays x[c] (n float64
+ * values each, device) of x[c][i]^2: exact, deterministic, NaN-propagating.
+ * Replaces VectorFieldBase.max_square (dedalus/data_objects/fields.py:153-157)
+ * on one process, behind compute_dt / set_dtlist (physics.py:601-610,
+ * 714-721, 830-836). */
+int dd_max_square(int ncomp, const double* const* x, int64_t n, double* out, void* stream);
 
 /* In-place 2/3 dealiasing of one k array.  Replaces dealias_cy_{2d,3d}.dealias_23
  * (dedalus/data_objects/dealias_cy_3d.pyx:13-37, dealias_cy_2d.pyx:59-78). */

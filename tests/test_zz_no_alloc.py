@@ -19,10 +19,13 @@ def _rel(a, b):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("shape", [(64, 64, 64), (32, 16, 64), (128, 128), (512, 512)])
-def test_noalloc_c2r_matches_workspace_c2r(dd, cuda, shape):
+@pytest.mark.parametrize("shape,dealiasing", [((64, 64, 64), '2/3 cython'), ((32, 16, 64), '2/3 cython'),
+                                              ((128, 128), '2/3 cython'), ((512, 512), '2/3 cython'),
+                                              # no dealiasing: every mode but the Nyquist ones, 4.16 MB
+                                              ((64, 64, 64), 'None'), ((512, 512), 'None')])
+def test_noalloc_c2r_matches_workspace_c2r(dd, cuda, shape, dealiasing):
     import torch
-    plan = dd.engine.Plan(shape, (2 * np.pi,) * len(shape))
+    plan = dd.engine.Plan(shape, (2 * np.pi,) * len(shape), dealiasing=dealiasing)
     rng = np.random.default_rng(sum(shape) + 11)
     st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     for call in range(2):
@@ -37,6 +40,14 @@ def test_noalloc_c2r_matches_workspace_c2r(dd, cuda, shape):
         a, b = x_na.cpu().numpy(), x_ref.cpu().numpy()
         assert np.isfinite(a).all(), "call %d left unwritten outputs" % call
         assert _rel(a, b) < 1e-13, "call %d" % call
+    # the claim itself: a further call takes no device memory
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    dd._lib.call("dd_fft_c2r_noalloc", plan.handle, ctypes.c_void_p(kd.data_ptr()),
+                 ctypes.c_void_p(x_na.data_ptr()), st)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
 
 
 @pytest.mark.gpu
