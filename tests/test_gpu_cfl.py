@@ -41,7 +41,9 @@ def case(dd, kind):
     if kind == 'bouss2d':
         shape = (64, 64)
         T = dd.init_cond.band_limited_noise_2d(shape, seed=23)
-        u = dd.init_cond.turbulence_2d(shape, seed=24, energy_target=1e-2)
+        # |u|max > N = 1, so the advective limit is the smaller one and a
+        # halved state doubles it (the buoyancy-wave limit dx/N is fixed)
+        u = dd.init_cond.turbulence_2d(shape, seed=24, energy_target=20.0)
         return 'BoussinesqHydro', shape, BPAR, {('u', 0): u[0], ('u', 1): u[1], ('T', 0): T}
     shape = (32, 32, 32)
     u = dd.init_cond.turbulence_3d(shape, seed=25, k0=3.0)
