@@ -502,10 +502,11 @@ def les_problem(les_n=64, nu=5e-3, closure=None, precision='fp32'):
     return RHS, data, mods.RK4(RHS)
 
 
-def compare_spectra(e_ref, e, kmax):
-    """max over bins 1 <= k <= kmax of |e - e_ref| / e_ref."""
-    k = np.arange(len(e_ref))
-    sel = (k >= 1) & (k <= kmax) & (e_ref > 0)
+def compare_spectra(kc, e_ref, e, kcut):
+    """max over the spectrum bins centred at 0 < k <= kcut (kc: bin centres)
+    of |e - e_ref| / e_ref."""
+    kc, e_ref, e = np.asarray(kc), np.asarray(e_ref), np.asarray(e)
+    sel = (kc > 0) & (kc <= kcut) & (e_ref > 0)
     return float(np.max(np.abs(e[sel] - e_ref[sel]) / e_ref[sel]))
 
 
@@ -578,7 +579,7 @@ def evaluate(models, seed=7, dns_n=256, les_n=64, nu=5e-3, dt=2e-3, nsteps=1000,
             ref[1]['u'][i].kdata.copy_(ub[i])
             ref[1]['u'][i]._curr_space = 'kspace'
             ref[1]['u'][i].data = ref[1]['u'][i].kdata
-        _, e_ref = D.power_spectrum(ref[1]['u'])
+        kc, e_ref = D.power_spectrum(ref[1]['u'])
         out["steps"].append(step)
         out["dns_E"].append(e_ref.tolist())
         out["dns_diss"].append(D.energy_dissipation(dd, nu))
@@ -591,8 +592,8 @@ def evaluate(models, seed=7, dns_n=256, les_n=64, nu=5e-3, dt=2e-3, nsteps=1000,
             r["diss"].append(D.energy_dissipation(data, nu))
             r["diss_sgs"].append(sgs_dissipation(cl, data, precision) if cl is not None else 0.0)
             r["ekin"].append(D.ekin(data))
-            r["err_half"].append(compare_spectra(e_ref, e, kmax / 2.0))
-            r["err_full"].append(compare_spectra(e_ref, e, kmax))
+            r["err_half"].append(compare_spectra(kc, e_ref, e, kmax / 2.0))
+            r["err_full"].append(compare_spectra(kc, e_ref, e, kmax))
 
     record(0)
     for step in range(1, nsteps + 1):
@@ -617,3 +618,158 @@ def evaluate(models, seed=7, dns_n=256, les_n=64, nu=5e-3, dt=2e-3, nsteps=1000,
     out["kmax"] = kmax
     out["models"] = list(runs)
     return out
+
+
+# ------------------------------------------------- a-posteriori weight fit
+def dns_reference(seed, dns_n=256, les_n=64, nu=5e-3, dt=2e-3, nsteps=1000, every=100, sampler=None):
+    """One plain FP64 DNS trajectory as the judge of an LES: the filtered
+    initial state on the LES grid (device k arrays) and, every `every` steps,
+    the filtered-DNS spectrum E(k) and the DNS dissipation rate
+    2 nu <|curl u|^2> / 2 (volume_average.py:254-265)."""
+    from . import mods, diagnostics as D
+    from .init_cond import turbulence_3d
+    shape = (dns_n,) * 3
+    sampler = sampler or FilteredSampler(shape, (les_n,) * 3)
+    dns = mods.IncompressibleHydro(shape, mods.FourierRepresentation)
+    dns.parameters['nu'] = nu
+    dd = dns.create_fields(0.)
+    u0 = turbulence_3d(shape, seed=seed)
+    for i in range(3):
+        dd['u'][i]['kspace'] = u0[i]
+    ti = mods.RK4(dns)
+    _rhs, probe, _t = les_problem(les_n, nu, None)
+    ref = {"seed": seed, "nu": nu, "dt": dt, "every": every, "les_n": les_n, "steps": [], "E": [], "Es": [],
+           "diss": [],
+           "u0": [c.clone() for c in sampler.filter_velocity([dd['u'][i].kdata for i in range(3)])]}
+    t0 = time.time()
+    for step in range(0, nsteps + 1):
+        if step:
+            ti.do_advance(dd, dt)
+        if step % every == 0:
+            ub = sampler.filter_velocity([dd['u'][i].kdata for i in range(3)])
+            for i in range(3):
+                probe['u'][i].kdata.copy_(ub[i])
+                probe['u'][i]._curr_space = 'kspace'
+                probe['u'][i].data = probe['u'][i].kdata
+            kc, e = D.power_spectrum(probe['u'])
+            ks, es = D.power_spectrum(probe['u'], shells=True)
+            ref["kc"], ref["ks"] = np.asarray(kc), np.asarray(ks)
+            ref["steps"].append(step)
+            ref["E"].append(np.asarray(e))
+            ref["Es"].append(np.asarray(es))
+            ref["diss"].append(D.energy_dissipation(dd, nu))
+    torch.cuda.synchronize()
+    ref["seconds"] = time.time() - t0
+    ref["kmax"] = sampler.les.mx
+    return ref
+
+
+def _closure_energy_rate(RHS, data, d_with, d_without):
+    """Energy the closure term feeds into the LES state per unit time:
+    sum over modes of Re(conj(u) . F), F = RHS with the closure minus RHS
+    without it (Hermitian weight 2 for kx > 0), in the normalisation of
+    ekin.  Negative for a draining closure."""
+    cl = RHS.closure
+    RHS.RHS(data, d_with)
+    RHS.closure = None
+    try:
+        RHS.RHS(data, d_without)
+    finally:
+        RHS.closure = cl
+    tot = 0.0
+    for i in range(3):
+        u = data['u'][i].kdata
+        f = d_with['u'][i].kdata - d_without['u'][i].kdata
+        p = (u.conj() * f).real
+        tot += float(2.0 * p.sum() - p[..., 0].sum())
+    return tot
+
+
+def les_trajectory(closure, ref, precision='fp32'):
+    """Run the 64^3 LES (closure or None) from the reference's filtered
+    initial state over its steps.  At each of its record steps: the E(k)
+    error against the filtered DNS, max over the reference's spectrum bins
+    (PowerSpectrum, analysis_set.py:778-815) centred at k <= kmax/2
+    ("err_half") and k <= kmax ("err_full"), and over unit shells
+    k = 1 .. kmax/2 ("err_half_shells"); and the LES energy-loss rate
+    (resolved viscous dissipation minus the closure term's energy input)
+    relative to the DNS dissipation rate ("diss_err", (LES - DNS) / DNS)."""
+    from . import diagnostics as D
+    nu, dt, every = ref["nu"], ref["dt"], ref["every"]
+    les_n = ref["les_n"]
+    RHS, data, ti = les_problem(les_n, nu, closure, precision)
+    for i in range(3):
+        data['u'][i].kdata.copy_(ref["u0"][i])
+    out = {"steps": [], "err_half": [], "err_full": [], "err_half_shells": [], "diss_err": [], "diss": [],
+           "closure_input": []}
+    d1 = RHS.create_fields(0.) if closure is not None else None
+    d2 = RHS.create_fields(0.) if closure is not None else None
+    kmax = ref["kmax"]
+    nsteps = ref["steps"][-1]
+    for step in range(0, nsteps + 1):
+        if step:
+            ti.do_advance(data, dt)
+        if step % every == 0:
+            r = ref["steps"].index(step)
+            _, e = D.power_spectrum(data['u'])
+            _, es = D.power_spectrum(data['u'], shells=True)
+            diss = D.energy_dissipation(data, nu)
+            inp = _closure_energy_rate(RHS, data, d1, d2) if closure is not None else 0.0
+            out["steps"].append(step)
+            out["err_half"].append(compare_spectra(ref["kc"], ref["E"][r], e, kmax / 2.0))
+            out["err_full"].append(compare_spectra(ref["kc"], ref["E"][r], e, kmax))
+            out["err_half_shells"].append(compare_spectra(ref["ks"], ref["Es"][r], es, kmax / 2.0))
+            out["diss"].append(diss)
+            out["closure_input"].append(inp)
+            out["diss_err"].append((diss - inp - ref["diss"][r]) / ref["diss"][r])
+    return out
+
+
+def shell_table(knots, values, les_n=64):
+    """Closure-term weights per integer |k| (the dd_closure shell table):
+    piecewise linear through (knots, values), constant beyond either end."""
+    kk = np.arange(shell_count(les_n), dtype=np.float64)
+    return np.interp(kk, np.asarray(knots, dtype=np.float64), np.asarray(values, dtype=np.float64))
+
+
+def posteriori_score(trajs):
+    """max over runs of the largest of: the max over time of the E(k <= kmax/2)
+    error in the reference's bins and in unit shells, and the max over time
+    (after the start) of |dissipation error|."""
+    s = 0.0
+    for t in trajs:
+        s = max(s, max(t["err_half"]), max(t["err_half_shells"]), max(abs(x) for x in t["diss_err"][1:]))
+    return s
+
+
+def fit_posteriori(closure, refs, knots, x0, max_evals=300, log=None, precision='fp32'):
+    """Fit the closure-term weight table a posteriori: the weights at the
+    knots (piecewise linear in |k|) that minimise posteriori_score of the
+    LES runs against the DNS references refs (training seeds), by the
+    Nelder-Mead simplex (scipy.optimize).  Returns (weights at the knots,
+    info)."""
+    from scipy.optimize import minimize
+    hist = []
+
+    def obj(x):
+        cl = closure.with_shells(shell_table(knots, x))
+        trajs = [les_trajectory(cl, r, precision) for r in refs]
+        sc = posteriori_score(trajs)
+        hist.append({"x": [float(v) for v in x], "score": sc,
+                     "err_half": [max(t["err_half"]) for t in trajs],
+                     "err_half_shells": [max(t["err_half_shells"]) for t in trajs],
+                     "diss_err": [max(abs(v) for v in t["diss_err"][1:]) for t in trajs]})
+        if log and len(hist) % 10 == 0:
+            best = min(hist, key=lambda h: h["score"])
+            log("fit eval %d: score %.4f (best %.4f at %s)" % (len(hist), sc, best["score"],
+                                                                 np.round(best["x"], 3).tolist()))
+        return sc
+
+    x0 = np.asarray(x0, dtype=np.float64)
+    simplex = [x0] + [x0 + np.eye(len(x0))[i] * max(0.25, 0.3 * abs(x0[i])) for i in range(len(x0))]
+    t0 = time.time()
+    res = minimize(obj, x0, method='Nelder-Mead',
+                   options={"maxfev": max_evals, "xatol": 1e-3, "fatol": 1e-4, "initial_simplex": np.array(simplex)})
+    best = min(hist, key=lambda h: h["score"])
+    return np.asarray(best["x"]), {"evals": len(hist), "seconds": time.time() - t0, "best": best,
+                                   "start": hist[0], "knots": list(knots), "message": str(res.message)}

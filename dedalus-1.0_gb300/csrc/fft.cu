@@ -56,15 +56,25 @@ static void make_twiddles(int L, std::vector<double>& re, std::vector<double>& i
     }
 }
 
+// The FP64 and FP32 tables hold W_L^m = g (1 + i t) as (g, t) for the
+// fused multiply-add butterflies (fft_engine.cuh): g = Re W, t = Im W / Re W
+// (an IEEE division of the rounded parts, so every host gives the same
+// table); where Re W = 0 the pair is (2^-60, Im W 2^60), exact powers of two
+// whose product is Im W.  The double-float table keeps (cos, sin).
 static int upload_twiddles(int L, double2** d64, float2** d32, float4** ddf) {
     std::vector<double> re, im;
     make_twiddles(L, re, im);
     std::vector<double2> h64(L);
     std::vector<float2> h32(L);
     std::vector<float4> hdf(L);
+    const double tiny = ldexp(1.0, -60), huge = ldexp(1.0, 60);
     for (int m = 0; m < L; m++) {
-        h64[m] = make_double2(re[m], im[m]);
-        h32[m] = make_float2((float)re[m], (float)im[m]);
+        double g, t;
+        if (re[m] == 0.0) { g = tiny; t = im[m] * huge; }
+        else { g = re[m]; t = im[m] / re[m]; }
+        h64[m] = make_double2(g, t);
+        const float g32 = (float)g;
+        h32[m] = make_float2(g32, re[m] == 0.0 ? (float)t : (float)(im[m] / (double)g32));
         const df64 a(re[m]), b(im[m]);
         hdf[m] = make_float4(a.hi, a.lo, b.hi, b.lo);
     }

@@ -12,6 +12,22 @@
 // come from a per-length table W_L^m = exp(-2 pi i m / L) staged in shared
 // memory (conjugated for the inverse transform).
 //
+// FP64 and FP32 butterflies are written for fused multiply-add hardware
+// (Linzer and Feig, "Implementation of efficient FFT algorithms on fused
+// multiply-add architectures", IEEE Trans. Signal Processing 41(1), 1993):
+// a twiddle is stored as (g, t) with W = g (1 + i t), t = Im W / Re W, so
+// that a twiddled radix-2 step a +/- W b costs six FMAs (b (1 + i t), then
+// a +/- g (...)) instead of a complex product plus two complex additions.
+// A radix-R butterfly with inter-pass twiddles w^r is split 4 x 4 (R = 16),
+// 4 x 2 (R = 8) or 2 x 2 (R = 4) so that every twiddle it applies is a power
+// of one factor per sub-DFT: the first sub-DFTs take w^(R/4) (and its square),
+// the second ones w W_R^k1 (and its square), which folds the leftover w^n2
+// of the first stage into the second (24 FMAs per twiddled radix-4, 192
+// operations per twiddled radix 16 instead of 220).  A twiddle with Re W = 0
+// is stored with g = 2^-60 and t = Im W * 2^60: the product is exact and the
+// extra 2^-60 |b| is far below the rounding of the result.  The double-float
+// type keeps the plain butterflies on (cos, sin) tables.
+//
 // Forward transforms use exp(-i...), inverse exp(+i...); neither is scaled.
 #pragma once
 #include "dd_common.cuh"
@@ -125,6 +141,153 @@ __device__ __forceinline__ void dft(C<T>* v) {
     }
 }
 
+// --------------------------------------------------- FMA (Linzer-Feig) butterflies
+template <typename T> struct IsLF { static constexpr bool value = false; };
+template <> struct IsLF<double> { static constexpr bool value = true; };
+template <> struct IsLF<float> { static constexpr bool value = true; };
+
+__device__ __forceinline__ double fmx(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float fmx(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+
+// tan(pi/8) and tan(3 pi/8) = sqrt(2) -+ 1 (correctly rounded decimal expansions)
+#define DD_T8 0.41421356237309504880
+#define DD_T38 2.41421356237309504880
+
+// b (1 + i t) for the forward sign, b (1 - i t) for the inverse (the
+// conjugate twiddle): two FMAs.
+template <bool INV, typename T>
+__device__ __forceinline__ C<T> lf_rot(C<T> b, T t) {
+    const T tt = INV ? -t : t;
+    return mk<T>(fmx(-tt, b.y, b.x), fmx(tt, b.x, b.y));
+}
+
+// s = a + g u, d = a - g u: four FMAs.
+template <typename T>
+__device__ __forceinline__ void lf_pm(C<T> a, C<T> u, T g, C<T>& s, C<T>& d) {
+    s = mk<T>(fmx(g, u.x, a.x), fmx(g, u.y, a.y));
+    d = mk<T>(fmx(-g, u.x, a.x), fmx(-g, u.y, a.y));
+}
+
+// In place X_m = sum_n x_n z^n W4^(nm) with z = g1 (1 + i t1) and
+// z^2 = g2 (1 + i t2) (conjugated for INV): 24 FMAs.
+template <bool INV, typename T>
+__device__ __forceinline__ void dft4_lf(C<T>& x0, C<T>& x1, C<T>& x2, C<T>& x3, T g1, T t1, T g2, T t2) {
+    C<T> A, B, Cp, Dp;
+    lf_pm(x0, lf_rot<INV>(x2, t2), g2, A, B);
+    lf_pm(x1, lf_rot<INV>(x3, t2), g2, Cp, Dp);
+    lf_pm(A, lf_rot<INV>(Cp, t1), g1, x0, x2);
+    lf_pm(B, mul_mi<INV>(lf_rot<INV>(Dp, t1)), g1, x1, x3);
+}
+
+// The same with z^2 = W4 (-i forward, +i inverse), i.e. z = W8: 20 operations.
+template <bool INV, typename T>
+__device__ __forceinline__ void dft4_lf_zsq_w4(C<T>& x0, C<T>& x1, C<T>& x2, C<T>& x3, T g1, T t1) {
+    const C<T> a2 = mul_mi<INV>(x2), a3 = mul_mi<INV>(x3);
+    const C<T> A = x0 + a2, B = x0 - a2, Cp = x1 + a3, Dp = x1 - a3;
+    lf_pm(A, lf_rot<INV>(Cp, t1), g1, x0, x2);
+    lf_pm(B, mul_mi<INV>(lf_rot<INV>(Dp, t1)), g1, x1, x3);
+}
+
+// Radix-R butterfly of Stockham pass NS on v[0..R-1] (natural order in and
+// out), with the inter-pass twiddles w^r, w = W_(NS R)^k, taken from the
+// staged (g, t) table lf (W_L^m at index m).
+template <int R, int NS, int L, bool INV, typename T>
+__device__ __forceinline__ void bfly_lf(C<T>* v, const C<T>* lf, int k) {
+    constexpr int STEP = L / (NS * R);
+    if constexpr (R == 16) {
+        if constexpr (NS > 1) {
+            const C<T> a4 = lf[(4 * k) * STEP], a8 = lf[(8 * k) * STEP];
+#pragma unroll
+            for (int n2 = 0; n2 < 4; n2++) dft4_lf<INV>(v[n2], v[4 + n2], v[8 + n2], v[12 + n2], a4.x, a4.y, a8.x, a8.y);
+        } else {
+#pragma unroll
+            for (int n2 = 0; n2 < 4; n2++) dft4<INV>(v[n2], v[4 + n2], v[8 + n2], v[12 + n2]);
+        }
+        // now v[4 k1 + n2] = Y'[n2][k1]; second sub-DFTs over n2 with z = w W16^k1
+        C<T> y[4][4];
+#pragma unroll
+        for (int k1 = 0; k1 < 4; k1++) {
+#pragma unroll
+            for (int n2 = 0; n2 < 4; n2++) y[k1][n2] = v[4 * k1 + n2];
+            if constexpr (NS > 1) {
+                const int e = k + k1 * NS;
+                const C<T> z = lf[e * STEP], z2 = lf[(2 * e) * STEP];
+                dft4_lf<INV>(y[k1][0], y[k1][1], y[k1][2], y[k1][3], z.x, z.y, z2.x, z2.y);
+            } else if (k1 == 0) {
+                dft4<INV>(y[0][0], y[0][1], y[0][2], y[0][3]);
+            } else if (k1 == 1) {   // z = W16, z^2 = W8
+                dft4_lf<INV>(y[1][0], y[1][1], y[1][2], y[1][3], T(DD_C8), T(-DD_T8), T(DD_R2), T(-1));
+            } else if (k1 == 2) {   // z = W8, z^2 = W4
+                dft4_lf_zsq_w4<INV>(y[2][0], y[2][1], y[2][2], y[2][3], T(DD_R2), T(-1));
+            } else {                // z = W16^3, z^2 = W16^6
+                dft4_lf<INV>(y[3][0], y[3][1], y[3][2], y[3][3], T(DD_S8), T(-DD_T38), T(-DD_R2), T(1));
+            }
+        }
+#pragma unroll
+        for (int k1 = 0; k1 < 4; k1++) {
+#pragma unroll
+            for (int k2 = 0; k2 < 4; k2++) v[k1 + 4 * k2] = y[k1][k2];
+        }
+    } else if constexpr (R == 8) {
+        if constexpr (NS > 1) {
+            const C<T> a2 = lf[(2 * k) * STEP], a4 = lf[(4 * k) * STEP];
+#pragma unroll
+            for (int n2 = 0; n2 < 2; n2++) dft4_lf<INV>(v[n2], v[2 + n2], v[4 + n2], v[6 + n2], a2.x, a2.y, a4.x, a4.y);
+        } else {
+#pragma unroll
+            for (int n2 = 0; n2 < 2; n2++) dft4<INV>(v[n2], v[2 + n2], v[4 + n2], v[6 + n2]);
+        }
+        // v[2 k1 + n2] = Y'[n2][k1]; radix-2 steps with z = w W8^k1
+        C<T> X[8];
+#pragma unroll
+        for (int k1 = 0; k1 < 4; k1++) {
+            const C<T> y0 = v[2 * k1], y1 = v[2 * k1 + 1];
+            if constexpr (NS > 1) {
+                const C<T> z = lf[(k + k1 * NS) * STEP];
+                lf_pm(y0, lf_rot<INV>(y1, z.y), z.x, X[k1], X[k1 + 4]);
+            } else if (k1 == 0) {
+                X[0] = y0 + y1; X[4] = y0 - y1;
+            } else if (k1 == 1) {
+                lf_pm(y0, lf_rot<INV>(y1, T(-1)), T(DD_R2), X[1], X[5]);
+            } else if (k1 == 2) {
+                const C<T> a = mul_mi<INV>(y1);
+                X[2] = y0 + a; X[6] = y0 - a;
+            } else {
+                lf_pm(y0, lf_rot<INV>(y1, T(1)), T(-DD_R2), X[3], X[7]);
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < 8; r++) v[r] = X[r];
+    } else if constexpr (R == 4) {
+        if constexpr (NS > 1) {
+            const C<T> z = lf[k * STEP], z2 = lf[(2 * k) * STEP];
+            dft4_lf<INV>(v[0], v[1], v[2], v[3], z.x, z.y, z2.x, z2.y);
+        } else {
+            dft4<INV>(v[0], v[1], v[2], v[3]);
+        }
+    } else if constexpr (R == 2) {
+        if constexpr (NS > 1) {
+            const C<T> z = lf[k * STEP];
+            C<T> a, b;
+            lf_pm(v[0], lf_rot<INV>(v[1], z.y), z.x, a, b);
+            v[0] = a; v[1] = b;
+        } else {
+            dft2<INV>(v[0], v[1]);
+        }
+    } else {
+        static_assert(R == 3, "unsupported radix");
+        if constexpr (NS > 1) {
+#pragma unroll
+            for (int r = 1; r < 3; r++) {
+                const C<T> z = lf[(r * k) * STEP];
+                const C<T> u = lf_rot<INV>(v[r], z.y);
+                v[r] = mk<T>(u.x * z.x, u.y * z.x);
+            }
+        }
+        dft<3, INV>(v);
+    }
+}
+
 // --------------------------------------------------- pencil configuration
 // Per length: pencils per block (P), threads per block (NT) and radix
 // schedule (R1, R2, R3; 1 = unused).  Threads per pencil TPP = NT / P and every
@@ -169,7 +332,9 @@ struct Pencil {
     static constexpr size_t smem_bytes() { return DefSched<L>::template smem_bytes<T>(); }
 };
 
-// One Stockham pass of radix R with current sub-transform length NS.
+// One Stockham pass of radix R with current sub-transform length NS.  tw is
+// the staged twiddle table: (g, t) pairs for FP64 / FP32, (cos, sin) for
+// double-float.
 template <typename T, class S, int R, int NS, bool INV>
 __device__ __forceinline__ void stockham_pass(C<T>* tile, const C<T>* tw, int p, int jt) {
     constexpr int L = S::L, PS = S::PS, TPP = S::TPP;
@@ -188,15 +353,19 @@ __device__ __forceinline__ void stockham_pass(C<T>* tile, const C<T>* tw, int p,
     for (int b = 0; b < BPT; b++) {
         const int j = jt + TPP * b;
         const int k = j & (NS - 1);
-        if constexpr (NS > 1) {
-            constexpr int STEP = L / (NS * R);
+        if constexpr (IsLF<T>::value) {
+            bfly_lf<R, NS, L, INV>(v[b], tw, k);
+        } else {
+            if constexpr (NS > 1) {
+                constexpr int STEP = L / (NS * R);
 #pragma unroll
-            for (int r = 1; r < R; r++) {
-                const C<T> w = tw[(r * k) * STEP];
-                v[b][r] = INV ? cmulc(v[b][r], w) : cmul(v[b][r], w);
+                for (int r = 1; r < R; r++) {
+                    const C<T> w = tw[(r * k) * STEP];
+                    v[b][r] = INV ? cmulc(v[b][r], w) : cmul(v[b][r], w);
+                }
             }
+            dft<R, INV>(v[b]);
         }
-        dft<R, INV>(v[b]);
         const int d = (j - k) * R + k;
 #pragma unroll
         for (int r = 0; r < R; r++) tile[(d + r * NS) * PS + p] = v[b][r];

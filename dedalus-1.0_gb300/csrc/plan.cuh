@@ -13,7 +13,8 @@ struct dd_plan {
     double* kx;
     double* ky;
     double* kz;
-    // twiddle tables W_L^m, m < L, per axis length (device), fp64 and fp32
+    // twiddle tables W_L^m, m < L, per axis length (device): fp64 and fp32 as
+    // (g, t) with W = g (1 + i t) for the FMA butterflies, double-float as (cos, sin)
     double2* tw64_x; double2* tw64_y; double2* tw64_z;
     float2* tw32_x;  float2* tw32_y;  float2* tw32_z;
     float4* twdf_x;  float4* twdf_y;  float4* twdf_z;   // double-float (hi, lo) pairs

@@ -69,6 +69,11 @@ def main(argv=None):
     ap.add_argument("--calibrate-seeds", type=int, default=0)
     ap.add_argument("--backscatter", type=float, nargs="+", default=None, metavar="B",
                     help="also select among shell tables gain * ramp(10.5, 21) - B below 10.5 (gain 2)")
+    ap.add_argument("--fit-seeds", type=int, nargs="+", default=None,
+                    help="with --base: fit the closure-term weight table a posteriori against the FP64 DNS of "
+                         "these (training) seeds, then evaluate on --eval-seeds")
+    ap.add_argument("--fit-knots", type=float, nargs="+", default=[0.0, 3.0, 6.0, 9.0, 12.0, 16.0, 21.0, 30.0])
+    ap.add_argument("--fit-evals", type=int, default=300)
     ap.add_argument("--out", default=os.path.join(HERE, "les_closure_256to64.npz"))
     ap.add_argument("--report", default=None)
     ap.add_argument("--dump-samples", type=int, default=0, help="save this many random raw samples")
@@ -97,6 +102,8 @@ def main(argv=None):
     if a.base:
         models["stress"] = C.MLPClosure.load(a.base)
         rep["base"] = {"file": os.path.basename(a.base), "meta": models["stress"].meta}
+        if a.fit_seeds:
+            return fit_weights(a, C, rep, models["stress"], log, write_report)
         return finish(a, C, rep, models, band, log, write_report)
     raw, seeds, info = C.generate_dataset(a.seeds, a.snaps, a.stride, a.dns, a.les, a.nu, a.dt, a.seed0, log=log,
                                           band=band)
@@ -140,6 +147,53 @@ def main(argv=None):
     torch.cuda.empty_cache()
     write_report()
     finish(a, C, rep, models, band, log, write_report)
+
+
+def fit_weights(a, C, rep, base, log, write_report):
+    """A-posteriori fit of the closure-term weight table (closure.fit_posteriori)
+    on the training seeds a.fit_seeds, then evaluation of the fitted closure,
+    the starting one and the unclosed LES on a.eval_seeds against the FP64 DNS;
+    the fitted closure is saved to a.out."""
+    import numpy as np
+    knots = list(a.fit_knots)
+    if base.shell_w is not None:
+        start = np.interp(knots, np.arange(base.shell_w.numel()), base.shell_w.cpu().numpy())
+    else:
+        lo, hi = base.band
+        start = np.clip((np.asarray(knots) - lo) / max(hi - lo, 1e-9), 0.0, 1.0) if hi > 0 else np.ones(len(knots))
+    steps = a.eval_steps or 1000
+    refs = []
+    for s in a.fit_seeds:
+        refs.append(C.dns_reference(s, a.dns, a.les, a.nu, a.dt, steps, a.eval_every))
+        log("DNS reference seed %d: %.1f s" % (s, refs[-1]["seconds"]))
+    w, info = C.fit_posteriori(base, refs, knots, start, max_evals=a.fit_evals, log=log)
+    info["fit_seeds"] = list(a.fit_seeds)
+    rep["fit"] = info
+    log("fitted weights at %s: %s (score %.4f, start %.4f)" % (knots, np.round(w, 4).tolist(),
+                                                               info["best"]["score"], info["start"]["score"]))
+    write_report()
+    fitted = base.with_shells(C.shell_table(knots, w, a.les))
+    fitted.meta = dict(base.meta or {})
+    fitted.meta["posteriori_fit"] = {"knots": knots, "weights": [float(v) for v in w], "seeds": list(a.fit_seeds),
+                                     "score": info["best"]["score"], "steps": steps}
+    cands = {"fitted": fitted, "start": base, "no_model": None}
+    rep["eval"] = {}
+    for seed in (a.eval_seeds or [a.eval_seed]):
+        ref = C.dns_reference(seed, a.dns, a.les, a.nu, a.dt, steps, a.eval_every)
+        rep["eval"][str(seed)] = {}
+        for name, cl in cands.items():
+            t = C.les_trajectory(cl, ref)
+            rep["eval"][str(seed)][name] = {k: t[k] for k in ("steps", "err_half", "err_full", "diss_err")}
+            log("seed %d %s: max E(k) err k<=kmax/2 %.4f (final %.4f), max |diss err| %.4f (final %+.4f)" % (
+                seed, name, max(t["err_half"]), t["err_half"][-1], max(abs(v) for v in t["diss_err"][1:]),
+                t["diss_err"][-1]))
+        write_report()
+    fitted.meta["eval"] = {s: {"err_half_max": max(v["fitted"]["err_half"]),
+                               "diss_err_max_abs": max(abs(x) for x in v["fitted"]["diss_err"][1:])}
+                           for s, v in rep["eval"].items()}
+    fitted.save(a.out)
+    log("saved %s" % a.out)
+    write_report()
 
 
 def finish(a, C, rep, models, band, log, write_report):

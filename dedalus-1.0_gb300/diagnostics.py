@@ -87,13 +87,24 @@ def spectrum_bins(field):
     return kbottom, ktop
 
 
-def power_spectrum(field, norm=1.):
-    """(bin centres, mean power1d per bin) as PowerSpectrum._compute_spectrum."""
+def shell_bins(field):
+    """Unit-width shells centred on the integers: [k - 1/2, k + 1/2) for
+    k = 0 .. the largest |k| of the grid (the first shell starts at 0)."""
+    c0 = field[0]
+    kmax = np.sqrt(np.sum(c0.kny ** 2))
+    k = np.arange(int(np.ceil(kmax)) + 2, dtype=np.float64)
+    return np.maximum(k - 0.5, 0.0), k + 0.5
+
+
+def power_spectrum(field, norm=1., shells=False):
+    """(bin centres, mean power1d per bin) as PowerSpectrum._compute_spectrum;
+    with shells=True the same estimator over unit shells centred on the
+    integers (shell_bins) instead of the reference's bins."""
     comps = _comps(field)
     plan = comps[0].plan
     for c in comps:
         c.require_space('kspace')
-    kbottom, ktop = spectrum_bins(field)
+    kbottom, ktop = shell_bins(field) if shells else spectrum_bins(field)
     nb = kbottom.size
     n = ctypes.c_size_t()
     _lib.call("dd_diag_workspace_size", plan.handle, nb, ctypes.byref(n))
@@ -103,9 +114,12 @@ def power_spectrum(field, norm=1.):
     s = torch.empty(nb, dtype=torch.float64, device=plan.device)
     cnt = torch.empty(nb, dtype=torch.float64, device=plan.device)
     ptrs, _keep = _lib.ptr_array([c.kdata.data_ptr() for c in comps])
-    _lib.call("dd_spectrum", plan.handle, len(comps), ptrs, float(norm), nb, dptr(kb), dptr(kt), float(kbottom[1]),
+    dk = float(ktop[0] - kbottom[0]) if not shells else 1.0
+    _lib.call("dd_spectrum", plan.handle, len(comps), ptrs, float(norm), nb, dptr(kb), dptr(kt), dk,
               dptr(s), dptr(cnt), dptr(ws), ws.numel(), current_stream())
     spec = s.cpu().numpy()
     counts = cnt.cpu().numpy()
     counts[counts == 0] = 1.
+    if shells:
+        return np.arange(nb, dtype=np.float64), spec / counts
     return kbottom + kbottom[1] / 2., spec / counts
