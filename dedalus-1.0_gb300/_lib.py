@@ -47,6 +47,8 @@ SIGNATURES = {
     "dd_deriv": [P, I, P, P, P],
     "dd_scale_add": [P, P, D, I, I64, P],
     "dd_max_square": [I, PP, I64, P, P],
+    "dd_plan_set_schedule": [P, I, I],
+    "dd_plan_get_schedule": [P, I, ctypes.POINTER(I), ctypes.POINTER(I)],
     "dd_euler": [P, P, P, D, I64, P],
     "dd_etd1": [I, P, P, P, P, D, I64, P],
     "dd_etd2rk1": [I, P, P, P, P, P, D, I64, P],

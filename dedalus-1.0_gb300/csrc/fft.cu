@@ -164,6 +164,23 @@ int dd_plan_destroy(dd_plan* p) {
     return DD_OK;
 }
 
+int dd_plan_set_schedule(dd_plan* p, int which, int variant) {
+    DD_CHECK_ARG(p, "dd_plan_set_schedule: null plan");
+    DD_CHECK_ARG(which == 0, "dd_plan_set_schedule: unknown pass group %d", which);
+    DD_CHECK_ARG(variant >= 0 && variant < kYSchedVariants, "dd_plan_set_schedule: variant %d out of range", variant);
+    p->sched_y2d = variant;
+    return DD_OK;
+}
+
+int dd_plan_get_schedule(const dd_plan* p, int which, int* variant, int* count) {
+    DD_CHECK_ARG(p && variant && count, "dd_plan_get_schedule: null pointer");
+    DD_CHECK_ARG(which == 0, "dd_plan_get_schedule: unknown pass group %d", which);
+    *variant = p->sched_y2d;
+    const int n = p->ndim == 2 ? p->g2.Ny : 0;
+    *count = (n == 64 || n == 128 || n == 256 || n == 512) ? kYSchedVariants : 1;
+    return DD_OK;
+}
+
 int dd_plan_workspace_size(const dd_plan* p, int nfield, int precision, size_t* bytes) {
     DD_CHECK_ARG(p && bytes, "dd_plan_workspace_size: null pointer");
     DD_CHECK_ARG(nfield >= 1 && nfield <= 8, "nfield must be in [1, 8]");

@@ -126,6 +126,34 @@ int launch_pass_small(int L, const Op& op, int npencil, int nslow, int nfield, c
     return 1;
 }
 
+// Tile variants of the default schedule for the 2D y passes of 64..512-point
+// grids, chosen per plan by the ensemble autotuner (dd_plan_set_schedule):
+// the same radix sequence as the default (so every pencil's arithmetic, and
+// its result, is identical) on fewer pencils per block: variant 1 the
+// smallest tile (2-4 pencils), variant 2 a middle one (4-8 pencils).
+constexpr int kYSchedVariants = 3;
+template <int L, int V> struct YVariant;
+template <> struct YVariant<64, 1>  { using S = Sched<64, 4, 32, 8, 8, 1>; };
+template <> struct YVariant<64, 2>  { using S = Sched<64, 8, 64, 8, 8, 1>; };
+template <> struct YVariant<128, 1> { using S = Sched<128, 4, 32, 16, 8, 1>; };
+template <> struct YVariant<128, 2> { using S = Sched<128, 8, 64, 16, 8, 1>; };
+template <> struct YVariant<256, 1> { using S = Sched<256, 4, 64, 16, 16, 1>; };
+template <> struct YVariant<256, 2> { using S = Sched<256, 8, 128, 16, 16, 1>; };
+template <> struct YVariant<512, 1> { using S = Sched<512, 2, 64, 8, 8, 8>; };
+template <> struct YVariant<512, 2> { using S = Sched<512, 4, 128, 8, 8, 8>; };
+
+// Launch a pass with tile variant v (1 or 2) of length L; returns 1 (not
+// launched) when no variant exists.
+template <typename T, bool INV, bool LD_E, bool ST_E, class Op>
+int launch_pass_variant(int L, int v, const Op& op, int npencil, int nslow, int nfield, cudaStream_t st) {
+#define DD_YV(N, VV) \
+    if (L == N && v == VV) \
+        return launch_pass_sched<T, typename YVariant<N, VV>::S, INV, LD_E, ST_E>(op, npencil, nslow, nfield, st);
+    DD_YV(64, 1) DD_YV(64, 2) DD_YV(128, 1) DD_YV(128, 2) DD_YV(256, 1) DD_YV(256, 2) DD_YV(512, 1) DD_YV(512, 2)
+#undef DD_YV
+    return 1;
+}
+
 // ============================================================ 3D operators
 // Inverse along kz: K[ky][kz][kx] (kept entries) -> W1[kyc][z][kxc].
 template <typename T, typename KT>

@@ -20,6 +20,8 @@ struct dd_plan {
     float4* twdf_x;  float4* twdf_y;  float4* twdf_z;   // double-float (hi, lo) pairs
     // rounded-down 1/N_total used by the forward transform
     double inv_n;
+    // tile schedule of the fused 2D y passes (dd_plan_set_schedule; 0 = default)
+    int sched_y2d;
 };
 
 namespace dd {

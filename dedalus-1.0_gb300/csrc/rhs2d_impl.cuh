@@ -167,10 +167,15 @@ int nonlinear2(const dd_plan* pl, const Work2& w, const void* const* st, int64_t
     for (int f = 0; f < PH::NO; f++) nc.p[f] = w.NC<T>(f);
     // one run of a 64- or 128-point grid: small tiles, so that the y passes
     // have enough blocks (the default 32-pencil tiles give 2 per field)
-    const bool small = w.nrun == 1 && (g.Ny == 64 || g.Ny == 128);
+    // (a tuned tile variant, set on the plan, takes precedence)
+    const int yv = pl->sched_y2d;
+    const bool small = yv == 0 && w.nrun == 1 && (g.Ny == 64 || g.Ny == 128);
     OpYInvPhys2<T, COMPACT, PHYS> a{g, sin, st_rs, wo, (int64_t)w.w, TwSel<T>::y(pl), pl->kx, pl->ky};
-    if (small) DD_TRY((launch_pass_small<T, true, true, false>(g.Ny, a, g.Kx, w.nrun, PH::NI, s)));
-    else DD_TRY((launch_pass_len<T, true, true, false>(g.Ny, a, g.Kx, w.nrun, PH::NI, s)));
+    int rc = 1;
+    if (yv) rc = launch_pass_variant<T, true, true, false>(g.Ny, yv, a, g.Kx, w.nrun, PH::NI, s);
+    if (rc == 1 && small) rc = launch_pass_small<T, true, true, false>(g.Ny, a, g.Kx, w.nrun, PH::NI, s);
+    if (rc == 1) rc = launch_pass_len<T, true, true, false>(g.Ny, a, g.Kx, w.nrun, PH::NI, s);
+    DD_TRY(rc);
     if constexpr (PHYS == PHYS_HYDRO_DIV) {
         DD_TRY((launch_x_prod_len<T>("x_div_hydro2d", g.Nx, g.Ny, g.Kx, wi, wo, w.nrun, (int64_t)w.w, (int64_t)w.w,
                                      TwSel<T>::x(pl), (T)pl->inv_n, ProdHydroDiv2<T>{}, s)));
@@ -185,8 +190,11 @@ int nonlinear2(const dd_plan* pl, const Work2& w, const void* const* st, int64_t
                                      TwSel<T>::x(pl), (T)pl->inv_n, ProdBouss2<T>{}, s)));
     }
     OpYFwdCompact2<T> c{g, wi, (int64_t)w.w, nc, (int64_t)w.kc, TwSel<T>::y(pl)};
-    if (small) DD_TRY((launch_pass_small<T, false, false, true>(g.Ny, c, g.Kx, w.nrun, PH::NO, s)));
-    else DD_TRY((launch_pass_len<T, false, false, true>(g.Ny, c, g.Kx, w.nrun, PH::NO, s)));
+    rc = 1;
+    if (yv) rc = launch_pass_variant<T, false, false, true>(g.Ny, yv, c, g.Kx, w.nrun, PH::NO, s);
+    if (rc == 1 && small) rc = launch_pass_small<T, false, false, true>(g.Ny, c, g.Kx, w.nrun, PH::NO, s);
+    if (rc == 1) rc = launch_pass_len<T, false, false, true>(g.Ny, c, g.Kx, w.nrun, PH::NO, s);
+    DD_TRY(rc);
     return DD_OK;
 }
 

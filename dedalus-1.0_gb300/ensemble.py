@@ -10,9 +10,14 @@ classes are issued on their own CUDA streams, and a complete ensemble step
 (every class, every chunk) is captured once into a CUDA graph and replayed, so
 an ensemble step costs one graph launch on the host.
 
-``autotune`` measures, per size class, the chunking of its runs (runs per
-launch) and the order in which classes are issued, keeps the fastest schedule
-and caches it in a JSON file keyed by GPU, size, run count and precision.
+``autotune`` measures, per size class, the tile schedule of its y passes
+(dd_plan_set_schedule: the default tile or two smaller ones with the same
+radix sequence, so results are bitwise unchanged for classes of more than
+one run), the chunking of its runs
+(runs per launch) and the order in which classes are issued, keeps the
+fastest schedule and caches it in a JSON file keyed by GPU, size, run count
+and precision.  Each size class owns its plan, so a tuned schedule does not
+leak into other users of the same grid size.
 """
 import ctypes
 import json
@@ -23,7 +28,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .engine import get_plan, dptr
+from .engine import Plan, dptr
 from . import init_cond
 
 PHYS_BOUSS = 1
@@ -42,7 +47,8 @@ class _SizeClass:
         self.runs = list(runs)                    # global run indices
         self.nrun = len(self.runs)
         self.shape = (n, n)
-        self.plan = get_plan(self.shape, (2 * np.pi, 2 * np.pi), '2/3 cython')
+        self.plan = Plan(self.shape, (2 * np.pi, 2 * np.pi), '2/3 cython')   # own plan: own tile schedule
+        self.ysched = 0
         kx, ky = self.plan.kshape
         self.kshape = (kx, ky)
         self.fsize = kx * ky                      # complex entries per field
@@ -52,6 +58,15 @@ class _SizeClass:
         self.ws = None
         self.stream = torch.cuda.Stream(device=device)
         self.phys = PHYS_BOUSS
+
+    def set_ysched(self, v):
+        _lib.call("dd_plan_set_schedule", self.plan.handle, 0, int(v))
+        self.ysched = int(v)
+
+    def ysched_count(self):
+        v, n = ctypes.c_int(), ctypes.c_int()
+        _lib.call("dd_plan_get_schedule", self.plan.handle, 0, ctypes.byref(v), ctypes.byref(n))
+        return n.value
 
     def workspace(self, chunk):
         n = ctypes.c_size_t()
@@ -275,8 +290,9 @@ class BoussinesqEnsemble2D:
         return a.elapsed_time(b) / reps
 
     def autotune(self, dt, cache=None, chunks=(None, 128, 64, 32, 16), verbose=False):
-        """Choose per-class run chunking and the class issue order by timing
-        graph replays; results are cached as JSON.  Returns the schedule."""
+        """Choose per class the y-pass tile schedule and the run chunking, and
+        the class issue order, by timing graph replays; results are cached as
+        JSON.  Returns the schedule."""
         cache = cache or _default_cache()
         gpu = torch.cuda.get_device_name(self.device)
         key = "%s|%s|%s|%s" % (gpu, self.precision, ",".join(str(c.n) for c in self.classes),
@@ -291,13 +307,26 @@ class BoussinesqEnsemble2D:
             sched = db[key]
             for c, ch in zip(self.classes, sched["chunks"]):
                 c.chunk = ch
+            for c, ys in zip(self.classes, sched.get("ysched", [0] * len(self.classes))):
+                c.set_ysched(ys)
             self.order = sched["order"]
             self._graph = None
             return sched
-        # largest classes first, then refine each class's chunk in turn
+        # largest classes first, then refine each class's tile schedule and chunk in turn
         self.order = sorted(range(len(self.classes)), key=lambda i: -self.classes[i].n ** 2 * self.classes[i].nrun)
         best = self._time_schedule(dt)
         for c in self.classes:
+            best_ys = c.ysched
+            for ys in range(c.ysched_count()):
+                if ys == best_ys:
+                    continue
+                c.set_ysched(ys)
+                t = self._time_schedule(dt)
+                if verbose:
+                    print("class %d y tiles %d: %.3f ms" % (c.n, ys, t))
+                if t < best:
+                    best, best_ys = t, ys
+            c.set_ysched(best_ys)
             best_ch = c.chunk
             for ch in chunks:
                 cand = c.nrun if ch is None else min(ch, c.nrun)
@@ -318,7 +347,8 @@ class BoussinesqEnsemble2D:
             self.order = saved_order
         else:
             best = t
-        sched = {"chunks": [c.chunk for c in self.classes], "order": self.order, "ms_per_step": best,
+        sched = {"chunks": [c.chunk for c in self.classes], "ysched": [c.ysched for c in self.classes],
+                 "order": self.order, "ms_per_step": best,
                  "when": time.strftime("%Y-%m-%dT%H:%M:%S")}
         db[key] = sched
         try:

@@ -73,6 +73,18 @@ int dd_plan_create(int ndim, const int64_t* xshape, const double* kx, const doub
                    const double* kz, int mx, int my, int mz, dd_plan** out);
 int dd_plan_destroy(dd_plan* plan);
 
+/* Tile schedule of a pass group of this plan (which = 0: the y passes of the
+ * fused 2D steps, dd_rhs2d / dd_rk2mid_step2d): variant 0 is the default,
+ * 1 and 2 run the default tile's radix sequence on smaller tiles (bitwise the
+ * same results, except against a single run of 64 or 128 points, whose
+ * default is the small-tile schedule with its own radix sequence); dd_plan_get_schedule reports the current variant and how many this
+ * plan's length offers (3 for 64, 128, 256, 512 points, else 1; a variant
+ * the length lacks runs the default).  Set by the ensemble autotuner.  No
+ * counterpart in the reference (FFTW chooses its own plans:
+ * dedalus/utils/fftw/_fftw.pyx:246-309, flags FFTW_MEASURE). */
+int dd_plan_set_schedule(dd_plan* plan, int which, int variant);
+int dd_plan_get_schedule(const dd_plan* plan, int which, int* variant, int* count);
+
 /* Scratch bytes needed by dd_fft_* for `nfield` fields at `precision`. */
 int dd_plan_workspace_size(const dd_plan* plan, int nfield, int precision, size_t* bytes);
 
