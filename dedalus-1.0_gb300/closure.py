@@ -621,11 +621,13 @@ def evaluate(models, seed=7, dns_n=256, les_n=64, nu=5e-3, dt=2e-3, nsteps=1000,
 
 
 # ------------------------------------------------- a-posteriori weight fit
-def dns_reference(seed, dns_n=256, les_n=64, nu=5e-3, dt=2e-3, nsteps=1000, every=100, sampler=None):
+def dns_reference(seed, dns_n=256, les_n=64, nu=5e-3, dt=2e-3, nsteps=1000, every=100, sampler=None,
+                  full_spectrum=False):
     """One plain FP64 DNS trajectory as the judge of an LES: the filtered
     initial state on the LES grid (device k arrays) and, every `every` steps,
     the filtered-DNS spectrum E(k) and the DNS dissipation rate
-    2 nu <|curl u|^2> / 2 (volume_average.py:254-265)."""
+    2 nu <|curl u|^2> / 2 (volume_average.py:254-265); with full_spectrum,
+    also the DNS's own spectrum on its grid ("E_dns", bin centres "kc_dns")."""
     from . import mods, diagnostics as D
     from .init_cond import turbulence_3d
     shape = (dns_n,) * 3
@@ -658,6 +660,10 @@ def dns_reference(seed, dns_n=256, les_n=64, nu=5e-3, dt=2e-3, nsteps=1000, ever
             ref["E"].append(np.asarray(e))
             ref["Es"].append(np.asarray(es))
             ref["diss"].append(D.energy_dissipation(dd, nu))
+            if full_spectrum:
+                kd, ed = D.power_spectrum(dd['u'])
+                ref["kc_dns"] = np.asarray(kd)
+                ref.setdefault("E_dns", []).append(np.asarray(ed))
     torch.cuda.synchronize()
     ref["seconds"] = time.time() - t0
     ref["kmax"] = sampler.les.mx

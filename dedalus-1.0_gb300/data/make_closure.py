@@ -183,7 +183,8 @@ def fit_weights(a, C, rep, base, log, write_report):
         rep["eval"][str(seed)] = {}
         for name, cl in cands.items():
             t = C.les_trajectory(cl, ref)
-            rep["eval"][str(seed)][name] = {k: t[k] for k in ("steps", "err_half", "err_full", "diss_err")}
+            rep["eval"][str(seed)][name] = {k: t[k] for k in ("steps", "err_half", "err_half_shells", "err_full",
+                                                               "diss_err", "closure_input")}
             log("seed %d %s: max E(k) err k<=kmax/2 %.4f (final %.4f), max |diss err| %.4f (final %+.4f)" % (
                 seed, name, max(t["err_half"]), t["err_half"][-1], max(abs(v) for v in t["diss_err"][1:]),
                 t["diss_err"][-1]))

@@ -355,19 +355,28 @@ def test_les_rk4_step_matches_oracle(dd, cuda, fused):
 
 
 @pytest.mark.gpu
-def test_trained_closure_beats_no_model(dd, cuda):
-    """The committed network (trained on filtered FP64 256^3 DNS, seeds
-    1000-1049; target, band and gain chosen on seed 11) against the unclosed
-    64^3 LES on a seed used for neither (13): after 500 steps (t = 1) its
-    spectrum is closer to the filtered DNS over all resolved k, and it drains
-    energy on average."""
+def test_trained_closure_meets_the_bar_and_beats_no_model(dd, cuda):
+    """The committed closure -- the network trained on filtered FP64 256^3 DNS
+    (seeds 1000-1049) with its closure-term weight table fitted a posteriori
+    on training seeds 1000-1002 -- on a seed used for neither (13), over the
+    configured 1000 LES steps from the filtered DNS state: the E(k) error
+    against the filtered FP64 DNS stays within 5% for k <= kmax/2 (the
+    reference's spectrum bins, analysis_set.py:778-815) and the LES energy
+    loss rate (resolved dissipation minus the closure's energy input) within
+    5% of the DNS dissipation rate at every check; the unclosed LES misses the
+    spectrum bar and does worse over all resolved k."""
     C = dd.closure
     if not os.path.isfile(C.DEFAULT_WEIGHTS):
         pytest.fail("trained weights missing: %s" % C.DEFAULT_WEIGHTS)
     cl = C.MLPClosure.load()
     assert cl.meta["data"]["n_seeds"] == 50 and cl.meta["data"]["n_snap"] == 20
-    assert cl.band == (10.5, 21.0) and cl.gain == 2.0
-    ev = C.evaluate({"closure": cl, "no_model": None}, seed=13, nsteps=500, every=500)
-    c, n = ev["closure"], ev["no_model"]
-    assert c["err_full"][-1] < n["err_full"][-1], (c["err_full"], n["err_full"])
-    assert c["diss_sgs"][-1] > 0.0
+    assert cl.shell_w is not None and cl.meta["posteriori_fit"]["seeds"] == [1000, 1001, 1002]
+    ref = C.dns_reference(13, nsteps=1000, every=100)
+    c = C.les_trajectory(cl, ref)
+    n = C.les_trajectory(None, ref)
+    print("seed 13: closure E(k) %.4f diss %.4f; no model E(k) %.4f" % (
+        max(c["err_half"]), max(abs(v) for v in c["diss_err"][1:]), max(n["err_half"])))
+    assert max(c["err_half"]) <= 0.05, c["err_half"]
+    assert max(abs(v) for v in c["diss_err"][1:]) <= 0.05, c["diss_err"]
+    assert max(n["err_half"]) > 0.05
+    assert max(c["err_full"]) < max(n["err_full"])
