@@ -188,11 +188,70 @@ __device__ __forceinline__ void dft4_lf_zsq_w4(C<T>& x0, C<T>& x1, C<T>& x2, C<T
     lf_pm(B, mul_mi<INV>(lf_rot<INV>(Dp, t1)), g1, x1, x3);
 }
 
+// --------------------------------------------------- 2/3-band pruning
+// Under the 2/3 rule an L-point axis keeps |mode index| <= kept23(L); the
+// band kept23(L) < i < L - kept23(L) is zero on the way in (inverse
+// transforms) and discarded on the way out (forward transforms).
+__host__ __device__ constexpr int kept23(int L) { return (L + 2) / 3 - 1; }
+
+// Bit r set: in a radix-R pass of L points whose butterfly j touches the
+// elements j + r (L/R) (first pass: inputs; last pass: outputs), all L/R of
+// them lie in the 2/3 band.  Only radices 8 and 16 use it.
+template <int L, int R>
+constexpr unsigned band_mask() {
+    if (R != 8 && R != 16) return 0u;
+    unsigned m = 0u;
+    const int NB = L / R, K = kept23(L);
+    for (int r = 0; r < R; r++)
+        if (r * NB > K && (r + 1) * NB - 1 < L - K) m |= 1u << r;
+    return m;
+}
+
+// dft4 of (a0, a1, a2, a3) with the inputs flagged Zi known to be zero (at
+// most one per pair (a0, a2), (a1, a3)): the additions with a zero vanish.
+template <bool INV, bool Z0, bool Z1, bool Z2, bool Z3, typename T>
+__device__ __forceinline__ void dft4_zin(C<T>& a0, C<T>& a1, C<T>& a2, C<T>& a3) {
+    static_assert(!(Z0 && Z2) && !(Z1 && Z3), "at most one zero input per pair");
+    C<T> t0, t1, t2, t3;
+    if constexpr (Z2) { t0 = a0; t1 = a0; }
+    else if constexpr (Z0) { t0 = a2; t1 = mk<T>(-a2.x, -a2.y); }
+    else { t0 = a0 + a2; t1 = a0 - a2; }
+    if constexpr (Z3) { t2 = a1; t3 = mul_mi<INV>(a1); }
+    else if constexpr (Z1) { t2 = a3; t3 = mul_mi<INV>(mk<T>(-a3.x, -a3.y)); }
+    else { t2 = a1 + a3; t3 = mul_mi<INV>(a1 - a3); }
+    a0 = t0 + t2; a2 = t0 - t2; a1 = t1 + t3; a3 = t1 - t3;
+}
+
+// dft4_lf computing only the outputs not flagged Di (the others keep
+// whatever they held).
+template <bool INV, bool D0, bool D1, bool D2, bool D3, typename T>
+__device__ __forceinline__ void dft4_lf_out(C<T>& x0, C<T>& x1, C<T>& x2, C<T>& x3, T g1, T t1, T g2, T t2) {
+    C<T> A, B, Cp, Dp;
+    lf_pm(x0, lf_rot<INV>(x2, t2), g2, A, B);
+    lf_pm(x1, lf_rot<INV>(x3, t2), g2, Cp, Dp);
+    if constexpr (!(D0 && D2)) {
+        const C<T> p = lf_rot<INV>(Cp, t1);
+        if constexpr (!D0) x0 = mk<T>(fmx(g1, p.x, A.x), fmx(g1, p.y, A.y));
+        if constexpr (!D2) x2 = mk<T>(fmx(-g1, p.x, A.x), fmx(-g1, p.y, A.y));
+    }
+    if constexpr (!(D1 && D3)) {
+        const C<T> q = mul_mi<INV>(lf_rot<INV>(Dp, t1));
+        if constexpr (!D1) x1 = mk<T>(fmx(g1, q.x, B.x), fmx(g1, q.y, B.y));
+        if constexpr (!D3) x3 = mk<T>(fmx(-g1, q.x, B.x), fmx(-g1, q.y, B.y));
+    }
+}
+
+template <unsigned M, int B>
+constexpr bool bit() { return (M >> B) & 1u; }
+
 // Radix-R butterfly of Stockham pass NS on v[0..R-1] (natural order in and
 // out), with the inter-pass twiddles w^r, w = W_(NS R)^k, taken from the
-// staged (g, t) table lf (W_L^m at index m).
-template <int R, int NS, int L, bool INV, typename T>
+// staged (g, t) table lf (W_L^m at index m).  ZIN (first pass only): inputs
+// v[r] known zero; ZOUT (a pass with NS > 1 only): outputs v[r] not needed.
+template <int R, int NS, int L, bool INV, unsigned ZIN = 0u, unsigned ZOUT = 0u, typename T>
 __device__ __forceinline__ void bfly_lf(C<T>* v, const C<T>* lf, int k) {
+    static_assert(ZIN == 0u || NS == 1, "zero inputs only in a first pass");
+    static_assert(ZOUT == 0u || NS > 1, "discarded outputs only in a later pass");
     constexpr int STEP = L / (NS * R);
     if constexpr (R == 16) {
         if constexpr (NS > 1) {
@@ -200,10 +259,13 @@ __device__ __forceinline__ void bfly_lf(C<T>* v, const C<T>* lf, int k) {
 #pragma unroll
             for (int n2 = 0; n2 < 4; n2++) dft4_lf<INV>(v[n2], v[4 + n2], v[8 + n2], v[12 + n2], a4.x, a4.y, a8.x, a8.y);
         } else {
-#pragma unroll
-            for (int n2 = 0; n2 < 4; n2++) dft4<INV>(v[n2], v[4 + n2], v[8 + n2], v[12 + n2]);
+            dft4_zin<INV, bit<ZIN, 0>(), bit<ZIN, 4>(), bit<ZIN, 8>(), bit<ZIN, 12>()>(v[0], v[4], v[8], v[12]);
+            dft4_zin<INV, bit<ZIN, 1>(), bit<ZIN, 5>(), bit<ZIN, 9>(), bit<ZIN, 13>()>(v[1], v[5], v[9], v[13]);
+            dft4_zin<INV, bit<ZIN, 2>(), bit<ZIN, 6>(), bit<ZIN, 10>(), bit<ZIN, 14>()>(v[2], v[6], v[10], v[14]);
+            dft4_zin<INV, bit<ZIN, 3>(), bit<ZIN, 7>(), bit<ZIN, 11>(), bit<ZIN, 15>()>(v[3], v[7], v[11], v[15]);
         }
-        // now v[4 k1 + n2] = Y'[n2][k1]; second sub-DFTs over n2 with z = w W16^k1
+        // now v[4 k1 + n2] = Y'[n2][k1]; second sub-DFTs over n2 with z = w W16^k1,
+        // whose outputs are X[k1 + 4 k2]
         C<T> y[4][4];
 #pragma unroll
         for (int k1 = 0; k1 < 4; k1++) {
@@ -212,7 +274,18 @@ __device__ __forceinline__ void bfly_lf(C<T>* v, const C<T>* lf, int k) {
             if constexpr (NS > 1) {
                 const int e = k + k1 * NS;
                 const C<T> z = lf[e * STEP], z2 = lf[(2 * e) * STEP];
-                dft4_lf<INV>(y[k1][0], y[k1][1], y[k1][2], y[k1][3], z.x, z.y, z2.x, z2.y);
+                if (k1 == 0)
+                    dft4_lf_out<INV, bit<ZOUT, 0>(), bit<ZOUT, 4>(), bit<ZOUT, 8>(), bit<ZOUT, 12>()>(
+                        y[0][0], y[0][1], y[0][2], y[0][3], z.x, z.y, z2.x, z2.y);
+                else if (k1 == 1)
+                    dft4_lf_out<INV, bit<ZOUT, 1>(), bit<ZOUT, 5>(), bit<ZOUT, 9>(), bit<ZOUT, 13>()>(
+                        y[1][0], y[1][1], y[1][2], y[1][3], z.x, z.y, z2.x, z2.y);
+                else if (k1 == 2)
+                    dft4_lf_out<INV, bit<ZOUT, 2>(), bit<ZOUT, 6>(), bit<ZOUT, 10>(), bit<ZOUT, 14>()>(
+                        y[2][0], y[2][1], y[2][2], y[2][3], z.x, z.y, z2.x, z2.y);
+                else
+                    dft4_lf_out<INV, bit<ZOUT, 3>(), bit<ZOUT, 7>(), bit<ZOUT, 11>(), bit<ZOUT, 15>()>(
+                        y[3][0], y[3][1], y[3][2], y[3][3], z.x, z.y, z2.x, z2.y);
             } else if (k1 == 0) {
                 dft4<INV>(y[0][0], y[0][1], y[0][2], y[0][3]);
             } else if (k1 == 1) {   // z = W16, z^2 = W8
@@ -234,8 +307,8 @@ __device__ __forceinline__ void bfly_lf(C<T>* v, const C<T>* lf, int k) {
 #pragma unroll
             for (int n2 = 0; n2 < 2; n2++) dft4_lf<INV>(v[n2], v[2 + n2], v[4 + n2], v[6 + n2], a2.x, a2.y, a4.x, a4.y);
         } else {
-#pragma unroll
-            for (int n2 = 0; n2 < 2; n2++) dft4<INV>(v[n2], v[2 + n2], v[4 + n2], v[6 + n2]);
+            dft4_zin<INV, bit<ZIN, 0>(), bit<ZIN, 2>(), bit<ZIN, 4>(), bit<ZIN, 6>()>(v[0], v[2], v[4], v[6]);
+            dft4_zin<INV, bit<ZIN, 1>(), bit<ZIN, 3>(), bit<ZIN, 5>(), bit<ZIN, 7>()>(v[1], v[3], v[5], v[7]);
         }
         // v[2 k1 + n2] = Y'[n2][k1]; radix-2 steps with z = w W8^k1
         C<T> X[8];
@@ -244,7 +317,10 @@ __device__ __forceinline__ void bfly_lf(C<T>* v, const C<T>* lf, int k) {
             const C<T> y0 = v[2 * k1], y1 = v[2 * k1 + 1];
             if constexpr (NS > 1) {
                 const C<T> z = lf[(k + k1 * NS) * STEP];
-                lf_pm(y0, lf_rot<INV>(y1, z.y), z.x, X[k1], X[k1 + 4]);
+                if (((ZOUT >> k1) & 1u) && ((ZOUT >> (k1 + 4)) & 1u)) continue;
+                const C<T> u = lf_rot<INV>(y1, z.y);
+                if (!((ZOUT >> k1) & 1u)) X[k1] = mk<T>(fmx(z.x, u.x, y0.x), fmx(z.x, u.y, y0.y));
+                if (!((ZOUT >> (k1 + 4)) & 1u)) X[k1 + 4] = mk<T>(fmx(-z.x, u.x, y0.x), fmx(-z.x, u.y, y0.y));
             } else if (k1 == 0) {
                 X[0] = y0 + y1; X[4] = y0 - y1;
             } else if (k1 == 1) {
@@ -335,7 +411,7 @@ struct Pencil {
 // One Stockham pass of radix R with current sub-transform length NS.  tw is
 // the staged twiddle table: (g, t) pairs for FP64 / FP32, (cos, sin) for
 // double-float.
-template <typename T, class S, int R, int NS, bool INV>
+template <typename T, class S, int R, int NS, bool INV, unsigned ZIN = 0u, unsigned ZOUT = 0u>
 __device__ __forceinline__ void stockham_pass(C<T>* tile, const C<T>* tw, int p, int jt) {
     constexpr int L = S::L, PS = S::PS, TPP = S::TPP;
     constexpr int NB = L / R;          // butterflies per pencil
@@ -346,7 +422,7 @@ __device__ __forceinline__ void stockham_pass(C<T>* tile, const C<T>* tw, int p,
     for (int b = 0; b < BPT; b++) {
         const int j = jt + TPP * b;
 #pragma unroll
-        for (int r = 0; r < R; r++) v[b][r] = tile[(j + r * NB) * PS + p];
+        for (int r = 0; r < R; r++) v[b][r] = ((ZIN >> r) & 1u) ? zero<T>() : tile[(j + r * NB) * PS + p];
     }
     __syncthreads();
 #pragma unroll
@@ -354,7 +430,7 @@ __device__ __forceinline__ void stockham_pass(C<T>* tile, const C<T>* tw, int p,
         const int j = jt + TPP * b;
         const int k = j & (NS - 1);
         if constexpr (IsLF<T>::value) {
-            bfly_lf<R, NS, L, INV>(v[b], tw, k);
+            bfly_lf<R, NS, L, INV, ZIN, ZOUT>(v[b], tw, k);
         } else {
             if constexpr (NS > 1) {
                 constexpr int STEP = L / (NS * R);
@@ -368,7 +444,8 @@ __device__ __forceinline__ void stockham_pass(C<T>* tile, const C<T>* tw, int p,
         }
         const int d = (j - k) * R + k;
 #pragma unroll
-        for (int r = 0; r < R; r++) tile[(d + r * NS) * PS + p] = v[b][r];
+        for (int r = 0; r < R; r++)
+            if (!((ZOUT >> r) & 1u)) tile[(d + r * NS) * PS + p] = v[b][r];
     }
     __syncthreads();
 }
@@ -377,14 +454,30 @@ __device__ __forceinline__ void stockham_pass(C<T>* tile, const C<T>* tw, int p,
 // threads of the block (all of them must reach the barriers: threads beyond
 // S::NT call with active = false).  The caller synchronises before (tile
 // filled); this returns synchronised with the result in natural order.
-template <typename T, class S, bool INV>
+// PRUNE (FP64 / FP32 only, with at least two passes): the pencils follow the
+// 2/3 rule, so an inverse transform's first pass skips the inputs in the
+// removed band (they are zero) and a forward transform's last pass skips the
+// outputs in it (the caller never reads them; those tile entries are left
+// stale).
+template <typename T, class S, bool INV, bool PRUNE = false>
 __device__ __forceinline__ void pencil_fft_s(C<T>* tile, const C<T>* tw, bool active = true) {
     const int p = active ? threadIdx.x % S::P : 0;
     const int jt = active ? threadIdx.x / S::P : 0;
+    constexpr bool PR = PRUNE && IsLF<T>::value && S::R2 > 1;
+    constexpr int RL = S::R3 > 1 ? S::R3 : S::R2;
+    constexpr unsigned ZI = (PR && INV) ? band_mask<S::L, S::R1>() : 0u;
+    constexpr unsigned ZO = (PR && !INV) ? band_mask<S::L, RL>() : 0u;
     if (active) {
-        stockham_pass<T, S, S::R1, 1, INV>(tile, tw, p, jt);
-        if constexpr (S::R2 > 1) stockham_pass<T, S, S::R2, S::R1, INV>(tile, tw, p, jt);
-        if constexpr (S::R3 > 1) stockham_pass<T, S, S::R3, S::R1 * S::R2, INV>(tile, tw, p, jt);
+        if constexpr (S::R3 > 1) {
+            stockham_pass<T, S, S::R1, 1, INV, ZI>(tile, tw, p, jt);
+            stockham_pass<T, S, S::R2, S::R1, INV>(tile, tw, p, jt);
+            stockham_pass<T, S, S::R3, S::R1 * S::R2, INV, 0u, ZO>(tile, tw, p, jt);
+        } else if constexpr (S::R2 > 1) {
+            stockham_pass<T, S, S::R1, 1, INV, ZI>(tile, tw, p, jt);
+            stockham_pass<T, S, S::R2, S::R1, INV, 0u, ZO>(tile, tw, p, jt);
+        } else {
+            stockham_pass<T, S, S::R1, 1, INV>(tile, tw, p, jt);
+        }
     } else {
         __syncthreads(); __syncthreads();
         if constexpr (S::R2 > 1) { __syncthreads(); __syncthreads(); }

@@ -13,10 +13,29 @@
 // contiguous in memory) or pencils (pencils are adjacent in memory) when
 // moving data to and from the tile, so global accesses stay coalesced.
 #pragma once
+#include <type_traits>
+#include <utility>
+
 #include "fft_engine.cuh"
 #include "geometry.cuh"
 
 namespace dd {
+
+// An Op whose pencils follow the 2/3 rule along the transform axis says so
+// with kept() (its largest kept |mode index| there): an inverse Op's load then
+// returns zero in the removed band and a forward Op's store never reads it,
+// and the transform prunes that band when kept() == kept23(L).
+template <class Op, class = void> struct HasKept : std::false_type {};
+template <class Op>
+struct HasKept<Op, std::void_t<decltype(std::declval<const Op&>().kept())>> : std::true_type {};
+
+template <typename T, class S, bool INV, class Op>
+__device__ __forceinline__ void pass_fft(const Op& op, C<T>* tile, const C<T>* tw) {
+    if constexpr (HasKept<Op>::value) {
+        if (op.kept() == kept23(S::L)) { pencil_fft_s<T, S, INV, true>(tile, tw); return; }
+    }
+    pencil_fft_s<T, S, INV, false>(tile, tw);
+}
 
 template <typename T, int L, bool INV, bool LD_E, bool ST_E, class Op>
 __global__ void __launch_bounds__(FFTCfg<L>::NT) k_pass(const Op op, int nfield) {
@@ -36,7 +55,7 @@ __global__ void __launch_bounds__(FFTCfg<L>::NT) k_pass(const Op op, int nfield)
         tile[e * PS + p] = (f < npen) ? op.load(fld, s, e, f) : zero<T>();
     }
     __syncthreads();
-    pencil_fft<T, L, INV>(tile, tw);
+    pass_fft<T, DefSched<L>, INV>(op, tile, tw);
     const int nst = op.nstore();
     for (int idx = threadIdx.x; idx < nst * P; idx += NT) {
         const int e = ST_E ? idx % nst : idx / P;
@@ -87,7 +106,7 @@ __global__ void __launch_bounds__(S::NT) k_pass_sched(const Op op, int nfield) {
         tile[e * PS + p] = (f < npen) ? op.load(fld, s, e, f) : zero<T>();
     }
     __syncthreads();
-    pencil_fft_s<T, S, INV>(tile, tw);
+    pass_fft<T, S, INV>(op, tile, tw);
     const int nst = op.nstore();
     for (int idx = threadIdx.x; idx < nst * P; idx += NT) {
         const int e = ST_E ? idx % nst : idx / P;
@@ -163,6 +182,7 @@ struct OpZInv3 {
     static constexpr int lmin = 8, lmax = 512;
     using KV = typename Vec2<KT>::type;
     Geo3 g; CPtrs in; Ptrs out; const V* tw;
+    __device__ int kept() const { return g.Mz; }
     __device__ int npencil() const { return g.Kx; }
     __device__ int nstore() const { return g.Nz; }
     __device__ C<T> load(int fld, int kyc, int e, int kx) const {
@@ -183,6 +203,7 @@ struct OpYInv3 {
     static constexpr const char* name = "y_inv";
     static constexpr int lmin = 8, lmax = 512;
     Geo3 g; CPtrs in; Ptrs out; const V* tw;
+    __device__ int kept() const { return g.My; }
     __device__ int npencil() const { return g.Kx; }
     __device__ int nstore() const { return g.Ny; }
     __device__ C<T> load(int fld, int z, int e, int kx) const {
@@ -226,6 +247,7 @@ struct OpXc2r3 {
     static constexpr const char* name = "x_c2r";
     static constexpr int lmin = 8, lmax = 512;
     int nrows, Nx, Kx; CPtrs in; Ptrs out; const V* tw;
+    __device__ int kept() const { return Kx - 1; }
     __device__ int npencil() const { return (nrows + 1) / 2; }
     __device__ int nstore() const { return Nx; }
     __device__ C<T> load(int fld, int, int e, int f) const {
@@ -251,6 +273,7 @@ struct OpXr2c3 {
     static constexpr const char* name = "x_r2c";
     static constexpr int lmin = 8, lmax = 512;
     int nrows, Nx, Kx; T s; CPtrs in; Ptrs out; const V* tw;
+    __device__ int kept() const { return Kx - 1; }
     __device__ int npencil() const { return (nrows + 1) / 2; }
     __device__ int nstore() const { return Kx; }
     __device__ C<T> load(int fld, int, int e, int f) const {
@@ -275,6 +298,7 @@ struct OpYFwd3 {
     static constexpr const char* name = "y_fwd";
     static constexpr int lmin = 8, lmax = 512;
     Geo3 g; CPtrs in; Ptrs out; const V* tw;
+    __device__ int kept() const { return g.My; }
     __device__ int npencil() const { return g.Kx; }
     __device__ int nstore() const { return g.Ny; }
     __device__ C<T> load(int fld, int z, int e, int kx) const {
@@ -296,6 +320,7 @@ struct OpZFwd3 {
     static constexpr int lmin = 8, lmax = 512;
     using KV = typename Vec2<KT>::type;
     Geo3 g; CPtrs in; Ptrs out; const V* tw;
+    __device__ int kept() const { return g.Mz; }
     __device__ int npencil() const { return g.Kx; }
     __device__ int nstore() const { return g.Nz; }
     __device__ C<T> load(int fld, int kyc, int e, int kx) const {
@@ -319,6 +344,7 @@ struct OpYInv2 {
     static constexpr int lmin = 8, lmax = 512;
     using KV = typename Vec2<KT>::type;
     Geo2 g; CPtrs in; Ptrs out; const V* tw;
+    __device__ int kept() const { return g.My; }
     __device__ int npencil() const { return g.Kx; }
     __device__ int nstore() const { return g.Ny; }
     __device__ C<T> load(int fld, int, int e, int kx) const {
@@ -339,6 +365,7 @@ struct OpYFwd2 {
     static constexpr int lmin = 8, lmax = 512;
     using KV = typename Vec2<KT>::type;
     Geo2 g; CPtrs in; Ptrs out; const V* tw;
+    __device__ int kept() const { return g.My; }
     __device__ int npencil() const { return g.Kx; }
     __device__ int nstore() const { return g.Ny; }
     __device__ C<T> load(int fld, int, int e, int kx) const {

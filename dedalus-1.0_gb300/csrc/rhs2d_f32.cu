@@ -1,6 +1,6 @@
-// 2D fused transform passes, float arithmetic.
+// 2D fused transform passes, float arithmetic: hydro forms.
 #include "rhs2d_impl.cuh"
 
 namespace dd {
-DD_RHS2D_INSTANTIATE(, float)
+DD_RHS2D_INSTANTIATE_A(, float)
 }  // namespace dd

@@ -50,6 +50,7 @@ struct OpYInvPhys2 {
     static constexpr int lmin = 32, lmax = 512;
     Geo2 g; CPtrs st; int64_t st_rs; Ptrs out; int64_t w_rs; const V* tw;
     const double* kx; const double* ky;
+    __device__ int kept() const { return g.My; }
     __device__ int npencil() const { return g.Kx; }
     __device__ int nstore() const { return g.Ny; }
     __device__ double2 get(int c, int run, int ix, int e) const {
@@ -122,6 +123,7 @@ struct OpYFwdCompact2 {
     static constexpr const char* name = "y_fwd_compact2d";
     static constexpr int lmin = 32, lmax = 512;
     Geo2 g; CPtrs in; int64_t w_rs; Ptrs out; int64_t nc_rs; const V* tw;
+    __device__ int kept() const { return g.My; }
     __device__ int npencil() const { return g.Kx; }
     __device__ int nstore() const { return g.Ny; }
     __device__ C<T> load(int fld, int run, int e, int ix) const {
@@ -198,22 +200,16 @@ int nonlinear2(const dd_plan* pl, const Work2& w, const void* const* st, int64_t
     return DD_OK;
 }
 
-#define DD_RHS2D_INSTANTIATE(EXT, T)                                                                     \
-    EXT template int nonlinear2<T, false, PHYS_HYDRO>(const dd_plan*, const Work2&, const void* const*, int64_t, \
-                                                      cudaStream_t);                                         \
-    EXT template int nonlinear2<T, true, PHYS_HYDRO>(const dd_plan*, const Work2&, const void* const*, int64_t,  \
-                                                     cudaStream_t);                                          \
-    EXT template int nonlinear2<T, false, PHYS_BOUSS>(const dd_plan*, const Work2&, const void* const*, int64_t, \
-                                                      cudaStream_t);                                         \
-    EXT template int nonlinear2<T, true, PHYS_BOUSS>(const dd_plan*, const Work2&, const void* const*, int64_t,  \
-                                                     cudaStream_t);                                          \
-    EXT template int nonlinear2<T, false, PHYS_HYDRO_DIV>(const dd_plan*, const Work2&, const void* const*,     \
-                                                          int64_t, cudaStream_t);                            \
-    EXT template int nonlinear2<T, true, PHYS_HYDRO_DIV>(const dd_plan*, const Work2&, const void* const*,      \
-                                                         int64_t, cudaStream_t);                             \
-    EXT template int nonlinear2<T, false, PHYS_BOUSS_DIV>(const dd_plan*, const Work2&, const void* const*,     \
-                                                          int64_t, cudaStream_t);                            \
-    EXT template int nonlinear2<T, true, PHYS_BOUSS_DIV>(const dd_plan*, const Work2&, const void* const*,      \
-                                                         int64_t, cudaStream_t);
+#define DD_RHS2D_INSTANTIATE_PH(EXT, T, PH)                                                            \
+    EXT template int nonlinear2<T, false, PH>(const dd_plan*, const Work2&, const void* const*, int64_t,    \
+                                              cudaStream_t);                                            \
+    EXT template int nonlinear2<T, true, PH>(const dd_plan*, const Work2&, const void* const*, int64_t,     \
+                                             cudaStream_t);
+// hydro forms and Boussinesq forms, each compiled in its own translation unit
+#define DD_RHS2D_INSTANTIATE_A(EXT, T) DD_RHS2D_INSTANTIATE_PH(EXT, T, PHYS_HYDRO) \
+    DD_RHS2D_INSTANTIATE_PH(EXT, T, PHYS_HYDRO_DIV)
+#define DD_RHS2D_INSTANTIATE_B(EXT, T) DD_RHS2D_INSTANTIATE_PH(EXT, T, PHYS_BOUSS) \
+    DD_RHS2D_INSTANTIATE_PH(EXT, T, PHYS_BOUSS_DIV)
+#define DD_RHS2D_INSTANTIATE(EXT, T) DD_RHS2D_INSTANTIATE_A(EXT, T) DD_RHS2D_INSTANTIATE_B(EXT, T)
 
 }  // namespace dd

@@ -1,6 +1,6 @@
-// 3D fused transform passes, float arithmetic.
+// 3D fused transform passes, float arithmetic: hydro forms.
 #include "rhs3d_impl.cuh"
 
 namespace dd {
-DD_RHS3D_INSTANTIATE(, float)
+DD_RHS3D_INSTANTIATE_A(, float)
 }  // namespace dd

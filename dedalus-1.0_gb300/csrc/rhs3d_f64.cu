@@ -1,6 +1,6 @@
-// 3D fused transform passes, double arithmetic.
+// 3D fused transform passes, double arithmetic: hydro forms.
 #include "rhs3d_impl.cuh"
 
 namespace dd {
-DD_RHS3D_INSTANTIATE(, double)
+DD_RHS3D_INSTANTIATE_A(, double)
 }  // namespace dd

@@ -57,6 +57,7 @@ struct OpZInvCurl3 {
     static constexpr int lmin = 16, lmax = 512;
     Geo3 g; CPtrs u; Ptrs out; const V* tw;
     const double* kx; const double* ky; const double* kz;
+    __device__ int kept() const { return g.Mz; }
     __device__ int npencil() const { return g.Kx; }
     __device__ int nstore() const { return g.Nz; }
     __device__ double2 get(int c, int kyc, int ky_i, int e, int ix) const {
@@ -173,6 +174,7 @@ struct OpZFwdCompact3 {
     static constexpr const char* name = "z_fwd_compact";
     static constexpr int lmin = 16, lmax = 512;
     Geo3 g; CPtrs in; Ptrs out; const V* tw;
+    __device__ int kept() const { return g.Mz; }
     __device__ int npencil() const { return g.Kx; }
     __device__ int nstore() const { return g.Nz; }
     __device__ C<T> load(int fld, int kyc, int e, int kx) const {
@@ -261,7 +263,11 @@ int nonlinear3(const dd_plan* pl, const void* const* u, double inv_fpr, const Wo
                                               cudaStream_t);                                            \
     EXT template int nonlinear3<T, true, PH>(const dd_plan*, const void* const*, double, const Work3&,      \
                                              cudaStream_t);
-#define DD_RHS3D_INSTANTIATE(EXT, T) DD_RHS3D_INSTANTIATE_PH(EXT, T, P3_HYDRO) DD_RHS3D_INSTANTIATE_PH(EXT, T, P3_MHD) \
-    DD_RHS3D_INSTANTIATE_PH(EXT, T, P3_HYDRO_DIV) DD_RHS3D_INSTANTIATE_PH(EXT, T, P3_MHD_DIV)
+// hydro forms and MHD forms, each compiled in its own translation unit
+#define DD_RHS3D_INSTANTIATE_A(EXT, T) DD_RHS3D_INSTANTIATE_PH(EXT, T, P3_HYDRO) \
+    DD_RHS3D_INSTANTIATE_PH(EXT, T, P3_HYDRO_DIV)
+#define DD_RHS3D_INSTANTIATE_B(EXT, T) DD_RHS3D_INSTANTIATE_PH(EXT, T, P3_MHD) \
+    DD_RHS3D_INSTANTIATE_PH(EXT, T, P3_MHD_DIV)
+#define DD_RHS3D_INSTANTIATE(EXT, T) DD_RHS3D_INSTANTIATE_A(EXT, T) DD_RHS3D_INSTANTIATE_B(EXT, T)
 
 }  // namespace dd

@@ -126,7 +126,11 @@ k_x_prod(int nrows, int Kx, CPtrs win, Ptrs wout, int64_t in_rs, int64_t out_rs,
         tile[e * PSI + pj] = z;
     }
     __syncthreads();
-    pencil_fft_s<T, SI, true>(tile, tw);
+    // kept kx <= Kx - 1: under the 2/3 rule the packed pencils are zero in the
+    // removed band and the unpacking never reads it
+    const bool prune = Kx - 1 == kept23(L);
+    if (prune) pencil_fft_s<T, SI, true, true>(tile, tw);
+    else pencil_fft_s<T, SI, true>(tile, tw);
     T outv[NPT][NO];
 #pragma unroll
     for (int i = 0; i < NPT; i++) {
@@ -161,7 +165,8 @@ k_x_prod(int nrows, int Kx, CPtrs win, Ptrs wout, int64_t in_rs, int64_t out_rs,
         for (int e = threadIdx.x; e < L; e += NT) tile[e * PSF + (NO * Q) / 2].y = T(0);
     }
     __syncthreads();
-    pencil_fft_s<T, SF, false>(tile, tw, threadIdx.x < SF::NT);
+    if (prune) pencil_fft_s<T, SF, false, true>(tile, tw, threadIdx.x < SF::NT);
+    else pencil_fft_s<T, SF, false>(tile, tw, threadIdx.x < SF::NT);
     for (int idx = threadIdx.x; idx < Kx * Q * NO; idx += NT) {
         const int k = idx % Kx, t = idx / Kx;
         const int r = t / NO, g = t % NO;
