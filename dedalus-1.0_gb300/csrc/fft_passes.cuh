@@ -31,7 +31,7 @@ struct HasKept<Op, std::void_t<decltype(std::declval<const Op&>().kept())>> : st
 
 template <typename T, class S, bool INV, class Op>
 __device__ __forceinline__ void pass_fft(const Op& op, C<T>* tile, const C<T>* tw) {
-    if constexpr (HasKept<Op>::value) {
+    if constexpr (HasKept<Op>::value && IsLF<T>::value) {   // one copy of the transform for double-float
         if (op.kept() == kept23(S::L)) { pencil_fft_s<T, S, INV, true>(tile, tw); return; }
     }
     pencil_fft_s<T, S, INV, false>(tile, tw);

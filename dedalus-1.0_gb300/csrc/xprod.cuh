@@ -76,21 +76,36 @@ template <> struct ProdCfg<512, 12, 6> {
     static constexpr int Q = 2, NT = 384;
 };
 
-template <int L, int NI, int NO>
+// The schedule a precision runs: ProdCfg, except where 8-byte FP32 complex
+// entries need other tiles.  A half-warp moves 16 x 8 B through the 32 banks,
+// so a pencil-major Stockham access (16 consecutive threads = consecutive
+// pencils of one row) is conflict-free only when a row holds a multiple of 16
+// pencils; FP64 entries (16 B, a quarter-warp per wavefront) need a multiple
+// of 8, which the FP64 schedules have.
+template <typename T, int L, int NI, int NO>
+struct ProdCfgT : ProdCfg<L, NI, NO> {};
+// FP32 hydro in divergence form (3 -> 5): 6 rows per block, 9 inverse and 15
+// forward pencils, each side on a 16-pencil tile (16 threads per pencil).
+template <> struct ProdCfgT<float, 256, 3, 5> {
+    using SI = Sched<256, 16, 256, 16, 16, 1>;  using SF = Sched<256, 16, 256, 16, 16, 1>;
+    static constexpr int Q = 6, NT = 256;
+};
+
+template <typename T, int L, int NI, int NO>
 constexpr size_t prod_smem(size_t csize) {
-    using CC = ProdCfg<L, NI, NO>;
+    using CC = ProdCfgT<T, L, NI, NO>;
     const size_t a = (size_t)L * CC::SI::PS, b = (size_t)L * CC::SF::PS;
     return csize * ((a > b ? a : b) + L);
 }
 
 template <typename T, int L, class Op>
-__global__ void __launch_bounds__(ProdCfg<L, Op::NI, Op::NO>::NT, std::is_same<T, df64>::value ? 5 : 1)
+__global__ void __launch_bounds__(ProdCfgT<T, L, Op::NI, Op::NO>::NT, std::is_same<T, df64>::value ? 5 : 1)
 k_x_prod(int nrows, int Kx, CPtrs win, Ptrs wout, int64_t in_rs, int64_t out_rs,
          const typename Vec2<T>::type* gtw, T scale, const Op op) {
     using V = typename Vec2<T>::type;
     constexpr int NI = Op::NI, NO = Op::NO;
     static_assert(NI <= DD_MAXF && NO <= DD_MAXF, "too many fields for Ptrs");
-    using CC = ProdCfg<L, NI, NO>;
+    using CC = ProdCfgT<T, L, NI, NO>;
     using SI = typename CC::SI;
     using SF = typename CC::SF;
     extern __shared__ __align__(16) unsigned char dd_smem[];
@@ -128,9 +143,14 @@ k_x_prod(int nrows, int Kx, CPtrs win, Ptrs wout, int64_t in_rs, int64_t out_rs,
     __syncthreads();
     // kept kx <= Kx - 1: under the 2/3 rule the packed pencils are zero in the
     // removed band and the unpacking never reads it
-    const bool prune = Kx - 1 == kept23(L);
-    if (prune) pencil_fft_s<T, SI, true, true>(tile, tw);
-    else pencil_fft_s<T, SI, true>(tile, tw);
+    // (double-float has no pruned butterflies: one copy of its transform)
+    const bool prune = IsLF<T>::value && Kx - 1 == kept23(L);
+    if constexpr (IsLF<T>::value) {
+        if (prune) pencil_fft_s<T, SI, true, true>(tile, tw);
+        else pencil_fft_s<T, SI, true>(tile, tw);
+    } else {
+        pencil_fft_s<T, SI, true>(tile, tw);
+    }
     T outv[NPT][NO];
 #pragma unroll
     for (int i = 0; i < NPT; i++) {
@@ -165,8 +185,12 @@ k_x_prod(int nrows, int Kx, CPtrs win, Ptrs wout, int64_t in_rs, int64_t out_rs,
         for (int e = threadIdx.x; e < L; e += NT) tile[e * PSF + (NO * Q) / 2].y = T(0);
     }
     __syncthreads();
-    if (prune) pencil_fft_s<T, SF, false, true>(tile, tw, threadIdx.x < SF::NT);
-    else pencil_fft_s<T, SF, false>(tile, tw, threadIdx.x < SF::NT);
+    if constexpr (IsLF<T>::value) {
+        if (prune) pencil_fft_s<T, SF, false, true>(tile, tw, threadIdx.x < SF::NT);
+        else pencil_fft_s<T, SF, false>(tile, tw, threadIdx.x < SF::NT);
+    } else {
+        pencil_fft_s<T, SF, false>(tile, tw, threadIdx.x < SF::NT);
+    }
     for (int idx = threadIdx.x; idx < Kx * Q * NO; idx += NT) {
         const int k = idx % Kx, t = idx / Kx;
         const int r = t / NO, g = t % NO;
@@ -180,8 +204,8 @@ k_x_prod(int nrows, int Kx, CPtrs win, Ptrs wout, int64_t in_rs, int64_t out_rs,
 template <typename T, int L, class Op>
 int launch_x_prod(const char* name, int nrows, int Kx, const CPtrs& win, const Ptrs& wout, int nrun, int64_t in_rs,
                   int64_t out_rs, const typename Vec2<T>::type* tw, T scale, const Op& op, cudaStream_t st) {
-    using CC = ProdCfg<L, Op::NI, Op::NO>;
-    const size_t smem = prod_smem<L, Op::NI, Op::NO>(sizeof(C<T>));
+    using CC = ProdCfgT<T, L, Op::NI, Op::NO>;
+    const size_t smem = prod_smem<T, L, Op::NI, Op::NO>(sizeof(C<T>));
     static std::atomic<unsigned long long> configured{0};
     DD_TRY(ensure_smem((const void*)k_x_prod<T, L, Op>, smem, configured));
     static const std::string label = std::string(name) + "_" + std::to_string(L) + PrecName<T>::s;

@@ -125,8 +125,11 @@ def test_non_dealiased_state_decays_like_reference(dd, cuda):
 
 
 @pytest.mark.gpu
-def test_fp32_path_error(dd, cuda):
-    shape = (64, 64, 64)
+@pytest.mark.parametrize("shape", [(64, 64, 64), (16, 32, 256)])
+def test_fp32_path_error(dd, cuda, shape):
+    """FP32 transforms (divergence form for this solenoidal state) against the
+    FP64 oracle; (16, 32, 256) runs the FP32 256-point x-pass schedule of the
+    headline's FP32 arm."""
     u0 = dd.init_cond.turbulence_3d(shape, seed=6)
     ro, do = oracle_hydro(shape, 5e-3, u0)
     OT.RK4(ro).do_advance(do, 2e-3)
