@@ -13,6 +13,7 @@ configuration of the project):
 
     hydro3d-256-{fp64,df64,fp32}  3D hydro 256^3 RK4 with FP64 / double-float / FP32 transforms
     hydro3d-128-{fp64,df64}       the same at 128^3 (small cases for profiling)
+    hydro3d-192-fp32              the same at 192^3, FP32 (profiling the x pass's store alignment)
     mhd3d-256-{fp32,fp64}         3D MHD 256^3 RK4, nu = eta = 5e-3, dt = 1e-3
     hydro2d-128                   2D hydro 128^2 RK2mid, nu = 1e-3, dt = 1e-3
     bouss2d-ensemble-512[-fp32]   512 2D Boussinesq runs, sizes uniform in {64,128,256,512}^2,
@@ -53,6 +54,9 @@ WORKLOADS = {
     # 256-point x rows on a grid small enough for a full ncu capture, larger than L2
     "hydro3d-128x128x256-fp64": dict(kind="hydro3d", shape=(128, 128, 256), nu=5e-3, dt=2e-3, precision="fp64"),
     "hydro3d-128-df64": dict(kind="hydro3d", shape=(128,) * 3, nu=5e-3, dt=2e-3, precision="df64"),
+    # 192-point rows (64 kept kx: 512-byte FP32 rows, whole 32-byte sectors) beside the 256-point
+    # ones (86 kept kx: 688-byte rows): the sector alignment of the x-pass stores
+    "hydro3d-192-fp32": dict(kind="hydro3d", shape=(192,) * 3, nu=5e-3, dt=2e-3, precision="fp32"),
     "mhd3d-256-fp32": dict(kind="mhd3d", shape=(256,) * 3, nu=5e-3, dt=1e-3, precision="fp32"),
     "mhd3d-256-fp64": dict(kind="mhd3d", shape=(256,) * 3, nu=5e-3, dt=1e-3, precision="fp64"),
     "hydro2d-128": dict(kind="hydro2d", shape=(128, 128), nu=1e-3, dt=1e-3, precision="fp64"),

@@ -76,20 +76,14 @@ template <> struct ProdCfg<512, 12, 6> {
     static constexpr int Q = 2, NT = 384;
 };
 
-// The schedule a precision runs: ProdCfg, except where 8-byte FP32 complex
-// entries need other tiles.  A half-warp moves 16 x 8 B through the 32 banks,
-// so a pencil-major Stockham access (16 consecutive threads = consecutive
-// pencils of one row) is conflict-free only when a row holds a multiple of 16
-// pencils; FP64 entries (16 B, a quarter-warp per wavefront) need a multiple
-// of 8, which the FP64 schedules have.
+// The schedule a precision runs (ProdCfg for all three; the indirection is
+// where a precision would get its own tiles).  FP32 tiles of 16 pencils per
+// row (conflict-free 8-byte shared-memory access) were measured on the 256-point
+// hydro pass in divergence form and lost: bank conflicts 42% -> 4% of the
+// wavefronts, but 314 -> 330 us per launch, the idle pencil slots of a 16-wide
+// tile for 9 inverse pencils costing more than the conflicts.
 template <typename T, int L, int NI, int NO>
 struct ProdCfgT : ProdCfg<L, NI, NO> {};
-// FP32 hydro in divergence form (3 -> 5): 6 rows per block, 9 inverse and 15
-// forward pencils, each side on a 16-pencil tile (16 threads per pencil).
-template <> struct ProdCfgT<float, 256, 3, 5> {
-    using SI = Sched<256, 16, 256, 16, 16, 1>;  using SF = Sched<256, 16, 256, 16, 16, 1>;
-    static constexpr int Q = 6, NT = 256;
-};
 
 template <typename T, int L, int NI, int NO>
 constexpr size_t prod_smem(size_t csize) {
