@@ -284,6 +284,10 @@ class Hydro3Runner:
             return no * (w2 + w1)
         if label.startswith("z_fwd_compact"):
             return no * (w1 + kc)
+        if label.startswith("rk4_stage3_lo"):
+            # FP32 step: complex64 products (no), increment (read + write) and stage state,
+            # complex128 state read (a middle stage; the last writes the state instead)
+            return no * kc // 2 + 3 * g * (3 * kc // 2 + kc)
         if label.startswith("rk4_stage3"):
             return 3 * g * kc * 5 + (2 * kc if self.divergence_form() else 0)
         if label.startswith("div_sums3"):

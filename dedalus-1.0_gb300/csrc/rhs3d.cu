@@ -8,6 +8,8 @@ namespace dd {
 
 DD_RHS3D_INSTANTIATE(extern, double)
 DD_RHS3D_INSTANTIATE(extern, float)
+DD_RHS3D_INSTANTIATE_LO(extern, P3_HYDRO_DIV)
+DD_RHS3D_INSTANTIATE_LO(extern, P3_MHD_DIV)
 DD_RHS3D_INSTANTIATE_PH(extern, df64, P3_HYDRO)
 
 // ------------------------------------------------------------------ pass 6
@@ -203,6 +205,83 @@ __global__ void k_rk4_stage3(RK4Args a) {
     }
 }
 
+// The same stage for the FP32 step in divergence form, with low-storage
+// intermediates: the compact products, the stage states and the increment are
+// complex64, and N = -i k_j T_ij, its projection (and, for MHD, the curl of
+// u x B) are formed in FP32, the precision the FP32 transforms give them; the
+// ETD update of the complex128 state -- phi functions, y phi0 + h phi1 N --
+// stays FP64.  Same stage definitions as k_rk4_stage3.
+__device__ __forceinline__ float2 fderiv(float2 a, float k) { return make_float2(-(a.y * k), a.x * k); }
+
+template <int PH>
+__global__ void k_rk4_stage3_lo(RK4Args a) {
+    static_assert(PH == P3_HYDRO_DIV || PH == P3_MHD_DIV, "low-storage stages are for the divergence forms");
+    const Geo3& g = a.pa.g;
+    constexpr int NF = Phys3<PH>::NF, NG = Phys3<PH>::NG;
+    const int n = g.Ky * g.Kz * g.Kx;      // < 2^31 for every supported grid
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int ix = i % g.Kx, r = i / g.Kx;
+        const int kzc = r % g.Kz, kyc = r / g.Kz;
+        const int ky_i = compact_to_full(kyc, g.Ny, g.Ky), kz_i = compact_to_full(kzc, g.Nz, g.Kz);
+        const double kxd = a.pa.kx[ix], kyd = a.pa.ky[ky_i], kzd = a.pa.kz[kz_i];
+        const double k2 = k2_of(a.pa, ix, ky_i, kz_i);
+        int q;
+        const float s = (float)inv_k2_of(a.pa, k2, q);
+        const float kx = (float)kxd, ky = (float)kyd, kz = (float)kzd;
+        const float2* P[8];
+#pragma unroll
+        for (int c = 0; c < Phys3<PH>::NO; c++) P[c] = (const float2*)a.nc.p[c];
+        // N = -i k_j T_ij from xx - zz, yy - zz, xy, xz, yz; -i s = (s.y, -s.x)
+        const float2 A = P[0][i], B = P[1][i], Cc = P[2][i], D = P[3][i], E = P[4][i];
+        const float sxr = fmaf(kz, D.x, fmaf(ky, Cc.x, kx * A.x)), sxi = fmaf(kz, D.y, fmaf(ky, Cc.y, kx * A.y));
+        const float syr = fmaf(kz, E.x, fmaf(ky, B.x, kx * Cc.x)), syi = fmaf(kz, E.y, fmaf(ky, B.y, kx * Cc.y));
+        const float szr = fmaf(ky, E.x, kx * D.x), szi = fmaf(ky, E.y, kx * D.y);
+        float2 k[6];
+        k[0] = make_float2(sxi, -sxr); k[1] = make_float2(syi, -syr); k[2] = make_float2(szi, -szr);
+        // projection: N -= k (k . N) / k^2
+        const float cr = fmaf(kz, k[2].x, fmaf(ky, k[1].x, kx * k[0].x)) * s;
+        const float ci = fmaf(kz, k[2].y, fmaf(ky, k[1].y, kx * k[0].y)) * s;
+        k[0] = make_float2(fmaf(-kx, cr, k[0].x), fmaf(-kx, ci, k[0].y));
+        k[1] = make_float2(fmaf(-ky, cr, k[1].x), fmaf(-ky, ci, k[1].y));
+        k[2] = make_float2(fmaf(-kz, cr, k[2].x), fmaf(-kz, ci, k[2].y));
+        if constexpr (p3_mhd(PH)) {   // curl (u x B)
+            const float2 vx = P[5][i], vy = P[6][i], vz = P[7][i];
+            const float2 a0 = fderiv(vz, ky), b0 = fderiv(vy, kz), a1 = fderiv(vx, kz), b1 = fderiv(vz, kx);
+            const float2 a2 = fderiv(vy, kx), b2 = fderiv(vx, ky);
+            k[3] = make_float2(a0.x - b0.x, a0.y - b0.y);
+            k[4] = make_float2(a1.x - b1.x, a1.y - b1.y);
+            k[5] = make_float2(a2.x - b2.x, a2.y - b2.y);
+        }
+        double f0[NG], f1h[NG];
+#pragma unroll
+        for (int grp = 0; grp < NG; grp++) {
+            double Z, f1;
+            phis_for(a, grp, q, k2, Z, f0[grp], f1);
+            f1h[grp] = f1 * a.h;
+        }
+        const int64_t o = ((int64_t)ky_i * g.Nz + kz_i) * g.Nh + ix;
+        const float w = (float)a.w;
+#pragma unroll
+        for (int c = 0; c < NF; c++) {
+            const int grp = c / 3;
+            float2 t;
+            if (a.stage == 1) t = make_float2(k[c].x * w, k[c].y * w);
+            else {
+                t = ((const float2*)a.tot.p[c])[i];
+                t = make_float2(fmaf(k[c].x, w, t.x), fmaf(k[c].y, w, t.y));
+            }
+            const double2 y0 = ((const double2*)a.y.p[c])[o];
+            if (a.stage < 4) {
+                ((float2*)a.tot.p[c])[i] = t;
+                const double2 ys = etd1_fma(y0, make_double2((double)k[c].x, (double)k[c].y), f0[grp], f1h[grp]);
+                ((float2*)a.ys.p[c])[i] = make_float2((float)ys.x, (float)ys.y);
+            } else {
+                ((double2*)a.y.p[c])[o] = etd1_fma(y0, make_double2((double)t.x, (double)t.y), f0[grp], f1h[grp]);
+            }
+        }
+    }
+}
+
 // Non-kept modes of the state see no nonlinear forcing: y <- etd1(y, 0, dt).
 __global__ void k_decay_nonkept3(RK4Args a, int ncomp) {
     const Geo3& g = a.pa.g;
@@ -393,7 +472,22 @@ static int rk4_3(const dd_plan* p, const double* params, void* const* u, const d
     const double hs[4] = {dt / 2., dt / 2., dt, dt};
     const double ws[4] = {1. / 6., 1. / 3., 1. / 3., 1. / 6.};
     const unsigned nb = ew_grid((int64_t)w.kc);
+    // FP32 transforms in divergence form without a closure: low-storage stages
+    constexpr bool lo_ok = PH == P3_HYDRO_DIV || PH == P3_MHD_DIV;
+    const bool lo = lo_ok && prec == DD_FP32 && les == nullptr;
     for (int s = 1; s <= 4; s++) {
+        if constexpr (lo_ok) {
+            if (lo) {
+                if (s == 1) DD_TRY((nonlinear3<float, false, PH, float>(p, (const void* const*)u, inv_fpr, w, st)));
+                else DD_TRY((nonlinear3<float, true, PH, float>(p, ysc, inv_fpr, w, st)));
+                a.stage = s; a.h = hs[s - 1]; a.w = ws[s - 1];
+                for (int grp = 0; grp < P::NG; grp++)
+                    a.tab[grp] = intk ? (const double4*)(s <= 2 ? tab_half[grp] : tab_full[grp]) : nullptr;
+                DD_KT("rk4_stage3_lo", st, k_rk4_stage3_lo<PH><<<nb, 256, 0, st>>>(a));
+                DD_LAUNCH_CHECK();
+                continue;
+            }
+        }
         DD_TRY(nonlinear3_any<PH>(p, prec, s > 1, s == 1 ? (const void* const*)u : ysc, inv_fpr, w, st));
         if (les) {
             void* ncp[3] = {(void*)a.nc.p[0], (void*)a.nc.p[1], (void*)a.nc.p[2]};

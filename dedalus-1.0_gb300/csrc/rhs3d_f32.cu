@@ -3,4 +3,5 @@
 
 namespace dd {
 DD_RHS3D_INSTANTIATE_A(, float)
+DD_RHS3D_INSTANTIATE_LO(, P3_HYDRO_DIV)
 }  // namespace dd

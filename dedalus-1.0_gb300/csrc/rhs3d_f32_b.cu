@@ -3,4 +3,5 @@
 
 namespace dd {
 DD_RHS3D_INSTANTIATE_B(, float)
+DD_RHS3D_INSTANTIATE_LO(, P3_MHD_DIV)
 }  // namespace dd

@@ -50,7 +50,9 @@ __device__ __forceinline__ double2 ideriv(double2 a, double k) { return make_dou
 // physics.py:394-396: (d_y X_z - d_z X_y, d_z X_x - d_x X_z, d_x X_y - d_y X_x)).
 // The state is read from the full reference layout [ky][kz][kx] or from the
 // compact kept layout [kyc][kzc][kx] used for RK stage states.
-template <typename T, bool COMPACT, int NG, bool CURL = true>
+// ST: element type of a compact state (double; float for the FP32 step's
+// stage states).  The full-layout state is always complex128.
+template <typename T, bool COMPACT, int NG, bool CURL = true, typename ST = double>
 struct OpZInvCurl3 {
     using V = typename Vec2<T>::type;
     static constexpr const char* name = NG == 1 ? "z_inv_curl" : (CURL ? "z_inv_curl_mhd" : "z_inv_mhd");
@@ -61,9 +63,12 @@ struct OpZInvCurl3 {
     __device__ int npencil() const { return g.Kx; }
     __device__ int nstore() const { return g.Nz; }
     __device__ double2 get(int c, int kyc, int ky_i, int e, int ix) const {
-        const double2* U = (const double2*)u.p[c];
-        if (COMPACT) return U[((int64_t)kyc * g.Kz + full_to_compact(e, g.Nz, g.Kz)) * g.Kx + ix];
-        return U[((int64_t)ky_i * g.Nz + e) * g.Nh + ix];
+        if (COMPACT) {
+            using SV = typename Vec2<ST>::type;
+            const SV v = ((const SV*)u.p[c])[((int64_t)kyc * g.Kz + full_to_compact(e, g.Nz, g.Kz)) * g.Kx + ix];
+            return make_double2((double)v.x, (double)v.y);
+        }
+        return ((const double2*)u.p[c])[((int64_t)ky_i * g.Nz + e) * g.Nh + ix];
     }
     __device__ C<T> load(int fld, int kyc, int e, int ix) const {
         if (!kept_full(e, g.Nz, g.Mz)) return zero<T>();
@@ -168,9 +173,11 @@ struct ProdMHDDiv3 {
 };
 
 // ------------------------------------------------------------------ pass 5
-template <typename T>
+// ST: element type of the compact products (double; float for the FP32 step).
+template <typename T, typename ST = double>
 struct OpZFwdCompact3 {
     using V = typename Vec2<T>::type;
+    using SV = typename Vec2<ST>::type;
     static constexpr const char* name = "z_fwd_compact";
     static constexpr int lmin = 16, lmax = 512;
     Geo3 g; CPtrs in; Ptrs out; const V* tw;
@@ -183,8 +190,8 @@ struct OpZFwdCompact3 {
     __device__ void store(int fld, int kyc, int e, int kx, const C<T>* col, int PS) const {
         if (!kept_full(e, g.Nz, g.Mz)) return;
         const C<T> c = col[e * PS];
-        ((double2*)out.p[fld])[((int64_t)kyc * g.Kz + full_to_compact(e, g.Nz, g.Kz)) * g.Kx + kx] =
-            make_double2((double)c.x, (double)c.y);
+        SV v; v.x = (ST)c.x; v.y = (ST)c.y;
+        ((SV*)out.p[fld])[((int64_t)kyc * g.Kz + full_to_compact(e, g.Nz, g.Kz)) * g.Kx + kx] = v;
     }
 };
 
@@ -219,7 +226,9 @@ static Work3 make_work(const Geo3& g, void* base) {
                  (char*)base};
 }
 
-template <typename T, bool COMPACT, int PH>
+// ST = float (FP32 transforms only): compact stage states are read and the
+// compact products written as complex64 (the FP32 step's low-storage stages).
+template <typename T, bool COMPACT, int PH, typename ST = double>
 int nonlinear3(const dd_plan* pl, const void* const* u, double inv_fpr, const Work3& w, cudaStream_t st) {
     using P = Phys3<PH>;
     const Geo3& g = pl->g3;
@@ -231,7 +240,7 @@ int nonlinear3(const dd_plan* pl, const void* const* u, double inv_fpr, const Wo
         w1.p[f] = w.W1<T>(f); w1c.p[f] = w1.p[f];
         w2.p[f] = w.W2<T>(f); w2c.p[f] = w2.p[f];
     }
-    OpZInvCurl3<T, COMPACT, P::NG, p3_curl_inputs(PH)> a{g, uin, w1, TwSel<T>::z(pl), pl->kx, pl->ky, pl->kz};
+    OpZInvCurl3<T, COMPACT, P::NG, p3_curl_inputs(PH), ST> a{g, uin, w1, TwSel<T>::z(pl), pl->kx, pl->ky, pl->kz};
     DD_TRY((launch_pass_len<T, true, false, false>(g.Nz, a, g.Kx, g.Ky, P::NINV, st)));
     OpYInv3<T> b{g, w1c, w2, TwSel<T>::y(pl)};
     DD_TRY((launch_pass_len<T, true, false, false>(g.Ny, b, g.Kx, g.Nz, P::NINV, st)));
@@ -251,7 +260,7 @@ int nonlinear3(const dd_plan* pl, const void* const* u, double inv_fpr, const Wo
     }
     OpYFwd3<T> d{g, w2c, w1, TwSel<T>::y(pl)};
     DD_TRY((launch_pass_len<T, false, false, false>(g.Ny, d, g.Kx, g.Nz, P::NO, st)));
-    OpZFwdCompact3<T> e{g, w1c, nc, TwSel<T>::z(pl)};
+    OpZFwdCompact3<T, ST> e{g, w1c, nc, TwSel<T>::z(pl)};
     DD_TRY((launch_pass_len<T, false, false, false>(g.Nz, e, g.Kx, g.Ky, P::NO, st)));
     return DD_OK;
 }
@@ -263,7 +272,13 @@ int nonlinear3(const dd_plan* pl, const void* const* u, double inv_fpr, const Wo
                                               cudaStream_t);                                            \
     EXT template int nonlinear3<T, true, PH>(const dd_plan*, const void* const*, double, const Work3&,      \
                                              cudaStream_t);
-// hydro forms and MHD forms, each compiled in its own translation unit
+#define DD_RHS3D_INSTANTIATE_LO(EXT, PH)                                                                \
+    EXT template int nonlinear3<float, false, PH, float>(const dd_plan*, const void* const*, double,         \
+                                                         const Work3&, cudaStream_t);                        \
+    EXT template int nonlinear3<float, true, PH, float>(const dd_plan*, const void* const*, double,          \
+                                                        const Work3&, cudaStream_t);
+// hydro forms and MHD forms, each compiled in its own translation unit; FP32
+// adds the low-storage stage variants of the divergence forms
 #define DD_RHS3D_INSTANTIATE_A(EXT, T) DD_RHS3D_INSTANTIATE_PH(EXT, T, P3_HYDRO) \
     DD_RHS3D_INSTANTIATE_PH(EXT, T, P3_HYDRO_DIV)
 #define DD_RHS3D_INSTANTIATE_B(EXT, T) DD_RHS3D_INSTANTIATE_PH(EXT, T, P3_MHD) \
