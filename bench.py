@@ -200,6 +200,10 @@ class Hydro3Runner:
     def state(self):
         return [self.data[f][c].kdata for f, c in self.names]
 
+    def touch(self):
+        for f, c in self.names:
+            self.data[f][c].touch()
+
     def divergence_form(self):
         """True when the fused steps ran the divergence form (hydro 3 + 5,
         MHD 6 + 8 transforms per RHS; chosen per step for a solenoidal state)."""
@@ -1030,6 +1034,7 @@ def main():
         for _ in range(ke):
             for d, h in zip(dev_state, host_in):
                 d.copy_(h, non_blocking=True)
+            getattr(run, "touch", lambda: None)()     # the state was written behind the API's back
             api_step()
             for d, h in zip(dev_state, host_out):
                 h.copy_(d, non_blocking=True)

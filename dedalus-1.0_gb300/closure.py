@@ -565,6 +565,7 @@ def evaluate(models, seed=7, dns_n=256, les_n=64, nu=5e-3, dt=2e-3, nsteps=1000,
         ub = sampler.filter_velocity([dd['u'][i].kdata for i in range(3)])
         for i in range(3):
             data['u'][i].kdata.copy_(ub[i])
+            data['u'][i].touch()
         runs[name] = (RHS, data, ti_l, cl)
     ref = les_problem(les_n, nu, None)
     kmax = sampler.les.mx
@@ -706,6 +707,7 @@ def les_trajectory(closure, ref, precision='fp32'):
     RHS, data, ti = les_problem(les_n, nu, closure, precision)
     for i in range(3):
         data['u'][i].kdata.copy_(ref["u0"][i])
+        data['u'][i].touch()
     out = {"steps": [], "err_half": [], "err_full": [], "err_half_shells": [], "diss_err": [], "diss": [],
            "closure_input": []}
     d1 = RHS.create_fields(0.) if closure is not None else None

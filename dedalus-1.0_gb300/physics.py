@@ -257,11 +257,17 @@ class IncompressibleHydro(ReferenceOrderRHS, Physics):
     # terms (dd_rk4_step3d physics 2 for hydro: 3 + 5 transforms per RHS
     # instead of 6 + 3; physics 3 for MHD: 6 + 8 instead of 12 + 6) whenever
     # every vector field of the state is solenoidal to |k.u| <= 1e-12 |k||u|
-    # (checked before every step with dd_divergence_sums), and the curl forms
-    # otherwise; both equal the reference's terms to roundoff on such states.  'rotational' always uses the rotational form, and so does
-    # a step captured into a CUDA graph (the check reads back to the host).
+    # (1e-6 with FP32 transforms; dd_divergence_sums, re-checked whenever the
+    # state changed outside the fused steps), and the curl forms otherwise;
+    # both equal the reference's terms to roundoff on such states.
+    # 'rotational' always uses the rotational form, and so does a step
+    # captured into a CUDA graph (the check reads back to the host).
     nonlinear_form = 'auto'
     DIV_TOL2 = 1e-24
+    # With FP32 transforms the step keeps its increments (and so the state's
+    # divergence) at FP32 accuracy: a relative divergence up to 1e-6, below the
+    # FP32 path's own error, still takes the divergence form.
+    DIV_TOL2_FP32 = 1e-12
 
     def _step_phys3d(self, plan, prec, sp):
         """Physics code of dd_rk4_step3d for this step: the divergence form
@@ -281,8 +287,35 @@ class IncompressibleHydro(ReferenceOrderRHS, Physics):
             _lib.call("dd_divergence_sums", plan.handle, gp, ctypes.c_void_p(buf.data_ptr() + 16 * g),
                       current_stream())
         v = buf.tolist()
-        ok = all(v[2 * g] <= self.DIV_TOL2 * v[2 * g + 1] for g in range(ngroups))
+        tol = self.DIV_TOL2_FP32 if prec == _lib.DD_FP32 else self.DIV_TOL2
+        ok = all(v[2 * g] <= tol * v[2 * g + 1] for g in range(ngroups))
         return self._phys3d + 2 if ok else self._phys3d
+
+    def _state_form3d(self, data, plan, prec, sp):
+        """(physics code, non-kept flag) of a fused 3D step: the divergence
+        form when the state is solenoidal (_step_phys3d), and whether any state
+        component holds energy outside the kept modes (dd_any_nonkept; then the
+        step decays those modes, as the reference's etd1 does).  A fused step
+        keeps a solenoidal, dealiased state so, so the result is reused until a
+        state component is read or written through the public API (its
+        version moves) or replaced; inside a stream capture nothing is read back
+        (curl forms, decay on)."""
+        if torch.cuda.is_current_stream_capturing():
+            return self._step_phys3d(plan, prec, sp), None
+        comps = [data[f][c] for f, c in self._state3d()]
+        key = (tuple((id(c), c._version, c.kdata.data_ptr()) for c in comps), prec, self.nonlinear_form)
+        cached = getattr(self, '_form_cache', None)
+        if cached is not None and cached[0] == key:
+            return cached[1]
+        phys = self._step_phys3d(plan, prec, sp)
+        flag = self._tables.get('nonkept')
+        if flag is None:
+            flag = self._tables['nonkept'] = torch.zeros(1, dtype=torch.int32, device=plan.device)
+        flag.zero_()
+        _lib.call("dd_any_nonkept", plan.handle, len(comps), sp, dptr(flag), current_stream())
+        val = (phys, ctypes.c_int(int(flag.item())))
+        self._form_cache = (key, val)
+        return val
 
     def fused_rk4(self, data, dt):
         """One fused RK4 step on the device (dd_rk4_step3d) for 3D hydro / MHD;
@@ -292,7 +325,7 @@ class IncompressibleHydro(ReferenceOrderRHS, Physics):
         if self._generic():
             return False
         plan, prec, vo, cf, ik2, th, tf, sp, keep = self._rk4_args(data, dt)
-        phys = self._step_phys3d(plan, prec, sp)
+        phys, nonkept = self._state_form3d(data, plan, prec, sp)
         self.last_phys3d = phys
         n = ctypes.c_size_t()
         _lib.call("dd_rhs3d_workspace_size", plan.handle, phys, prec, ctypes.byref(n))
@@ -300,7 +333,8 @@ class IncompressibleHydro(ReferenceOrderRHS, Physics):
         pp = self._params3d()
         ppa = None if pp is None else (ctypes.c_double * len(pp))(*pp)
         _lib.call("dd_rk4_step3d", plan.handle, phys, ppa, sp, None if ik2 is None else dptr(ik2), th, tf,
-                  cf, vo, float(dt), prec, None, dptr(ws), ws.numel(), current_stream())
+                  cf, vo, float(dt), prec, None if nonkept is None else ctypes.byref(nonkept), dptr(ws), ws.numel(),
+                  current_stream())
         return True
 
     # ------------------------------------------------------------ 2D

@@ -60,6 +60,9 @@ class FourierRepresentation(Representation):
         self.data = self.kdata
         self.fwd_count = 0
         self.rev_count = 0
+        # bumped by every public read or write of the data (a read hands out a
+        # writable view); the fused steps re-check a state whose version moved
+        self._version = 0
 
     # ------------------------------------------------------------ storage
     def set_fft(self, method, dealiasing):
@@ -104,7 +107,14 @@ class FourierRepresentation(Representation):
     # ------------------------------------------------------- space access
     def __getitem__(self, space):
         self.require_space(space)
+        self._version += 1
         return self.data
+
+    def touch(self):
+        """Mark the data as changed: call after writing .kdata / .xdata
+        directly (not through ['kspace'] / ['xspace']), so that the fused steps
+        re-check the state's form (solenoidal, energy outside the kept modes)."""
+        self._version += 1
 
     def __setitem__(self, space, data):
         # representations.py:144-166
@@ -125,6 +135,7 @@ class FourierRepresentation(Representation):
                 src = src.expand(self.data.shape)
             self.data.copy_(src)
         self._curr_space = space
+        self._version += 1
 
     def to_numpy(self, space=None):
         """Host copy of the data in `space` (current space if None)."""
@@ -157,6 +168,7 @@ class FourierRepresentation(Representation):
         self.data = self.kdata
         self._curr_space = 'kspace'
         self.fwd_count += 1
+        self._version += 1
 
     def backward(self):
         # representations.py:347-357
@@ -167,6 +179,7 @@ class FourierRepresentation(Representation):
         self.data = self.xdata
         self._curr_space = 'xspace'
         self.rev_count += 1
+        self._version += 1
 
     def dealias(self):
         """2/3 rule (or Nyquist-only for dealiasing None), in place in k-space."""

@@ -279,3 +279,43 @@ def test_divergence_form_rhs_matches_rotational(dd, cuda, prec):
     got = sums.cpu().numpy()
     assert abs(got[1] - ref1) <= 1e-12 * ref1
     assert got[0] <= 1e-24 * ref1 and ref0 <= 1e-24 * ref1
+
+
+@pytest.mark.gpu
+def test_state_form_is_rechecked_when_the_state_changes(dd, cuda):
+    """The fused step reuses its solenoidality / non-kept check while the
+    state is only advanced by fused steps, and re-checks it after a write
+    through the public API or a touch() after a direct write: a divergent
+    state then takes the rotational form, a state with energy outside the kept
+    modes has them decayed, both matching the oracle."""
+    shape = (32, 32, 32)
+    u0 = dd.init_cond.turbulence_3d(shape, seed=12)
+    rg, dg = gpu_hydro(dd, shape, 5e-3, u0)
+    ti = dd.mods.RK4(rg)
+    ti.do_advance(dg, 2e-3)
+    ti.do_advance(dg, 2e-3)
+    assert rg.last_phys3d == 2
+    # a divergent state written through the API
+    kx, ky, kz = dd.kgrid.k_tables(shape, (2 * np.pi,) * 3)
+    grad = [kx[None, None, :], ky[:, None, None], kz[None, :, None]]
+    phi = np.zeros_like(u0[0])
+    phi[1:4, 1:4, 1:4] = 0.05
+    u1 = [host_u(dg)[i] + 1j * grad[i] * phi for i in range(3)]
+    for i in range(3):
+        dg['u'][i]['kspace'] = u1[i]
+    ti.do_advance(dg, 2e-3)
+    assert rg.last_phys3d == 0
+    ro, do = oracle_hydro(shape, 5e-3, u1)
+    OT.RK4(ro).do_advance(do, 2e-3)
+    assert rel_l2(host_u(dg), [do['u'][i]['kspace'] for i in range(3)]) < 1e-12
+    # energy outside the kept modes written directly, announced with touch()
+    rng = np.random.default_rng(3)
+    u2 = [c + 1e-3 * (rng.standard_normal(c.shape) + 1j * rng.standard_normal(c.shape)) for c in u0]
+    for i in range(3):
+        import torch
+        dg['u'][i].kdata.copy_(torch.from_numpy(u2[i]))
+        dg['u'][i].touch()
+    ti.do_advance(dg, 2e-3)
+    ro2, do2 = oracle_hydro(shape, 5e-3, u2)
+    OT.RK4(ro2).do_advance(do2, 2e-3)
+    assert rel_l2(host_u(dg), [do2['u'][i]['kspace'] for i in range(3)]) < 1e-12
