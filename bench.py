@@ -557,7 +557,8 @@ def cpu_reference_steps(wl, nsteps, workers, time_budget, seed=0):
         if "gain" in z.files:
             norm[40:46] *= np.float32(z["gain"])
         band = tuple(float(b) for b in z["band"]) if "band" in z.files else (0.0, 0.0)
-        rhs = OC.les_physics(shape, z["params"], norm, float(z["delta"]), band=band)
+        shells = z["shell_w"] if "shell_w" in z.files else None
+        rhs = OC.les_physics(shape, z["params"], norm, float(z["delta"]), band=band, shells=shells)
         rhs.parameters["nu"] = wl["nu"]
         fields = list(zip([("u", 0), ("u", 1), ("u", 2)], dd.init_cond.turbulence_3d(shape, seed=seed)))
         ti_cls = OT.RK4
