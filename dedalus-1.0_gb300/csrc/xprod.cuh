@@ -185,10 +185,15 @@ k_x_prod(int nrows, int Kx, CPtrs win, Ptrs wout, int64_t in_rs, int64_t out_rs,
     } else {
         pencil_fft_s<T, SF, false>(tile, tw, threadIdx.x < SF::NT);
     }
+    // field-major order: consecutive threads write the block's Q consecutive rows
+    // of one output field, a contiguous range, so a 32-byte sector shared by two
+    // rows (complex64 rows of an odd number of half-sectors) is written whole by
+    // one warp instead of in two halves at different times
     for (int idx = threadIdx.x; idx < Kx * Q * NO; idx += NT) {
-        const int k = idx % Kx, t = idx / Kx;
-        const int r = t / NO, g = t % NO;
+        const int k = idx % Kx, u = idx / Kx;
+        const int g = u / Q, r = u % Q;
         if (r >= nr) continue;
+        const int t = r * NO + g;              // its real row in the packed tile
         C<T> A, B;
         unpack_rows<T>(tile + t / 2, PSF, k, L, scale, A, B);
         stc<T>((V*)wout.p[g] + ob + (int64_t)(row0 + r) * Kx + k, (t & 1) ? B : A);
