@@ -92,6 +92,18 @@ constexpr size_t prod_smem(size_t csize) {
     return csize * ((a > b ? a : b) + L);
 }
 
+// p[i] for a runtime i < N from a pointer table passed by value: a chain of
+// selects over the compile-time range, so the table stays in the parameter
+// space (indexing it directly would copy it to every thread's local memory).
+template <int N, typename PT>
+__device__ __forceinline__ PT pick_ptr(const PT* p, int i) {
+    PT r = p[0];
+#pragma unroll
+    for (int j = 1; j < N; j++)
+        if (i == j) r = p[j];
+    return r;
+}
+
 template <typename T, int L, class Op>
 __global__ void __launch_bounds__(ProdCfgT<T, L, Op::NI, Op::NO>::NT, std::is_same<T, df64>::value ? 5 : 1)
 k_x_prod(int nrows, int Kx, CPtrs win, Ptrs wout, int64_t in_rs, int64_t out_rs,
@@ -125,8 +137,8 @@ k_x_prod(int nrows, int Kx, CPtrs win, Ptrs wout, int64_t in_rs, int64_t out_rs,
             const int ra = ta / NI, fa = ta % NI, rb = tb / NI, fb = tb % NI;
             const bool va = ra < nr, vb = tb < NI * Q && rb < nr;
             if (va || vb) {
-                const V* pa = (const V*)win.p[fa] + ib + (int64_t)(row0 + (va ? ra : rb)) * Kx;
-                const V* pb = (const V*)win.p[vb ? fb : fa] + ib + (int64_t)(row0 + (vb ? rb : ra)) * Kx;
+                const V* pa = (const V*)pick_ptr<NI>(win.p, fa) + ib + (int64_t)(row0 + (va ? ra : rb)) * Kx;
+                const V* pb = (const V*)pick_ptr<NI>(win.p, vb ? fb : fa) + ib + (int64_t)(row0 + (vb ? rb : ra)) * Kx;
                 z = pack_rows<T>(pa, pb, e, L, Kx);
                 if (!va) z.x = T(0);
                 if (!vb) z.y = T(0);
@@ -196,7 +208,7 @@ k_x_prod(int nrows, int Kx, CPtrs win, Ptrs wout, int64_t in_rs, int64_t out_rs,
         const int t = r * NO + g;              // its real row in the packed tile
         C<T> A, B;
         unpack_rows<T>(tile + t / 2, PSF, k, L, scale, A, B);
-        stc<T>((V*)wout.p[g] + ob + (int64_t)(row0 + r) * Kx + k, (t & 1) ? B : A);
+        stc<T>((V*)pick_ptr<NO>(wout.p, g) + ob + (int64_t)(row0 + r) * Kx + k, (t & 1) ? B : A);
     }
 }
 
