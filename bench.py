@@ -78,8 +78,8 @@ TRAFFIC = {
         8 * (67.76e6 + 18.20e6),
         "ncu capture of the same kernel on 128^3 FP64 (67.76 MB read + 18.20 MB written), x8 for 256^3"),
     ("hydro3d-256-fp64", "x_div_256_f64"): (
-        4 * (67.73e6 + 70.01e6),
-        "ncu capture of the same kernel on 128x128x256 FP64 (67.73 MB read + 70.01 MB written), x4 rows for 256^3"),
+        4 * (67.81e6 + 50.79e6),
+        "ncu capture of the same kernel on 128x128x256 FP64 (67.81 MB read + 50.79 MB written), x4 rows for 256^3"),
     ("les64-closure", "les_mlp"): (
         18.92e6 + 0.0, "ncu capture at full size (18.92 MB read, stresses still in L2 at kernel end)"),
 }

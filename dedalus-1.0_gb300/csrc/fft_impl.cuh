@@ -9,7 +9,7 @@ namespace dd {
 template <typename KT>
 __global__ void k_zero_nonkept3(Geo3 g, Ptrs k) {
     using KV = typename Vec2<KT>::type;
-    KV* K = (KV*)k.p[blockIdx.y];
+    KV* K = (KV*)pick_ptr<DD_MAXF>(k.p, (int)blockIdx.y);
     const int64_t n = g.kcount();
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const int kx = (int)(i % g.Nh);
@@ -21,7 +21,7 @@ __global__ void k_zero_nonkept3(Geo3 g, Ptrs k) {
 template <typename KT>
 __global__ void k_zero_nonkept2(Geo2 g, Ptrs k) {
     using KV = typename Vec2<KT>::type;
-    KV* K = (KV*)k.p[blockIdx.y];
+    KV* K = (KV*)pick_ptr<DD_MAXF>(k.p, (int)blockIdx.y);
     const int64_t n0 = (int64_t)g.Kx * g.Ny, n = g.kcount();
     for (int64_t i = n0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         KV z; z.x = 0; z.y = 0; K[i] = z;

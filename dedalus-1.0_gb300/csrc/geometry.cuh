@@ -46,4 +46,17 @@ struct CPtrs {
     const void* p[DD_MAXF];
 };
 
+// p[i] for a runtime i < N from a pointer table passed by value: a chain of
+// selects over the compile-time range, so the table stays in the parameter
+// space (indexing it directly would copy it to every thread's local memory).
+template <int N, typename PT>
+__device__ __forceinline__ PT pick_ptr(const PT* p, int i) {
+    PT r = p[0];
+#pragma unroll
+    for (int j = 1; j < N; j++)
+        if (i == j) r = p[j];
+    return r;
+}
+
+
 }  // namespace dd

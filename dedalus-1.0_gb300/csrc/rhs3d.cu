@@ -309,7 +309,9 @@ __global__ void k_decay_nonkept3(RK4Args a, int ncomp) {
 __global__ void k_any_nonkept3(Geo3 g, CPtrs y, int ncomp, int* flag) {
     const int64_t n = g.kcount();
     int found = 0;
-    for (int c = 0; c < ncomp; c++) {
+#pragma unroll
+    for (int c = 0; c < DD_MAXF; c++) {   // constant indices keep y in the parameter space
+        if (c >= ncomp) break;
         const double2* Y = (const double2*)y.p[c];
         for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
             const int ix = (int)(i % g.Nh);
@@ -325,7 +327,7 @@ __global__ void k_any_nonkept3(Geo3 g, CPtrs y, int ncomp, int* flag) {
 
 // Zero every non-kept entry of full-layout arrays (grid.y = component).
 __global__ void k_dealias3_all(Geo3 g, Ptrs k) {
-    double2* K = (double2*)k.p[blockIdx.y];
+    double2* K = (double2*)pick_ptr<DD_MAXF>(k.p, (int)blockIdx.y);
     const int64_t n = g.kcount();
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const int ix = (int)(i % g.Nh);

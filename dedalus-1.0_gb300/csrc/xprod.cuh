@@ -92,18 +92,6 @@ constexpr size_t prod_smem(size_t csize) {
     return csize * ((a > b ? a : b) + L);
 }
 
-// p[i] for a runtime i < N from a pointer table passed by value: a chain of
-// selects over the compile-time range, so the table stays in the parameter
-// space (indexing it directly would copy it to every thread's local memory).
-template <int N, typename PT>
-__device__ __forceinline__ PT pick_ptr(const PT* p, int i) {
-    PT r = p[0];
-#pragma unroll
-    for (int j = 1; j < N; j++)
-        if (i == j) r = p[j];
-    return r;
-}
-
 template <typename T, int L, class Op>
 __global__ void __launch_bounds__(ProdCfgT<T, L, Op::NI, Op::NO>::NT, std::is_same<T, df64>::value ? 5 : 1)
 k_x_prod(int nrows, int Kx, CPtrs win, Ptrs wout, int64_t in_rs, int64_t out_rs,
