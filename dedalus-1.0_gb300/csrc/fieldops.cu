@@ -47,7 +47,9 @@ __global__ void k_scale_add(const double2* x, double2* y, double w, int accumula
 // *out must hold +0.0 (all-zero bits) on entry.
 __global__ void k_max_square(CPtrs x, int ncomp, int64_t n, unsigned long long* out) {
     double m = 0.0;
-    for (int c = 0; c < ncomp; c++) {
+#pragma unroll
+    for (int c = 0; c < DD_MAXF; c++) {   // constant indices keep x in the parameter space
+        if (c >= ncomp) break;
         const double* xc = (const double*)x.p[c];
         for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
             const double v = xc[i];

@@ -157,7 +157,7 @@ __global__ void k_decay_nonkept2(Geo2 g, Ptrs y, int64_t y_rs, int nf, int nrun,
         const double k2 = radd(rmul(kx[ix], kx[ix]), rmul(ky[ky_i], ky[ky_i]));
         const int q = a.intk ? (int)k2 : 0;
         for (int c = 0; c < nf; c++) {
-            double2* Y = (double2*)y.p[c] + run * y_rs;
+            double2* Y = (double2*)pick_ptr<DD_MAXF>(y.p, c) + run * y_rs;
             const double2 y0 = Y[j];
             if (y0.x == 0. && y0.y == 0.) continue;
             double Z, f0, f1, f2;
@@ -169,7 +169,7 @@ __global__ void k_decay_nonkept2(Geo2 g, Ptrs y, int64_t y_rs, int nf, int nrun,
 }
 
 __global__ void k_zero_nonkept2_all(Geo2 g, Ptrs k, int64_t rs, int nrun) {
-    double2* K = (double2*)k.p[blockIdx.y];
+    double2* K = (double2*)pick_ptr<DD_MAXF>(k.p, (int)blockIdx.y);
     const int64_t per = g.kcount(), n = per * nrun;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const int run = (int)(i / per);
