@@ -35,9 +35,10 @@ How the reference is made to run under Python 3 (it is Python 2 code):
 
 Cases (inputs seeded with numpy PCG64; all fields are real by construction:
 drawn in grid space and transformed with the reference's own forward
-transform): one ``RHS`` call and three ``RK2mid`` steps each of 2D hydro
-32^2, 3D hydro 16^3, 2D Boussinesq 32^2 (direction y), 3D MHD 16^3, two
-``RK2trap`` steps of 3D hydro 16^3, and ``compute_dt`` for each physics.
+transform): one ``RHS`` call and two or three ``RK2mid`` steps each of 2D
+hydro 32^2, 3D hydro 16^3, 2D Boussinesq 32^2 (direction y), 3D Boussinesq
+16^3 (direction z), 3D MHD 16^3 and 2D MHD 32^2, two ``RK2trap`` steps of 3D
+hydro 16x8x32 and of 2D Boussinesq 32^2, and ``compute_dt`` for each.
 Outputs go to ``tests/golden/ref_<case>.npz``.  The reference's RK4 cannot
 run (``RKBase.forward_step`` calls methods defined nowhere,
 ``time_step.py:209-218``), so no fixture exists for it.
@@ -253,6 +254,14 @@ CASES = [
      [('u', 0), ('u', 1), ('T', 0)], "RK2mid", 3, 1e-2, 4),
     ("mhd3d_16", "IncompressibleMHD", (16, 16, 16), {'nu': 5e-3, 'eta': 8e-3, 'rho0': 1.5},
      [('u', 0), ('u', 1), ('u', 2), ('B', 0), ('B', 1), ('B', 2)], "RK2mid", 2, 1e-2, 5),
+    ("bouss3d_16", "BoussinesqHydro", (16, 16, 16),
+     {'nu': 4e-3, 'kappa': 6e-3, 'g': 1.5, 'alpha_t': 0.8, 'beta': 1.2},
+     [('u', 0), ('u', 1), ('u', 2), ('T', 0)], "RK2mid", 2, 1e-2, 6),
+    ("mhd2d_32", "IncompressibleMHD", (32, 32), {'nu': 3e-3, 'eta': 5e-3},
+     [('u', 0), ('u', 1), ('B', 0), ('B', 1)], "RK2mid", 2, 1e-2, 7),
+    ("bouss2d_32_trap", "BoussinesqHydro", (32, 32),
+     {'nu': 2e-3, 'kappa': 2e-3, 'g': 1., 'alpha_t': 1., 'beta': 1., 'boussinesq_direction': 'y'},
+     [('u', 0), ('u', 1), ('T', 0)], "RK2trap", 2, 1e-2, 8),
 ]
 
 

@@ -53,7 +53,7 @@ def seeded(rhs, z, names):
 
 
 def test_fixtures_present():
-    assert len(FILES) == 5, FILES
+    assert len(FILES) == 8, FILES
 
 
 @pytest.mark.parametrize("path", FILES, ids=[os.path.basename(f)[4:-4] for f in FILES])
