@@ -500,7 +500,8 @@ class LesRunner:
     def kernel_bytes(self, label):
         n = int(np.prod(self.wl["shape"]))
         if label == "les_mlp":
-            return 15 * 8 * n          # 9 gradients in, 6 stresses out (FP64)
+            # 9 gradients in, 6 stresses out: float fields on the FP32 path, double on FP64
+            return 15 * (4 if self.wl["precision"] == "fp32" else 8) * n
         return None
 
     def kernel_flops(self, label):

@@ -59,8 +59,10 @@ inline size_t ws_bytes(const dd_plan* pl, int nf) {
     return (size_t)nf * pl->g2.wcount() * sizeof(C<T>);
 }
 
-template <typename T>
-int fft_c2r(const dd_plan* pl, int nf, const void* const* k, double* const* x, void* work, size_t wb,
+// XT is the type of the grid-point values (double, or float beside float
+// arithmetic: the values are the same, at half the bytes).
+template <typename T, typename XT = double>
+int fft_c2r(const dd_plan* pl, int nf, const void* const* k, XT* const* x, void* work, size_t wb,
             cudaStream_t st) {
     DD_CHECK_ARG(wb >= ws_bytes<T>(pl, nf), "workspace too small: %zu < %zu bytes", wb, ws_bytes<T>(pl, nf));
     CPtrs kin{}; Ptrs xo{};
@@ -79,7 +81,7 @@ int fft_c2r(const dd_plan* pl, int nf, const void* const* k, double* const* x, v
         OpYInv3<T> b{g, w1c, w2, TwSel<T>::y(pl)};
         DD_TRY((launch_pass_len<T, true, false, false>(g.Ny, b, g.Kx, g.Nz, nf, st)));
         const int nrows = g.Nz * g.Ny;
-        OpXc2r3<T, double> c{nrows, g.Nx, g.Kx, w2c, xo, TwSel<T>::x(pl)};
+        OpXc2r3<T, XT> c{nrows, g.Nx, g.Kx, w2c, xo, TwSel<T>::x(pl)};
         DD_TRY((launch_pass_len<T, true, true, true>(g.Nx, c, (nrows + 1) / 2, 1, nf, st)));
     } else {
         const Geo2& g = pl->g2;
@@ -88,7 +90,7 @@ int fft_c2r(const dd_plan* pl, int nf, const void* const* k, double* const* x, v
         for (int f = 0; f < nf; f++) { w.p[f] = W + f * g.wcount(); wc.p[f] = w.p[f]; }
         OpYInv2<T, double> a{g, kin, w, TwSel<T>::y(pl)};
         DD_TRY((launch_pass_len<T, true, true, false>(g.Ny, a, g.Kx, 1, nf, st)));
-        OpXc2r3<T, double> c{g.Ny, g.Nx, g.Kx, wc, xo, TwSel<T>::x(pl)};
+        OpXc2r3<T, XT> c{g.Ny, g.Nx, g.Kx, wc, xo, TwSel<T>::x(pl)};
         DD_TRY((launch_pass_len<T, true, true, true>(g.Nx, c, (g.Ny + 1) / 2, 1, nf, st)));
     }
     return DD_OK;
@@ -96,8 +98,8 @@ int fft_c2r(const dd_plan* pl, int nf, const void* const* k, double* const* x, v
 
 // zero_nonkept = false leaves the entries outside the kept set unwritten (for
 // internal callers that read kept modes only).
-template <typename T>
-int fft_r2c(const dd_plan* pl, int nf, const double* const* x, void* const* k, void* work, size_t wb,
+template <typename T, typename XT = double>
+int fft_r2c(const dd_plan* pl, int nf, const XT* const* x, void* const* k, void* work, size_t wb,
             cudaStream_t st, bool zero_nonkept = true) {
     DD_CHECK_ARG(wb >= ws_bytes<T>(pl, nf), "workspace too small: %zu < %zu bytes", wb, ws_bytes<T>(pl, nf));
     CPtrs xin{}; Ptrs ko{};
@@ -113,7 +115,7 @@ int fft_r2c(const dd_plan* pl, int nf, const double* const* x, void* const* k, v
             w2.p[f] = W2 + f * g.w2count(); w2c.p[f] = w2.p[f];
         }
         const int nrows = g.Nz * g.Ny;
-        OpXr2c3<T, double> a{nrows, g.Nx, g.Kx, s, xin, w2, TwSel<T>::x(pl)};
+        OpXr2c3<T, XT> a{nrows, g.Nx, g.Kx, s, xin, w2, TwSel<T>::x(pl)};
         DD_TRY((launch_pass_len<T, false, true, true>(g.Nx, a, (nrows + 1) / 2, 1, nf, st)));
         OpYFwd3<T> b{g, w2c, w1, TwSel<T>::y(pl)};
         DD_TRY((launch_pass_len<T, false, false, false>(g.Ny, b, g.Kx, g.Nz, nf, st)));
@@ -128,7 +130,7 @@ int fft_r2c(const dd_plan* pl, int nf, const double* const* x, void* const* k, v
         C<T>* W = (C<T>*)work;
         Ptrs w{}; CPtrs wc{};
         for (int f = 0; f < nf; f++) { w.p[f] = W + f * g.wcount(); wc.p[f] = w.p[f]; }
-        OpXr2c3<T, double> a{g.Ny, g.Nx, g.Kx, s, xin, w, TwSel<T>::x(pl)};
+        OpXr2c3<T, XT> a{g.Ny, g.Nx, g.Kx, s, xin, w, TwSel<T>::x(pl)};
         DD_TRY((launch_pass_len<T, false, true, true>(g.Nx, a, (g.Ny + 1) / 2, 1, nf, st)));
         OpYFwd2<T, double> b{g, wc, ko, TwSel<T>::y(pl)};
         DD_TRY((launch_pass_len<T, false, false, true>(g.Ny, b, g.Kx, 1, nf, st)));
@@ -145,5 +147,10 @@ int fft_r2c(const dd_plan* pl, int nf, const double* const* x, void* const* k, v
     EXT template int fft_c2r<T>(const dd_plan*, int, const void* const*, double* const*, void*, size_t, cudaStream_t); \
     EXT template int fft_r2c<T>(const dd_plan*, int, const double* const*, void* const*, void*, size_t, cudaStream_t, \
                                 bool);
+#define DD_FFT_INSTANTIATE_X(EXT, T, XT)                                                                 \
+    EXT template int fft_c2r<T, XT>(const dd_plan*, int, const void* const*, XT* const*, void*, size_t,        \
+                                    cudaStream_t);                                                          \
+    EXT template int fft_r2c<T, XT>(const dd_plan*, int, const XT* const*, void* const*, void*, size_t,        \
+                                    cudaStream_t, bool);
 
 }  // namespace dd

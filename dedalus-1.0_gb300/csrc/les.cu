@@ -10,6 +10,7 @@ namespace dd {
 
 DD_FFT_INSTANTIATE(extern, double)
 DD_FFT_INSTANTIATE(extern, float)
+DD_FFT_INSTANTIATE_X(extern, float, float)
 
 static inline size_t up256(size_t b) { return (b + 255) & ~(size_t)255; }
 
@@ -51,94 +52,169 @@ __global__ void k_les_grad9(Geo3 g, const double* kx, const double* ky, const do
     }
 }
 
-// Closure network at the grid points.  Every warp works on its own tiles of
-// 16 points with private activation buffers (no block-wide barrier after the
-// weights are staged): the 9 gradients and the width are normalised to BF16
-// inputs, the MLP runs on the tensor cores and the 6 stresses are written.
-// tau may alias gx[0..5]: a warp reads all inputs of a tile before it writes
-// that tile's outputs, and tiles are disjoint.
-constexpr int LES_WARPS = 8;
+// Closure network at the grid points, one warp per tile of 16 points, with no
+// shared memory but the weights.  A lane loads its own entries of the first
+// product's A fragment straight from the gradient fields (lane 4 g + t holds
+// points g and g + 8 of the tile, inputs 2t, 2t + 1, 2t + 8, 2t + 9; input 8
+// is the ninth gradient and input 9 the width, so only t = 0 has the upper
+// pair), and the accumulator fragments of two adjacent 8-column tiles of a
+// layer are, rounded to BF16, the A fragment of one 16-column k tile of the
+// next layer: the activations never leave registers.  The products, their
+// order and the rounding points are those of mlp_forward16.  The next tile's
+// gradients are loaded while the current tile computes.  tau may alias
+// gx[0..5]: a warp has all inputs of a tile in registers before it writes that
+// tile's outputs, and tiles are disjoint.
+constexpr int LES_WARPS = 4;
 
 struct LesMlpSmem {
     bf16 w1[MLP_H * LDI];
     bf16 w2[MLP_H * LDH];
-    bf16 w3[16 * LDH];
+    bf16 w3[8 * LDH];         // the 8 output rows in use
     float b1[MLP_H], b2[MLP_H], b3[MLP_OUT];
-    float norm[MLP_NNORM];
-    struct Warp {
-        bf16 x[16 * LDI];
-        bf16 h1[16 * LDH];
-        bf16 h2[16 * LDH];
-    } w[LES_WARPS];
 };
 
+// B fragments from a row-major [out][in] BF16 weight matrix in shared memory
+// by ldmatrix (lane 4 g + t receives row g, columns 2t, 2t + 1 of each 8 x 8
+// matrix; lane 8 i + r gives the address of row r of matrix i).  Row strides
+// are multiples of 16 bytes.
+__device__ __forceinline__ void les_ldsm(uint32_t r[4], const bf16* q) {
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(q);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(a));
+}
+// rows [n0, n0 + 8), k tiles [k0, k0 + 16) and [k0 + 16, k0 + 32): r[0..1]
+// and r[2..3] are the B fragments of the two k tiles
+__device__ __forceinline__ void les_ldb_k32(uint32_t r[4], const bf16* w, int ld, int n0, int k0) {
+    const int lane = threadIdx.x & 31;
+    les_ldsm(r, w + (n0 + (lane & 7)) * ld + k0 + 8 * (lane >> 3));
+}
+// rows [n0, n0 + 8) and [n0 + 8, n0 + 16), k tile [k0, k0 + 16): r[0..1] and
+// r[2..3] are the B fragments of the two n tiles
+__device__ __forceinline__ void les_ldb_n16(uint32_t r[4], const bf16* w, int ld, int n0, int k0) {
+    const int lane = threadIdx.x & 31;
+    les_ldsm(r, w + (n0 + 8 * (lane >> 4) + (lane & 7)) * ld + k0 + 8 * ((lane >> 3) & 1));
+}
+
+__device__ __forceinline__ void les_mma(float c[4], const uint32_t a[4], uint32_t b0, uint32_t b1) {
+    const uint32_t b[2] = {b0, b1};
+    mma_bf16_16816(c, a, b);
+}
+
+// Hidden activations of an accumulator tile (rows g, g + 8; columns n + 2t,
+// n + 2t + 1 with bias + n the bias pair): lo/hi = the A-fragment registers of
+// rows g and g + 8 in the next layer.
+__device__ __forceinline__ void les_act(const float c[4], const float* bias, uint32_t& lo, uint32_t& hi) {
+    const float2 bb = *reinterpret_cast<const float2*>(bias);
+    lo = pack2(__float2bfloat16_rn(tanhf(c[0] + bb.x)), __float2bfloat16_rn(tanhf(c[1] + bb.y)));
+    hi = pack2(__float2bfloat16_rn(tanhf(c[2] + bb.x)), __float2bfloat16_rn(tanhf(c[3] + bb.y)));
+}
+
+template <typename GT, typename TT>
 __global__ void __launch_bounds__(32 * LES_WARPS) k_les_mlp(CPtrs gx, Ptrs tau, int64_t npts, const bf16* wb,
                                                             const float* p, const float* norm, double delta) {
-    extern __shared__ __align__(16) unsigned char les_smem[];
-    LesMlpSmem& s = *reinterpret_cast<LesMlpSmem*>(les_smem);
+    __shared__ __align__(16) LesMlpSmem s;
     for (int i = threadIdx.x; i < MLP_H * MLP_IN; i += blockDim.x)
         s.w1[(i / MLP_IN) * LDI + i % MLP_IN] = wb[BOFF_W1 + i];
     for (int i = threadIdx.x; i < MLP_H * MLP_H; i += blockDim.x)
         s.w2[(i / MLP_H) * LDH + i % MLP_H] = wb[BOFF_W2 + i];
-    for (int i = threadIdx.x; i < 16 * MLP_H; i += blockDim.x)
+    for (int i = threadIdx.x; i < 8 * MLP_H; i += blockDim.x)
         s.w3[(i / MLP_H) * LDH + i % MLP_H] = wb[BOFF_W3 + i];
     for (int i = threadIdx.x; i < MLP_H; i += blockDim.x) {
         s.b1[i] = p[OFF_B1 + i];
         s.b2[i] = p[OFF_B2 + i];
     }
     if (threadIdx.x < MLP_OUT) s.b3[threadIdx.x] = p[OFF_B3 + threadIdx.x];
-    if (threadIdx.x < MLP_NNORM) s.norm[threadIdx.x] = norm[threadIdx.x];
     __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    LesMlpSmem::Warp& w = s.w[warp];
-    const MlpW W{s.w1, s.w2, s.w3, s.b1, s.b2, s.b3};
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const bool lead = t == 0;
+    // this lane's inputs 2t, 2t + 1 (and 8 for t = 0), their normalisation
+    const GT* src0 = (const GT*)pick_ptr<8>(gx.p, 2 * t);
+    const GT* src1 = (const GT*)pick_ptr<8>(gx.p, 2 * t + 1);
+    const GT* src8 = (const GT*)gx.p[8];
+    const float m0 = norm[NORM_IN_MEAN + 2 * t], s0 = norm[NORM_IN_SCALE + 2 * t];
+    const float m1 = norm[NORM_IN_MEAN + 2 * t + 1], s1 = norm[NORM_IN_SCALE + 2 * t + 1];
+    const float m8 = norm[NORM_IN_MEAN + 8], s8 = norm[NORM_IN_SCALE + 8];
+    const bf16 xd = __float2bfloat16_rn(((float)delta - norm[NORM_IN_MEAN + 9]) * norm[NORM_IN_SCALE + 9]);
+    // this lane's outputs 2t, 2t + 1 (stresses 0..5: t < 3)
+    const bool out = t < 3;
+    TT* dst0 = (TT*)pick_ptr<MLP_NOUT>(tau.p, out ? 2 * t : 0);
+    TT* dst1 = (TT*)pick_ptr<MLP_NOUT>(tau.p, out ? 2 * t + 1 : 0);
+    const float om0 = norm[NORM_OUT_MEAN + 2 * t], os0 = norm[NORM_OUT_SCALE + 2 * t];
+    const float om1 = norm[NORM_OUT_MEAN + 2 * t + 1], os1 = norm[NORM_OUT_SCALE + 2 * t + 1];
+    const float b30 = s.b3[2 * t], b31 = s.b3[2 * t + 1];
+    // the output layer's B fragments (8 x 64) stay in registers
+    uint32_t w3[8];
+    les_ldb_k32(w3, s.w3, LDH, 0, 0);
+    les_ldb_k32(w3 + 4, s.w3, LDH, 0, 32);
+
     const int64_t ntiles = (npts + 15) / 16;
     const int64_t stride = (int64_t)gridDim.x * LES_WARPS;
-    // lane -> point lane % 16 of a tile and the gradient columns of parity
-    // lane / 16 (field indices stay compile-time constants); the next tile's
-    // gradients are loaded into registers while the current tile computes
-    const int r = lane & 15, half = lane >> 4;
-    double g[5];
-    const double* src[5];
-#pragma unroll
-    for (int j = 0; j < 5; j++) {
-        const double* p0 = (const double*)gx.p[2 * j];
-        const double* p1 = 2 * j + 1 < 9 ? (const double*)gx.p[2 * j + 1] : p0;
-        src[j] = half ? p1 : p0;
-    }
+    float f[6];
     auto fetch = [&](int64_t tile) {
-        const int64_t pt = tile * 16 + r;
-        const bool ok = tile < ntiles && pt < npts;
-#pragma unroll
-        for (int j = 0; j < 5; j++) g[j] = (ok && 2 * j + half < 9) ? src[j][pt] : 0.;
+        const int64_t pa = tile * 16 + g, pb = pa + 8;
+        const bool oka = tile < ntiles && pa < npts, okb = tile < ntiles && pb < npts;
+        f[0] = oka ? (float)src0[pa] : 0.f;
+        f[1] = oka ? (float)src1[pa] : 0.f;
+        f[2] = okb ? (float)src0[pb] : 0.f;
+        f[3] = okb ? (float)src1[pb] : 0.f;
+        f[4] = (lead && oka) ? (float)src8[pa] : 0.f;
+        f[5] = (lead && okb) ? (float)src8[pb] : 0.f;
     };
-    int64_t t = (int64_t)blockIdx.x * LES_WARPS + warp;
-    fetch(t);
-    for (; t < ntiles; t += stride) {
-        const int64_t base = t * 16;
-        __syncwarp();
+    auto nrm = [](float v, float m, float sc) { return __float2bfloat16_rn((v - m) * sc); };
+    int64_t tile = (int64_t)blockIdx.x * LES_WARPS + warp;
+    fetch(tile);
+    for (; tile < ntiles; tile += stride) {
+        uint32_t x[1][4];
+        x[0][0] = pack2(nrm(f[0], m0, s0), nrm(f[1], m1, s1));
+        x[0][1] = pack2(nrm(f[2], m0, s0), nrm(f[3], m1, s1));
+        x[0][2] = lead ? pack2(nrm(f[4], m8, s8), xd) : 0u;   // inputs 10..15 are zero
+        x[0][3] = lead ? pack2(nrm(f[5], m8, s8), xd) : 0u;
+        fetch(tile + stride);
+        // first hidden layer, n tiles in pairs
+        uint32_t h1[4][4];
 #pragma unroll
-        for (int j = 0; j < 8; j++) {
-            const int a = 2 * j + half;
-            float v = 0.f;
-            if (a < 9) v = (float)g[j < 5 ? j : 4];
-            else if (a == 9) v = (float)delta;
-            if (a < MLP_NIN) v = (v - s.norm[NORM_IN_MEAN + a]) * s.norm[NORM_IN_SCALE + a];
-            w.x[r * LDI + a] = __float2bfloat16_rn(v);
+        for (int np = 0; np < 4; np++) {
+            uint32_t b[4];
+            les_ldb_n16(b, s.w1, LDI, 16 * np, 0);
+            float c0[4] = {0.f, 0.f, 0.f, 0.f}, c1[4] = {0.f, 0.f, 0.f, 0.f};
+            les_mma(c0, x[0], b[0], b[1]);
+            les_mma(c1, x[0], b[2], b[3]);
+            les_act(c0, s.b1 + 16 * np + 2 * t, h1[np][0], h1[np][1]);
+            les_act(c1, s.b1 + 16 * np + 8 + 2 * t, h1[np][2], h1[np][3]);
         }
-        fetch(t + stride);
-        __syncwarp();
-        float y[4];
-        mlp_forward16(W, w.x, w.h1, w.h2, y);
+        // second hidden layer; its n tiles 2 kt, 2 kt + 1 form k tile kt of the
+        // output layer, which accumulates as soon as they are done
+        float c[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
-            const int c = frag_col(q);
-            const int64_t pt = base + frag_row(q);
-            if (pt >= npts) continue;
-            const double v = (double)(y[q] * s.norm[NORM_OUT_SCALE + (c & 7)] + s.norm[NORM_OUT_MEAN + (c & 7)]);
+        for (int kt = 0; kt < 4; kt++) {
+            uint32_t h2[4];
 #pragma unroll
-            for (int cc = 0; cc < MLP_NOUT; cc++)
-                if (cc == c) ((double*)tau.p[cc])[pt] = v;
+            for (int hf = 0; hf < 2; hf++) {
+                const int nt = 2 * kt + hf;
+                float c2[4] = {0.f, 0.f, 0.f, 0.f};
+                uint32_t b[4];
+                les_ldb_k32(b, s.w2, LDH, 8 * nt, 0);
+                les_mma(c2, h1[0], b[0], b[1]);
+                les_mma(c2, h1[1], b[2], b[3]);
+                les_ldb_k32(b, s.w2, LDH, 8 * nt, 32);
+                les_mma(c2, h1[2], b[0], b[1]);
+                les_mma(c2, h1[3], b[2], b[3]);
+                les_act(c2, s.b2 + 8 * nt + 2 * t, h2[2 * hf], h2[2 * hf + 1]);
+            }
+            les_mma(c, h2, w3[2 * kt], w3[2 * kt + 1]);
+        }
+        if (out) {
+            const int64_t pa = tile * 16 + g, pb = pa + 8;
+            const float y0 = c[0] + b30, y1 = c[1] + b31, y2 = c[2] + b30, y3 = c[3] + b31;
+            if (pa < npts) {
+                dst0[pa] = (TT)(y0 * os0 + om0);
+                dst1[pa] = (TT)(y1 * os1 + om1);
+            }
+            if (pb < npts) {
+                dst0[pb] = (TT)(y2 * os0 + om0);
+                dst1[pb] = (TT)(y3 * os1 + om1);
+            }
         }
     }
 }
@@ -307,6 +383,7 @@ __global__ void __launch_bounds__(256) k_les_transfer_bins(int64_t n, const doub
 struct LesWork {
     double2* gk[9];   // gradient spectra, later the stress spectra (0..5)
     double* gx[9];    // gradients at the grid points, later the stresses (0..5)
+    float* gxf[9];    // the same region as float fields (FP32 path)
     void* fw;
     size_t fwb;
 };
@@ -323,15 +400,20 @@ static LesWork les_carve(const dd_plan* p, void* work) {
     char* b = (char*)work;
     for (int f = 0; f < 9; f++) w.gk[f] = (double2*)b + f * g.kcount();
     b += up256(9 * (size_t)g.kcount() * sizeof(double2));
-    for (int f = 0; f < 9; f++) w.gx[f] = (double*)b + f * g.xcount();
+    for (int f = 0; f < 9; f++) {
+        w.gx[f] = (double*)b + f * g.xcount();
+        w.gxf[f] = (float*)b + f * g.xcount();
+    }
     b += up256(9 * (size_t)g.xcount() * sizeof(double));
     w.fw = b;
     w.fwb = up256(ws_bytes<double>(p, 9));
     return w;
 }
 
+// Gradients at the grid points: into w.gxf as float when xf32 (FP32
+// transforms only), else into w.gx as double.
 static int les_grads(const dd_plan* p, int prec, bool compact, const void* const* y, const LesWork& w,
-                     cudaStream_t st) {
+                     bool xf32, cudaStream_t st) {
     const Geo3& g = p->g3;
     CPtrs yc{};
     Ptrs gk{};
@@ -342,25 +424,35 @@ static int les_grads(const dd_plan* p, int prec, bool compact, const void* const
     else DD_KT("les_grad9", st, k_les_grad9<false><<<nb, 256, 0, st>>>(g, p->kx, p->ky, p->kz, yc, gk));
     DD_LAUNCH_CHECK();
     const void* kin[9];
-    double* xo[9];
-    for (int f = 0; f < 9; f++) { kin[f] = w.gk[f]; xo[f] = w.gx[f]; }
-    if (prec == DD_FP32) return fft_c2r<float>(p, 9, kin, xo, w.fw, w.fwb, st);
-    return fft_c2r<double>(p, 9, kin, xo, w.fw, w.fwb, st);
+    for (int f = 0; f < 9; f++) kin[f] = w.gk[f];
+    if (prec == DD_FP32 && xf32) return fft_c2r<float, float>(p, 9, kin, w.gxf, w.fw, w.fwb, st);
+    if (prec == DD_FP32) return fft_c2r<float>(p, 9, kin, w.gx, w.fw, w.fwb, st);
+    return fft_c2r<double>(p, 9, kin, w.gx, w.fw, w.fwb, st);
 }
 
-static int les_mlp(const dd_plan* p, const dd_closure* cl, const LesWork& w, double* const* tau, cudaStream_t st) {
-    static std::atomic<unsigned long long> configured{0};
-    DD_TRY(ensure_smem((const void*)k_les_mlp, sizeof(LesMlpSmem), configured));
+template <typename GT, typename TT>
+static int les_mlp(const dd_plan* p, const dd_closure* cl, const GT* const* gxi, TT* const* tau, cudaStream_t st) {
     const int64_t npts = p->g3.xcount();
     CPtrs gx{};
     Ptrs t{};
-    for (int f = 0; f < 9; f++) gx.p[f] = w.gx[f];
+    for (int f = 0; f < 9; f++) gx.p[f] = gxi[f];
     for (int c = 0; c < 6; c++) t.p[c] = tau[c];
-    unsigned nb = les_grid(npts, 16 * LES_WARPS);
-    if (nb > 152 * 3) nb = 152 * 3;
+    // one resident wave of blocks, each warp looping over its tiles
+    static std::atomic<int> resident{0};
+    int nres = resident.load();
+    if (nres == 0) {
+        int dev = 0, sms = 0, occ = 0;
+        DD_CUDA(cudaGetDevice(&dev));
+        DD_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        DD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_les_mlp<GT, TT>, 32 * LES_WARPS, 0));
+        nres = sms * (occ > 0 ? occ : 1);
+        resident.store(nres);
+    }
+    const int64_t need = (npts + 16 * LES_WARPS - 1) / (16 * LES_WARPS);
+    const unsigned nb = (unsigned)(need < nres ? (need < 1 ? 1 : need) : nres);
     DD_KT("les_mlp", st,
-          k_les_mlp<<<nb, 32 * LES_WARPS, sizeof(LesMlpSmem), st>>>(gx, t, npts, (const bf16*)cl->wbf16, cl->params,
-                                                                     cl->norm, cl->delta));
+          (k_les_mlp<GT, TT><<<nb, 32 * LES_WARPS, 0, st>>>(gx, t, npts, (const bf16*)cl->wbf16, cl->params, cl->norm,
+                                                            cl->delta)));
     DD_LAUNCH_CHECK();
     return DD_OK;
 }
@@ -369,14 +461,19 @@ int les_closure_add(const dd_plan* p, const LesHook& h, int prec, bool compact, 
                     void* const* nc, cudaStream_t st) {
     DD_CHECK_ARG(h.wb >= les_work_bytes(p), "closure workspace too small");
     const LesWork w = les_carve(p, h.work);
-    DD_TRY(les_grads(p, prec, compact, y, w, st));
-    DD_TRY(les_mlp(p, h.cl, w, w.gx, st));      // stresses overwrite gradients 0..5
-    const double* xin[6];
+    const bool f32 = prec == DD_FP32;
+    DD_TRY(les_grads(p, prec, compact, y, w, f32, st));
+    // the stresses overwrite gradients 0..5; k_les_add reads the kept modes
+    // only, so the forward transform leaves the rest unwritten
     void* kout[6];
-    for (int c = 0; c < 6; c++) { xin[c] = w.gx[c]; kout[c] = w.gk[c]; }
-    // k_les_add reads the kept modes only: no zeroing of the rest
-    if (prec == DD_FP32) DD_TRY(fft_r2c<float>(p, 6, xin, kout, w.fw, w.fwb, st, false));
-    else DD_TRY(fft_r2c<double>(p, 6, xin, kout, w.fw, w.fwb, st, false));
+    for (int c = 0; c < 6; c++) kout[c] = w.gk[c];
+    if (f32) {
+        DD_TRY((les_mlp<float, float>(p, h.cl, w.gxf, w.gxf, st)));
+        DD_TRY((fft_r2c<float, float>(p, 6, w.gxf, kout, w.fw, w.fwb, st, false)));
+    } else {
+        DD_TRY((les_mlp<double, double>(p, h.cl, w.gx, w.gx, st)));
+        DD_TRY(fft_r2c<double>(p, 6, w.gx, kout, w.fw, w.fwb, st, false));
+    }
     const Geo3& g = p->g3;
     CPtrs tk{};
     Ptrs n{};
@@ -465,7 +562,7 @@ int dd_les_gradients(const dd_plan* p, const void* const* u, double* const* gx, 
     for (int f = 0; f < 9; f++) DD_CHECK_ARG(gx[f], "null gradient %d", f);
     cudaStream_t st = (cudaStream_t)stream;
     const LesWork w = les_carve(p, work);
-    DD_TRY(les_grads(p, precision, false, u, w, st));
+    DD_TRY(les_grads(p, precision, false, u, w, false, st));
     const int64_t xb = p->g3.xcount() * (int64_t)sizeof(double);
     for (int f = 0; f < 9; f++) DD_CUDA(cudaMemcpyAsync(gx[f], w.gx[f], xb, cudaMemcpyDeviceToDevice, st));
     return DD_OK;
@@ -494,8 +591,10 @@ int dd_les_stress(const dd_plan* p, const void* const* u, double* const* tau, co
     for (int c = 0; c < 6; c++) DD_CHECK_ARG(tau[c], "null stress %d", c);
     cudaStream_t st = (cudaStream_t)stream;
     const LesWork w = les_carve(p, work);
-    DD_TRY(les_grads(p, precision, false, u, w, st));
-    return les_mlp(p, cl, w, tau, st);
+    const bool f32 = precision == DD_FP32;
+    DD_TRY(les_grads(p, precision, false, u, w, f32, st));
+    if (f32) return les_mlp<float, double>(p, cl, w.gxf, tau, st);
+    return les_mlp<double, double>(p, cl, w.gx, tau, st);
 }
 
 int dd_les_transfer(const dd_plan* p, const void* const* u, const double* const* tau, int nbins, double* out,

@@ -184,9 +184,9 @@ def test_truncation_copies_kept_modes(dd, cuda):
         assert np.array_equal(out[a].cpu().numpy(), OC.truncate(u[a], dns, les))
 
 
-def _les_pair(dd, shape, closure, u):
+def _les_pair(dd, shape, closure, u, precision=None):
     M = dd.mods
-    R = M.LESHydro(shape, M.FourierRepresentation, closure=closure)
+    R = M.LESHydro(shape, M.FourierRepresentation, closure=closure, precision=precision)
     R.parameters['nu'] = 5e-3
     d = R.create_fields(0.)
     for i in range(3):
@@ -268,6 +268,52 @@ def test_les_transfer_matches_oracle(dd, cuda, shape):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("shape,precision", [((16, 16, 16), "fp64"), ((32, 32, 32), "fp32"),
+                                             ((24, 16, 32), "fp32"), ((32, 32, 32), "fp64")])
+def test_grid_point_network_equals_mlp_infer(dd, cuda, shape, precision):
+    """The closure network at the grid points (dd_les_stress: each lane loads
+    its inputs into the MMA fragments, activations stay in registers) against
+    dd_mlp_infer (shared-memory tiles) on the same normalised BF16 inputs,
+    rebuilt here from dd_les_gradients with the kernel's float arithmetic:
+    the network outputs agree bitwise, so the stresses agree to the one
+    rounding of the final float multiply-add (1 ulp)."""
+    import torch
+    C = dd.closure
+    u = dd.init_cond.turbulence_3d(shape, seed=41)
+    delta = np.pi / (np.ceil(shape[0] / 3) - 1)
+    c = _closure(dd, _params(6), delta)
+    c.set_norm(*_norm_for(dd, shape, u, delta))
+    prec = dd._lib.DD_FP32 if precision == "fp32" else dd._lib.DD_FP64
+    plan = dd.engine.get_plan(shape, (2 * np.pi,) * 3)
+    n = ctypes.c_size_t()
+    dd._lib.call("dd_les_workspace_size", plan.handle, prec, ctypes.byref(n))
+    ws = torch.empty(n.value, dtype=torch.uint8, device="cuda")
+    ud = [_dev(x) for x in u]
+    g = [torch.empty(shape, dtype=torch.float64, device="cuda") for _ in range(9)]
+    tau = [torch.empty(shape, dtype=torch.float64, device="cuda") for _ in range(6)]
+    up, _a = C._ptrs(ud)
+    gp, _b = C._ptrs(g)
+    tp, _c = C._ptrs(tau)
+    st = dd.engine.current_stream()
+    dd._lib.call("dd_les_gradients", plan.handle, up, gp, prec, dd.engine.dptr(ws), ws.numel(), st)
+    cl = c.struct()
+    dd._lib.call("dd_les_stress", plan.handle, up, tp, ctypes.byref(cl), prec, dd.engine.dptr(ws), ws.numel(), st)
+    nv = c.norm.cpu().numpy()
+    in_mean, in_scale, out_mean, out_scale = nv[0:16], nv[16:32], nv[32:40], nv[40:48]
+    npts = int(np.prod(shape))
+    X = np.zeros((npts, 16), dtype=np.float32)
+    for f in range(9):
+        X[:, f] = (g[f].cpu().numpy().ravel().astype(np.float32) - in_mean[f]) * in_scale[f]
+    X[:, 9] = (np.float32(delta) - in_mean[9]) * in_scale[9]
+    Y = c.predict(torch.from_numpy(X).cuda().to(torch.bfloat16)).cpu().numpy()
+    for k in range(6):
+        exp = (Y[:, k].astype(np.float64) * out_scale[k] + out_mean[k]).astype(np.float32)
+        got = tau[k].cpu().numpy().ravel()
+        assert np.array_equal(got, got.astype(np.float32).astype(np.float64)), "stress is not a float value"
+        assert np.all(np.abs(got - exp) <= np.spacing(np.abs(exp))), k
+
+
+@pytest.mark.gpu
 def test_shell_table_survives_save_and_load(dd, cuda, tmp_path):
     c = _closure(dd, _params(9), 0.15).with_shells(_SHELLS)
     path = str(tmp_path / "c.npz")
@@ -324,18 +370,19 @@ def test_fused_les_step_matches_generic_rk4(dd, cuda):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("fused", [True, False])
-def test_les_rk4_step_matches_oracle(dd, cuda, fused):
+@pytest.mark.parametrize("fused,precision", [(True, None), (False, None), (True, "fp32")])
+def test_les_rk4_step_matches_oracle(dd, cuda, fused, precision):
     """One RK4 step of the closed LES (fused C-ABI step and the generic
-    integrator over dd_les_rhs3d) against the oracle's RK4 over the oracle
-    RHS + closure term: the step increments agree to 1e-3 relative L2."""
+    integrator over dd_les_rhs3d; FP64, and the FP32 path whose gradients and
+    stresses are float grid-point fields) against the oracle's RK4 over the
+    oracle RHS + closure term: the step increments agree to 1e-3 relative L2."""
     from oracle import time_step as OT
     shape = (32, 32, 32)
     u = dd.init_cond.turbulence_3d(shape, seed=24)
     delta = np.pi / 10
     c = _closure(dd, _params(6), delta)
     c.set_norm(*_norm_for(dd, shape, u, delta))
-    R, d = _les_pair(dd, shape, c, u)
+    R, d = _les_pair(dd, shape, c, u, precision)
     ti = dd.mods.RK4(R)
     ti.use_fused = fused
     ti.do_advance(d, 2e-3)
