@@ -81,7 +81,7 @@ TRAFFIC = {
         4 * (67.81e6 + 50.79e6),
         "ncu capture of the same kernel on 128x128x256 FP64 (67.81 MB read + 50.79 MB written), x4 rows for 256^3"),
     ("les64-closure", "les_mlp"): (
-        18.92e6 + 0.0, "ncu capture at full size (18.92 MB read, stresses still in L2 at kernel end)"),
+        9.48e6 + 0.0, "ncu capture at full size (9.48 MB read, stresses still in L2 at kernel end)"),
 }
 
 
