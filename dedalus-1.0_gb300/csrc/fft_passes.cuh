@@ -37,6 +37,43 @@ __device__ __forceinline__ void pass_fft(const Op& op, C<T>* tile, const C<T>* t
     pencil_fft_s<T, S, INV, false>(tile, tw);
 }
 
+// Global -> tile: the P pencils of L elements starting at pencil f0, pencils
+// beyond npen zero.  Each thread loads its elements in groups of G into
+// registers before storing any of the group to shared memory, so a group's
+// global loads are in flight together (element-by-element load / store keeps
+// one load in flight per thread: the shared stores may not move above the
+// loads of generic pointers).
+template <typename T, int L, int P, int PS, int NT, bool LD_E, class Op>
+__device__ __forceinline__ void load_tile(const Op& op, C<T>* tile, int fld, int s, int f0, int npen) {
+    constexpr int N = L * P;
+    constexpr int NPT = (N + NT - 1) / NT;
+    constexpr int GB = (int)(128 / sizeof(C<T>));   // 128 bytes of loads per thread in flight
+    constexpr int G = NPT < GB ? NPT : GB;
+#pragma unroll
+    for (int i0 = 0; i0 < NPT; i0 += G) {
+        C<T> v[G];
+#pragma unroll
+        for (int i = 0; i < G; i++) {
+            const int idx = threadIdx.x + (i0 + i) * NT;
+            v[i] = zero<T>();
+            if (i0 + i < NPT && (N % NT == 0 || idx < N)) {
+                const int e = LD_E ? idx % L : idx / P;
+                const int p = LD_E ? idx / L : idx % P;
+                if (f0 + p < npen) v[i] = op.load(fld, s, e, f0 + p);
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < G; i++) {
+            const int idx = threadIdx.x + (i0 + i) * NT;
+            if (i0 + i < NPT && (N % NT == 0 || idx < N)) {
+                const int e = LD_E ? idx % L : idx / P;
+                const int p = LD_E ? idx / L : idx % P;
+                tile[e * PS + p] = v[i];
+            }
+        }
+    }
+}
+
 template <typename T, int L, bool INV, bool LD_E, bool ST_E, class Op>
 __global__ void __launch_bounds__(FFTCfg<L>::NT) k_pass(const Op op, int nfield) {
     extern __shared__ __align__(16) unsigned char dd_smem[];
@@ -48,12 +85,7 @@ __global__ void __launch_bounds__(FFTCfg<L>::NT) k_pass(const Op op, int nfield)
     const int f0 = (blockIdx.x / nfield) * P;
     const int s = blockIdx.y + 65535 * blockIdx.z;
     const int npen = op.npencil();
-    for (int idx = threadIdx.x; idx < L * P; idx += NT) {
-        const int e = LD_E ? idx % L : idx / P;
-        const int p = LD_E ? idx / L : idx % P;
-        const int f = f0 + p;
-        tile[e * PS + p] = (f < npen) ? op.load(fld, s, e, f) : zero<T>();
-    }
+    load_tile<T, L, P, PS, NT, LD_E>(op, tile, fld, s, f0, npen);
     __syncthreads();
     pass_fft<T, DefSched<L>, INV>(op, tile, tw);
     const int nst = op.nstore();
@@ -99,12 +131,7 @@ __global__ void __launch_bounds__(S::NT) k_pass_sched(const Op op, int nfield) {
     const int f0 = (blockIdx.x / nfield) * P;
     const int s = blockIdx.y + 65535 * blockIdx.z;
     const int npen = op.npencil();
-    for (int idx = threadIdx.x; idx < L * P; idx += NT) {
-        const int e = LD_E ? idx % L : idx / P;
-        const int p = LD_E ? idx / L : idx % P;
-        const int f = f0 + p;
-        tile[e * PS + p] = (f < npen) ? op.load(fld, s, e, f) : zero<T>();
-    }
+    load_tile<T, L, P, PS, NT, LD_E>(op, tile, fld, s, f0, npen);
     __syncthreads();
     pass_fft<T, S, INV>(op, tile, tw);
     const int nst = op.nstore();

@@ -117,22 +117,37 @@ k_x_prod(int nrows, int Kx, CPtrs win, Ptrs wout, int64_t in_rs, int64_t out_rs,
     const int nr = min(Q, nrows - row0);
     const int64_t ib = blockIdx.y * in_rs, ob = blockIdx.y * out_rs;  // run (batch) offsets
     constexpr int NPI = (NI * Q + 1) / 2;  // inverse pencils in use
-    for (int idx = threadIdx.x; idx < L * SI::P; idx += NT) {
-        const int e = idx % L, pj = idx / L;
-        C<T> z = zero<T>();
-        if (pj < NPI) {
-            const int ta = 2 * pj, tb = 2 * pj + 1;
-            const int ra = ta / NI, fa = ta % NI, rb = tb / NI, fb = tb % NI;
-            const bool va = ra < nr, vb = tb < NI * Q && rb < nr;
-            if (va || vb) {
-                const V* pa = (const V*)pick_ptr<NI>(win.p, fa) + ib + (int64_t)(row0 + (va ? ra : rb)) * Kx;
-                const V* pb = (const V*)pick_ptr<NI>(win.p, vb ? fb : fa) + ib + (int64_t)(row0 + (vb ? rb : ra)) * Kx;
-                z = pack_rows<T>(pa, pb, e, L, Kx);
-                if (!va) z.x = T(0);
-                if (!vb) z.y = T(0);
+    // the loads of a group of GX entries are in flight together (see load_tile)
+    constexpr int NLD = L * SI::P, NPL = (NLD + NT - 1) / NT;
+    constexpr int GX0 = (int)(128 / sizeof(C<T>)), GX = NPL < GX0 ? NPL : GX0;
+#pragma unroll
+    for (int i0 = 0; i0 < NPL; i0 += GX) {
+        C<T> zv[GX];
+#pragma unroll
+        for (int i = 0; i < GX; i++) {
+            const int idx = threadIdx.x + (i0 + i) * NT;
+            const int e = idx % L, pj = idx / L;
+            C<T> z = zero<T>();
+            if (i0 + i < NPL && idx < NLD && pj < NPI) {
+                const int ta = 2 * pj, tb = 2 * pj + 1;
+                const int ra = ta / NI, fa = ta % NI, rb = tb / NI, fb = tb % NI;
+                const bool va = ra < nr, vb = tb < NI * Q && rb < nr;
+                if (va || vb) {
+                    const V* pa = (const V*)pick_ptr<NI>(win.p, fa) + ib + (int64_t)(row0 + (va ? ra : rb)) * Kx;
+                    const V* pb =
+                        (const V*)pick_ptr<NI>(win.p, vb ? fb : fa) + ib + (int64_t)(row0 + (vb ? rb : ra)) * Kx;
+                    z = pack_rows<T>(pa, pb, e, L, Kx);
+                    if (!va) z.x = T(0);
+                    if (!vb) z.y = T(0);
+                }
             }
+            zv[i] = z;
         }
-        tile[e * PSI + pj] = z;
+#pragma unroll
+        for (int i = 0; i < GX; i++) {
+            const int idx = threadIdx.x + (i0 + i) * NT;
+            if (i0 + i < NPL && idx < NLD) tile[(idx % L) * PSI + idx / L] = zv[i];
+        }
     }
     __syncthreads();
     // kept kx <= Kx - 1: under the 2/3 rule the packed pencils are zero in the
