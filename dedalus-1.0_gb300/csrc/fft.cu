@@ -93,6 +93,16 @@ static int upload_doubles(const double* h, int n, double** d) {
     return DD_OK;
 }
 
+// a wavenumber table as double and as float (rounded to nearest)
+static int upload_k(const double* h, int n, double** d, float** f) {
+    DD_TRY(upload_doubles(h, n, d));
+    std::vector<float> hf(n > 0 ? n : 1, 0.f);
+    for (int i = 0; i < n; i++) hf[i] = (float)h[i];
+    DD_CUDA(cudaMalloc((void**)f, sizeof(float) * hf.size()));
+    DD_CUDA(cudaMemcpy(*f, hf.data(), sizeof(float) * hf.size(), cudaMemcpyHostToDevice));
+    return DD_OK;
+}
+
 DD_FFT_INSTANTIATE(extern, double)
 DD_FFT_INSTANTIATE(extern, float)
 
@@ -135,8 +145,8 @@ int dd_plan_create(int ndim, const int64_t* xshape, const double* kx, const doub
         g.Mx = mx; g.My = my; g.Mz = mz;
         g.Kx = mx + 1; g.Ky = 2 * my + 1; g.Kz = 2 * mz + 1;
         p->inv_n = 1.0 / ((double)Nx * Ny * Nz);
-        if ((rc = upload_doubles(kx, Nh, &p->kx)) || (rc = upload_doubles(ky, Ny, &p->ky)) ||
-            (rc = upload_doubles(kz, Nz, &p->kz)))
+        if ((rc = upload_k(kx, Nh, &p->kx, &p->kxf)) || (rc = upload_k(ky, Ny, &p->ky, &p->kyf)) ||
+            (rc = upload_k(kz, Nz, &p->kz, &p->kzf)))
             return fail(rc);
     } else {
         Geo2& g = p->g2;
@@ -144,7 +154,7 @@ int dd_plan_create(int ndim, const int64_t* xshape, const double* kx, const doub
         g.Mx = mx; g.My = my;
         g.Kx = mx + 1; g.Ky = 2 * my + 1;
         p->inv_n = 1.0 / ((double)Nx * Ny);
-        if ((rc = upload_doubles(kx, Nh, &p->kx)) || (rc = upload_doubles(ky, Ny, &p->ky))) return fail(rc);
+        if ((rc = upload_k(kx, Nh, &p->kx, &p->kxf)) || (rc = upload_k(ky, Ny, &p->ky, &p->kyf))) return fail(rc);
     }
     if ((rc = upload_twiddles(Nx, &p->tw64_x, &p->tw32_x, &p->twdf_x)) ||
         (rc = upload_twiddles(Ny, &p->tw64_y, &p->tw32_y, &p->twdf_y)))
@@ -156,7 +166,7 @@ int dd_plan_create(int ndim, const int64_t* xshape, const double* kx, const doub
 
 int dd_plan_destroy(dd_plan* p) {
     if (!p) return DD_OK;
-    void* bufs[] = {p->kx, p->ky, p->kz, p->tw64_x, p->tw64_y, p->tw64_z, p->tw32_x, p->tw32_y, p->tw32_z,
+    void* bufs[] = {p->kx, p->ky, p->kz, p->kxf, p->kyf, p->kzf, p->tw64_x, p->tw64_y, p->tw64_z, p->tw32_x, p->tw32_y, p->tw32_z,
                     p->twdf_x, p->twdf_y, p->twdf_z};
     for (void* b : bufs)
         if (b) cudaFree(b);

@@ -1,9 +1,10 @@
 // Batched shared-memory FFT engine.
 //
 // A thread block holds P pencils of length L in a shared-memory tile laid out
-// [element][pencil] (pencil fastest, row stride PS >= P, PS odd so that both
-// pencil-contiguous and element-contiguous accesses are bank-conflict free
-// for 8- and 16-byte complex entries).  The transform is a mixed-radix
+// [element][pencil] (pencil fastest; row stride PS >= P, by default odd, so
+// that for tiles of 16 or more pencils both pencil-contiguous and
+// element-contiguous accesses are bank-conflict free for 8- and 16-byte
+// complex entries; narrower tiles may use a skewed row layout, see Sched).  The transform is a mixed-radix
 // Stockham autosort (decimation in time): each pass reads R inputs at stride
 // L/R, twiddles by W_{Ns R}^{r k}, does an in-register radix-R DFT and writes
 // the outputs at ((j-k) R + k) + r Ns.  Radices are 2, 3, 4, 8 and 16 (a radix
@@ -383,16 +384,26 @@ template <> struct FFTCfg<512>  { static constexpr int P = 8,  NT = 256, R1 = 8,
 template <> struct FFTCfg<1024> { static constexpr int P = 4,  NT = 256, R1 = 16, R2 = 16, R3 = 4; };
 
 // A schedule: length L, P pencils per tile, NT threads (TPP = NT / P per
-// pencil) and the radix sequence R1 R2 R3 (1 = unused).
-template <int L_, int P_, int NT_, int R1_, int R2_, int R3_>
+// pencil) and the radix sequence R1 R2 R3 (1 = unused).  Row e of the tile
+// starts at entry off(e) = e PS + (e / 8) SKD.  The default is PS = P | 1 and
+// no skew.  A schedule with few pencils (6, 10) may take PS = P and a skew of
+// SKD entries every 8 rows instead.  That keeps the pencil-contiguous Stockham
+// accesses (a half-warp spanning 2-3 rows) and the element-contiguous ones
+// (16 consecutive rows of one pencil) largely free of bank conflicts for 8-byte
+// entries, which no odd stride does for both.
+template <int L_, int P_, int NT_, int R1_, int R2_, int R3_, int PS_ = (P_ | 1), int SKD_ = 0>
 struct Sched {
     static constexpr int L = L_, P = P_, NT = NT_, R1 = R1_, R2 = R2_, R3 = R3_;
-    static constexpr int PS = P | 1;   // odd row stride (complex entries), >= P
+    static constexpr int PS = PS_, SKD = SKD_;
     static constexpr int TPP = NT / P;
+    static_assert(PS >= P, "row stride below the pencil count");
     static_assert(NT % P == 0, "threads must split evenly over pencils");
     static_assert(R1 * R2 * R3 == L, "radix schedule does not multiply to L");
+    __host__ __device__ static constexpr int off(int e) { return e * PS + (e >> 3) * SKD; }
+    // tile entries (the twiddle table follows them)
+    static constexpr int span = SKD == 0 ? L * PS : off(L - 1) + P;
     template <typename T>
-    static constexpr size_t smem_bytes() { return sizeof(C<T>) * ((size_t)L * PS + L); }
+    static constexpr size_t smem_bytes() { return sizeof(C<T>) * ((size_t)span + L); }
 };
 
 template <int L>
@@ -413,7 +424,7 @@ struct Pencil {
 // double-float.
 template <typename T, class S, int R, int NS, bool INV, unsigned ZIN = 0u, unsigned ZOUT = 0u>
 __device__ __forceinline__ void stockham_pass(C<T>* tile, const C<T>* tw, int p, int jt) {
-    constexpr int L = S::L, PS = S::PS, TPP = S::TPP;
+    constexpr int L = S::L, TPP = S::TPP;
     constexpr int NB = L / R;          // butterflies per pencil
     constexpr int BPT = NB / TPP;      // butterflies per thread
     static_assert(BPT >= 1 && NB % TPP == 0, "bad radix schedule");
@@ -422,7 +433,7 @@ __device__ __forceinline__ void stockham_pass(C<T>* tile, const C<T>* tw, int p,
     for (int b = 0; b < BPT; b++) {
         const int j = jt + TPP * b;
 #pragma unroll
-        for (int r = 0; r < R; r++) v[b][r] = ((ZIN >> r) & 1u) ? zero<T>() : tile[(j + r * NB) * PS + p];
+        for (int r = 0; r < R; r++) v[b][r] = ((ZIN >> r) & 1u) ? zero<T>() : tile[S::off(j + r * NB) + p];
     }
     __syncthreads();
 #pragma unroll
@@ -445,7 +456,7 @@ __device__ __forceinline__ void stockham_pass(C<T>* tile, const C<T>* tw, int p,
         const int d = (j - k) * R + k;
 #pragma unroll
         for (int r = 0; r < R; r++)
-            if (!((ZOUT >> r) & 1u)) tile[(d + r * NS) * PS + p] = v[b][r];
+            if (!((ZOUT >> r) & 1u)) tile[S::off(d + r * NS) + p] = v[b][r];
     }
     __syncthreads();
 }

@@ -257,14 +257,18 @@ __device__ __forceinline__ C<T> pack_rows(const V* ra, const V* rb, int e, int N
 }
 
 // Separation of the forward DFT Z of a + ib into the half spectra A (a), B (b)
-// at bin k, times s.
+// at bin k, times s, from z = Z[k] and zn = Z[N - k] (Z[0] at k = 0).
 template <typename T>
-__device__ __forceinline__ void unpack_rows(const C<T>* col, int PS, int k, int N, T s, C<T>& A, C<T>& B) {
-    const C<T> z = col[k * PS];
-    const C<T> zn = col[(k == 0 ? 0 : N - k) * PS];
+__device__ __forceinline__ void unpack_pair(C<T> z, C<T> zn, T s, C<T>& A, C<T>& B) {
     const T h = T(0.5) * s;
     A = mk<T>((z.x + zn.x) * h, (z.y - zn.y) * h);
     B = mk<T>((z.y + zn.y) * h, (zn.x - z.x) * h);
+}
+
+// The same with Z read from a tile column of row stride PS.
+template <typename T>
+__device__ __forceinline__ void unpack_rows(const C<T>* col, int PS, int k, int N, T s, C<T>& A, C<T>& B) {
+    unpack_pair<T>(col[k * PS], col[(k == 0 ? 0 : N - k) * PS], s, A, B);
 }
 
 // c2r along x: W2 rows [r][kxc] (r = z*Ny + y) -> x rows; pencil f = row pair.

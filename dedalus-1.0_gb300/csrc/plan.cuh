@@ -13,6 +13,10 @@ struct dd_plan {
     double* kx;
     double* ky;
     double* kz;
+    // the same tables rounded to float (FP32 stage arithmetic)
+    float* kxf;
+    float* kyf;
+    float* kzf;
     // twiddle tables W_L^m, m < L, per axis length (device): fp64 and fp32 as
     // (g, t) with W = g (1 + i t) for the FMA butterflies, double-float as (cos, sin)
     double2* tw64_x; double2* tw64_y; double2* tw64_z;

@@ -18,6 +18,7 @@ struct ProjArgs {
     const double* kx; const double* ky; const double* kz;
     const double* inv_k2;   // 1/k2 per integer q (q = 0 -> 1), or null
     int intk;               // wavenumbers are integers (q tables valid)
+    const float* kxf = nullptr; const float* kyf = nullptr; const float* kzf = nullptr;   // float copies
 };
 
 __device__ __forceinline__ void kept_index(const Geo3& g, int64_t i, int& kyc, int& kzc, int& ix) {
@@ -219,15 +220,25 @@ __global__ void k_rk4_stage3_lo(RK4Args a) {
     const Geo3& g = a.pa.g;
     constexpr int NF = Phys3<PH>::NF, NG = Phys3<PH>::NG;
     const int n = g.Ky * g.Kz * g.Kx;      // < 2^31 for every supported grid
+    // integer wavenumbers with their q tables: k^2 is an integer below 2^24,
+    // exact in float, and the phi values come from the tables
+    const bool tabs = a.pa.intk && a.pa.inv_k2 && a.tab[0] && (NG == 1 || a.tab[1]);
+    const float w = (float)a.w, hf = (float)a.h;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int ix = i % g.Kx, r = i / g.Kx;
         const int kzc = r % g.Kz, kyc = r / g.Kz;
         const int ky_i = compact_to_full(kyc, g.Ny, g.Ky), kz_i = compact_to_full(kzc, g.Nz, g.Kz);
-        const double kxd = a.pa.kx[ix], kyd = a.pa.ky[ky_i], kzd = a.pa.kz[kz_i];
-        const double k2 = k2_of(a.pa, ix, ky_i, kz_i);
-        int q;
-        const float s = (float)inv_k2_of(a.pa, k2, q);
-        const float kx = (float)kxd, ky = (float)kyd, kz = (float)kzd;
+        const float kx = a.pa.kxf[ix], ky = a.pa.kyf[ky_i], kz = a.pa.kzf[kz_i];
+        int q = 0;
+        double k2 = 0.;
+        float s;
+        if (tabs) {
+            q = (int)((ky * ky + kz * kz) + kx * kx);
+            s = (float)a.pa.inv_k2[q];
+        } else {
+            k2 = k2_of(a.pa, ix, ky_i, kz_i);
+            s = (float)inv_k2_of(a.pa, k2, q);
+        }
         const float2* P[8];
 #pragma unroll
         for (int c = 0; c < Phys3<PH>::NO; c++) P[c] = (const float2*)a.nc.p[c];
@@ -252,31 +263,50 @@ __global__ void k_rk4_stage3_lo(RK4Args a) {
             k[4] = make_float2(a1.x - b1.x, a1.y - b1.y);
             k[5] = make_float2(a2.x - b2.x, a2.y - b2.y);
         }
-        double f0[NG], f1h[NG];
+        double f0[NG], f1[NG];
 #pragma unroll
         for (int grp = 0; grp < NG; grp++) {
-            double Z, f1;
-            phis_for(a, grp, q, k2, Z, f0[grp], f1);
-            f1h[grp] = f1 * a.h;
+            if (tabs) {
+                const double* t = reinterpret_cast<const double*>(a.tab[grp] + q);
+                f0[grp] = t[1];
+                f1[grp] = t[2];
+            } else {
+                double Z;
+                phis_for(a, grp, q, k2, Z, f0[grp], f1[grp]);
+            }
         }
         const int64_t o = ((int64_t)ky_i * g.Nz + kz_i) * g.Nh + ix;
-        const float w = (float)a.w;
+        if (a.stage < 4) {
+            // stages 1-3: the accumulated increment and the next stage state,
+            // both float, in float arithmetic: ys = f0 y + h phi1 N
+            float f0f[NG], f1hf[NG];
 #pragma unroll
-        for (int c = 0; c < NF; c++) {
-            const int grp = c / 3;
-            float2 t;
-            if (a.stage == 1) t = make_float2(k[c].x * w, k[c].y * w);
-            else {
-                t = ((const float2*)a.tot.p[c])[i];
-                t = make_float2(fmaf(k[c].x, w, t.x), fmaf(k[c].y, w, t.y));
-            }
-            const double2 y0 = ((const double2*)a.y.p[c])[o];
-            if (a.stage < 4) {
+            for (int grp = 0; grp < NG; grp++) { f0f[grp] = (float)f0[grp]; f1hf[grp] = (float)f1[grp] * hf; }
+#pragma unroll
+            for (int c = 0; c < NF; c++) {
+                const int grp = c / 3;
+                float2 t;
+                if (a.stage == 1) t = make_float2(k[c].x * w, k[c].y * w);
+                else {
+                    t = ((const float2*)a.tot.p[c])[i];
+                    t = make_float2(fmaf(k[c].x, w, t.x), fmaf(k[c].y, w, t.y));
+                }
                 ((float2*)a.tot.p[c])[i] = t;
-                const double2 ys = etd1_fma(y0, make_double2((double)k[c].x, (double)k[c].y), f0[grp], f1h[grp]);
-                ((float2*)a.ys.p[c])[i] = make_float2((float)ys.x, (float)ys.y);
-            } else {
-                ((double2*)a.y.p[c])[o] = etd1_fma(y0, make_double2((double)t.x, (double)t.y), f0[grp], f1h[grp]);
+                const double2 y0 = ((const double2*)a.y.p[c])[o];
+                const float yr = (float)y0.x, yi = (float)y0.y;
+                ((float2*)a.ys.p[c])[i] =
+                    make_float2(fmaf(f1hf[grp], k[c].x, yr * f0f[grp]), fmaf(f1hf[grp], k[c].y, yi * f0f[grp]));
+            }
+        } else {
+            // stage 4: the FP64 state update y = f0 y + h phi1 (sum of the weighted N)
+#pragma unroll
+            for (int c = 0; c < NF; c++) {
+                const int grp = c / 3;
+                float2 t = ((const float2*)a.tot.p[c])[i];
+                t = make_float2(fmaf(k[c].x, w, t.x), fmaf(k[c].y, w, t.y));
+                const double2 y0 = ((const double2*)a.y.p[c])[o];
+                ((double2*)a.y.p[c])[o] =
+                    etd1_fma(y0, make_double2((double)t.x, (double)t.y), f0[grp], f1[grp] * a.h);
             }
         }
     }
@@ -460,7 +490,7 @@ static int rk4_3(const dd_plan* p, const double* params, void* const* u, const d
     const double inv_fpr = p3_mhd(PH) ? inv_fpr_of(params) : 0.;
     Work3 w = make_work<PH>(g, work);
     RK4Args a{};
-    a.pa = ProjArgs{g, p->kx, p->ky, p->kz, inv_k2, intk};
+    a.pa = ProjArgs{g, p->kx, p->ky, p->kz, inv_k2, intk, p->kxf, p->kyf, p->kzf};
     a.vo = vo;
     for (int grp = 0; grp < P::NG; grp++) a.coeff[grp] = coeff[grp];
     const void* ysc[6] = {};

@@ -76,24 +76,42 @@ template <> struct ProdCfg<512, 12, 6> {
     static constexpr int Q = 2, NT = 384;
 };
 
-// The schedule a precision runs (ProdCfg for all three; the indirection is
-// where a precision would get its own tiles).  FP32 tiles of 16 pencils per
-// row (conflict-free 8-byte shared-memory access) were measured on the 256-point
-// hydro pass in divergence form and lost: bank conflicts 42% -> 4% of the
-// wavefronts, but 314 -> 330 us per launch, the idle pencil slots of a 16-wide
-// tile for 9 inverse pencils costing more than the conflicts.
+// The schedule a precision runs (ProdCfg unless specialised).  per_point:
+// the product phase gives each thread one grid point of all Q rows, moving
+// whole complex entries through shared memory (otherwise each thread takes
+// one point of one row and reads and writes the real and imaginary halves
+// separately).
 template <typename T, int L, int NI, int NO>
-struct ProdCfgT : ProdCfg<L, NI, NO> {};
+struct ProdCfgT : ProdCfg<L, NI, NO> {
+    static constexpr bool per_point = false;
+    static constexpr int min_blocks = std::is_same<T, df64>::value ? 5 : 1;   // __launch_bounds__
+};
+// FP32 hydro in divergence form on 256-point rows: 6 inverse and 10 forward
+// pencils in tiles with unpadded rows and a skew every 8 rows (P / 2 entries),
+// and the per-point product phase.  With the odd strides 7 and 11, 41% of the
+// shared-memory wavefronts of a launch were bank conflicts (23.3 M of 57.2 M);
+// a model of every access of the kernel puts this layout at 37% fewer
+// wavefronts.  (Tiles 16 pencils wide, 9 inverse and 15 forward pencils per
+// 6 rows, cut the conflicts to 4% but ran slower: their idle pencil slots cost
+// more than the conflicts.)
+template <>
+struct ProdCfgT<float, 256, 3, 5> {
+    using SI = Sched<256, 6, 192, 8, 8, 4, 6, 3>;
+    using SF = Sched<256, 10, 160, 16, 16, 1, 10, 5>;
+    static constexpr int Q = 4, NT = 192;
+    static constexpr bool per_point = true;
+    static constexpr int min_blocks = 6;   // 56 registers: 6 blocks per SM (72 and 4 blocks without the bound)
+};
 
 template <typename T, int L, int NI, int NO>
 constexpr size_t prod_smem(size_t csize) {
     using CC = ProdCfgT<T, L, NI, NO>;
-    const size_t a = (size_t)L * CC::SI::PS, b = (size_t)L * CC::SF::PS;
+    const size_t a = (size_t)CC::SI::span, b = (size_t)CC::SF::span;
     return csize * ((a > b ? a : b) + L);
 }
 
 template <typename T, int L, class Op>
-__global__ void __launch_bounds__(ProdCfgT<T, L, Op::NI, Op::NO>::NT, std::is_same<T, df64>::value ? 5 : 1)
+__global__ void __launch_bounds__(ProdCfgT<T, L, Op::NI, Op::NO>::NT, ProdCfgT<T, L, Op::NI, Op::NO>::min_blocks)
 k_x_prod(int nrows, int Kx, CPtrs win, Ptrs wout, int64_t in_rs, int64_t out_rs,
          const typename Vec2<T>::type* gtw, T scale, const Op op) {
     using V = typename Vec2<T>::type;
@@ -104,13 +122,11 @@ k_x_prod(int nrows, int Kx, CPtrs win, Ptrs wout, int64_t in_rs, int64_t out_rs,
     using SF = typename CC::SF;
     extern __shared__ __align__(16) unsigned char dd_smem[];
     constexpr int NT = CC::NT, Q = CC::Q;
-    constexpr int PSI = SI::PS, PSF = SF::PS;
-    constexpr int NPT = (L * Q + NT - 1) / NT;
     static_assert(Q >= 2 && Q % 2 == 0, "need an even number of rows per block");
     static_assert((NI * Q + 1) / 2 <= SI::P && (NO * Q + 1) / 2 <= SF::P, "schedule too small for Q rows");
     static_assert(SI::NT == NT && SF::NT <= NT, "schedules must fit the block");
     C<T>* tile = reinterpret_cast<C<T>*>(dd_smem);
-    constexpr size_t TA = (size_t)L * PSI, TB = (size_t)L * PSF;
+    constexpr size_t TA = (size_t)SI::span, TB = (size_t)SF::span;
     C<T>* tw = tile + (TA > TB ? TA : TB);
     load_twiddles<T, L>(tw, gtw);
     const int row0 = blockIdx.x * Q;
@@ -146,7 +162,7 @@ k_x_prod(int nrows, int Kx, CPtrs win, Ptrs wout, int64_t in_rs, int64_t out_rs,
 #pragma unroll
         for (int i = 0; i < GX; i++) {
             const int idx = threadIdx.x + (i0 + i) * NT;
-            if (i0 + i < NPL && idx < NLD) tile[(idx % L) * PSI + idx / L] = zv[i];
+            if (i0 + i < NPL && idx < NLD) tile[SI::off(idx % L) + idx / L] = zv[i];
         }
     }
     __syncthreads();
@@ -160,38 +176,76 @@ k_x_prod(int nrows, int Kx, CPtrs win, Ptrs wout, int64_t in_rs, int64_t out_rs,
     } else {
         pencil_fft_s<T, SI, true>(tile, tw);
     }
-    T outv[NPT][NO];
+    if constexpr (CC::per_point) {
+        // one grid point of all Q rows per thread: the NPI inverse pencils of a
+        // row of the tile in, the NPF forward pencils out (the last one's
+        // imaginary half zero when NO Q is odd)
+        constexpr int NPP = (L + NT - 1) / NT, NPF = (NO * Q + 1) / 2;
+        T outv[NPP][NO * Q];
 #pragma unroll
-    for (int i = 0; i < NPT; i++) {
-        const int idx = threadIdx.x + i * NT;
-        if (idx < L * Q) {
-            const int e = idx % L, r = idx / L;
-            T in[NI];
+        for (int i = 0; i < NPP; i++) {
+            const int e = threadIdx.x + i * NT;
+            if (e < L) {
+                C<T> pin[NPI];
 #pragma unroll
-            for (int f = 0; f < NI; f++) {
-                const int t = r * NI + f;
-                const C<T> c = tile[e * PSI + t / 2];
-                in[f] = (t & 1) ? c.y : c.x;
-            }
-            op(in, outv[i], blockIdx.y);
-        }
-    }
-    __syncthreads();
+                for (int pj = 0; pj < NPI; pj++) pin[pj] = tile[SI::off(e) + pj];
 #pragma unroll
-    for (int i = 0; i < NPT; i++) {
-        const int idx = threadIdx.x + i * NT;
-        if (idx < L * Q) {
-            const int e = idx % L, r = idx / L;
+                for (int r = 0; r < Q; r++) {
+                    T in[NI];
 #pragma unroll
-            for (int g = 0; g < NO; g++) {
-                const int t = r * NO + g;
-                if (t & 1) tile[e * PSF + t / 2].y = outv[i][g];
-                else tile[e * PSF + t / 2].x = outv[i][g];
+                    for (int f = 0; f < NI; f++) {
+                        const int t = r * NI + f;
+                        in[f] = (t & 1) ? pin[t / 2].y : pin[t / 2].x;
+                    }
+                    op(in, &outv[i][r * NO], blockIdx.y);
+                }
             }
         }
-    }
-    if constexpr ((NO * Q) & 1) {  // the last pencil's imaginary half is unused
-        for (int e = threadIdx.x; e < L; e += NT) tile[e * PSF + (NO * Q) / 2].y = T(0);
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < NPP; i++) {
+            const int e = threadIdx.x + i * NT;
+            if (e < L) {
+#pragma unroll
+                for (int pj = 0; pj < NPF; pj++)
+                    tile[SF::off(e) + pj] = mk<T>(outv[i][2 * pj], 2 * pj + 1 < NO * Q ? outv[i][2 * pj + 1] : T(0));
+            }
+        }
+    } else {
+        constexpr int NPT = (L * Q + NT - 1) / NT;
+        T outv[NPT][NO];
+#pragma unroll
+        for (int i = 0; i < NPT; i++) {
+            const int idx = threadIdx.x + i * NT;
+            if (idx < L * Q) {
+                const int e = idx % L, r = idx / L;
+                T in[NI];
+#pragma unroll
+                for (int f = 0; f < NI; f++) {
+                    const int t = r * NI + f;
+                    const C<T> c = tile[SI::off(e) + t / 2];
+                    in[f] = (t & 1) ? c.y : c.x;
+                }
+                op(in, outv[i], blockIdx.y);
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < NPT; i++) {
+            const int idx = threadIdx.x + i * NT;
+            if (idx < L * Q) {
+                const int e = idx % L, r = idx / L;
+#pragma unroll
+                for (int g = 0; g < NO; g++) {
+                    const int t = r * NO + g;
+                    if (t & 1) tile[SF::off(e) + t / 2].y = outv[i][g];
+                    else tile[SF::off(e) + t / 2].x = outv[i][g];
+                }
+            }
+        }
+        if constexpr ((NO * Q) & 1) {  // the last pencil's imaginary half is unused
+            for (int e = threadIdx.x; e < L; e += NT) tile[SF::off(e) + (NO * Q) / 2].y = T(0);
+        }
     }
     __syncthreads();
     if constexpr (IsLF<T>::value) {
@@ -210,7 +264,7 @@ k_x_prod(int nrows, int Kx, CPtrs win, Ptrs wout, int64_t in_rs, int64_t out_rs,
         if (r >= nr) continue;
         const int t = r * NO + g;              // its real row in the packed tile
         C<T> A, B;
-        unpack_rows<T>(tile + t / 2, PSF, k, L, scale, A, B);
+        unpack_pair<T>(tile[SF::off(k) + t / 2], tile[SF::off(k == 0 ? 0 : L - k) + t / 2], scale, A, B);
         stc<T>((V*)pick_ptr<NO>(wout.p, g) + ob + (int64_t)(row0 + r) * Kx + k, (t & 1) ? B : A);
     }
 }
