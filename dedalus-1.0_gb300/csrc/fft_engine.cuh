@@ -433,7 +433,12 @@ __device__ __forceinline__ void stockham_pass(C<T>* tile, const C<T>* tw, int p,
     for (int b = 0; b < BPT; b++) {
         const int j = jt + TPP * b;
 #pragma unroll
-        for (int r = 0; r < R; r++) v[b][r] = ((ZIN >> r) & 1u) ? zero<T>() : tile[S::off(j + r * NB) + p];
+        for (int r = 0; r < R; r++) {
+            // off() is additive over multiples of 8 rows: with such a stride the
+            // row offsets are compile-time constants from the thread's base row
+            const int o = (S::SKD == 0 || NB % 8 == 0) ? S::off(j) + S::off(r * NB) : S::off(j + r * NB);
+            v[b][r] = ((ZIN >> r) & 1u) ? zero<T>() : tile[o + p];
+        }
     }
     __syncthreads();
 #pragma unroll
@@ -454,9 +459,14 @@ __device__ __forceinline__ void stockham_pass(C<T>* tile, const C<T>* tw, int p,
             dft<R, INV>(v[b]);
         }
         const int d = (j - k) * R + k;
+        // the same for the outputs: a stride of 8 rows, or d a multiple of 8 (the
+        // first pass, d = j R, with R a multiple of 8)
+        constexpr bool lin = S::SKD == 0 || NS % 8 == 0 || (NS == 1 && R % 8 == 0);
 #pragma unroll
-        for (int r = 0; r < R; r++)
-            if (!((ZOUT >> r) & 1u)) tile[S::off(d + r * NS) + p] = v[b][r];
+        for (int r = 0; r < R; r++) {
+            const int o = lin ? S::off(d) + S::off(r * NS) : S::off(d + r * NS);
+            if (!((ZOUT >> r) & 1u)) tile[o + p] = v[b][r];
+        }
     }
     __syncthreads();
 }

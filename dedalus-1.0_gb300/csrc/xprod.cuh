@@ -77,10 +77,12 @@ template <> struct ProdCfg<512, 12, 6> {
 };
 
 // The schedule a precision runs (ProdCfg unless specialised).  per_point:
-// the product phase gives each thread one grid point of all Q rows, moving
-// whole complex entries through shared memory (otherwise each thread takes
-// one point of one row and reads and writes the real and imaginary halves
-// separately).
+// the tile fill, the product phase and the output unpacking are organised by
+// grid point, with the pencils, rows and fields of a point in compile-time
+// loops.  A thread fills and multiplies whole tile rows (complex entries, not
+// their halves), and the field pointers are fixed per loop step instead of
+// selected at run time.  Otherwise each thread takes one tile entry or one
+// point of one row at a time.
 template <typename T, int L, int NI, int NO>
 struct ProdCfgT : ProdCfg<L, NI, NO> {
     static constexpr bool per_point = false;
@@ -133,36 +135,72 @@ k_x_prod(int nrows, int Kx, CPtrs win, Ptrs wout, int64_t in_rs, int64_t out_rs,
     const int nr = min(Q, nrows - row0);
     const int64_t ib = blockIdx.y * in_rs, ob = blockIdx.y * out_rs;  // run (batch) offsets
     constexpr int NPI = (NI * Q + 1) / 2;  // inverse pencils in use
-    // the loads of a group of GX entries are in flight together (see load_tile)
-    constexpr int NLD = L * SI::P, NPL = (NLD + NT - 1) / NT;
-    constexpr int GX0 = (int)(128 / sizeof(C<T>)), GX = NPL < GX0 ? NPL : GX0;
+    if constexpr (CC::per_point) {
+        // tile row e = grid point e of the block's rows: all NPI pencils of a
+        // row, the loads of a thread's rows in flight together
+        constexpr int NE = (L + NT - 1) / NT;
+        C<T> zv[NE][NPI];
 #pragma unroll
-    for (int i0 = 0; i0 < NPL; i0 += GX) {
-        C<T> zv[GX];
+        for (int i = 0; i < NE; i++) {
+            const int e = threadIdx.x + i * NT;
 #pragma unroll
-        for (int i = 0; i < GX; i++) {
-            const int idx = threadIdx.x + (i0 + i) * NT;
-            const int e = idx % L, pj = idx / L;
-            C<T> z = zero<T>();
-            if (i0 + i < NPL && idx < NLD && pj < NPI) {
+            for (int pj = 0; pj < NPI; pj++) {
                 const int ta = 2 * pj, tb = 2 * pj + 1;
                 const int ra = ta / NI, fa = ta % NI, rb = tb / NI, fb = tb % NI;
                 const bool va = ra < nr, vb = tb < NI * Q && rb < nr;
-                if (va || vb) {
-                    const V* pa = (const V*)pick_ptr<NI>(win.p, fa) + ib + (int64_t)(row0 + (va ? ra : rb)) * Kx;
-                    const V* pb =
-                        (const V*)pick_ptr<NI>(win.p, vb ? fb : fa) + ib + (int64_t)(row0 + (vb ? rb : ra)) * Kx;
-                    z = pack_rows<T>(pa, pb, e, L, Kx);
+                C<T> z = zero<T>();
+                if ((NE * NT == L || e < L) && (va || vb)) {
+                    const V* pa = (const V*)win.p[fa] + ib + (int64_t)(row0 + ra) * Kx;
+                    const V* pb = (const V*)win.p[tb < NI * Q ? fb : fa] + ib + (int64_t)(row0 + rb) * Kx;
+                    z = pack_rows<T>(va ? pa : pb, vb ? pb : pa, e, L, Kx);
                     if (!va) z.x = T(0);
                     if (!vb) z.y = T(0);
                 }
+                zv[i][pj] = z;
             }
-            zv[i] = z;
         }
 #pragma unroll
-        for (int i = 0; i < GX; i++) {
-            const int idx = threadIdx.x + (i0 + i) * NT;
-            if (i0 + i < NPL && idx < NLD) tile[SI::off(idx % L) + idx / L] = zv[i];
+        for (int i = 0; i < NE; i++) {
+            const int e = threadIdx.x + i * NT;
+            if (NE * NT == L || e < L) {
+#pragma unroll
+                for (int pj = 0; pj < NPI; pj++) tile[SI::off(e) + pj] = zv[i][pj];
+#pragma unroll
+                for (int pj = NPI; pj < SI::P; pj++) tile[SI::off(e) + pj] = zero<T>();
+            }
+        }
+    } else {
+        // the loads of a group of GX entries are in flight together (see load_tile)
+        constexpr int NLD = L * SI::P, NPL = (NLD + NT - 1) / NT;
+        constexpr int GX0 = (int)(128 / sizeof(C<T>)), GX = NPL < GX0 ? NPL : GX0;
+#pragma unroll
+        for (int i0 = 0; i0 < NPL; i0 += GX) {
+            C<T> zv[GX];
+#pragma unroll
+            for (int i = 0; i < GX; i++) {
+                const int idx = threadIdx.x + (i0 + i) * NT;
+                const int e = idx % L, pj = idx / L;
+                C<T> z = zero<T>();
+                if (i0 + i < NPL && idx < NLD && pj < NPI) {
+                    const int ta = 2 * pj, tb = 2 * pj + 1;
+                    const int ra = ta / NI, fa = ta % NI, rb = tb / NI, fb = tb % NI;
+                    const bool va = ra < nr, vb = tb < NI * Q && rb < nr;
+                    if (va || vb) {
+                        const V* pa = (const V*)pick_ptr<NI>(win.p, fa) + ib + (int64_t)(row0 + (va ? ra : rb)) * Kx;
+                        const V* pb =
+                            (const V*)pick_ptr<NI>(win.p, vb ? fb : fa) + ib + (int64_t)(row0 + (vb ? rb : ra)) * Kx;
+                        z = pack_rows<T>(pa, pb, e, L, Kx);
+                        if (!va) z.x = T(0);
+                        if (!vb) z.y = T(0);
+                    }
+                }
+                zv[i] = z;
+            }
+#pragma unroll
+            for (int i = 0; i < GX; i++) {
+                const int idx = threadIdx.x + (i0 + i) * NT;
+                if (i0 + i < NPL && idx < NLD) tile[SI::off(idx % L) + idx / L] = zv[i];
+            }
         }
     }
     __syncthreads();
@@ -254,18 +292,41 @@ k_x_prod(int nrows, int Kx, CPtrs win, Ptrs wout, int64_t in_rs, int64_t out_rs,
     } else {
         pencil_fft_s<T, SF, false>(tile, tw, threadIdx.x < SF::NT);
     }
-    // field-major order: consecutive threads write the block's Q consecutive rows
-    // of one output field, a contiguous range, so a 32-byte sector shared by two
-    // rows (complex64 rows of an odd number of half-sectors) is written whole by
-    // one warp instead of in two halves at different times
-    for (int idx = threadIdx.x; idx < Kx * Q * NO; idx += NT) {
-        const int k = idx % Kx, u = idx / Kx;
-        const int g = u / Q, r = u % Q;
-        if (r >= nr) continue;
-        const int t = r * NO + g;              // its real row in the packed tile
-        C<T> A, B;
-        unpack_pair<T>(tile[SF::off(k) + t / 2], tile[SF::off(k == 0 ? 0 : L - k) + t / 2], scale, A, B);
-        stc<T>((V*)pick_ptr<NO>(wout.p, g) + ob + (int64_t)(row0 + r) * Kx + k, (t & 1) ? B : A);
+    if constexpr (CC::per_point) {
+        // two halves of the block take the rows r < Q/2 and r >= Q/2; within a
+        // half consecutive threads take consecutive kx of one output row
+        constexpr int KG = NT / 2;
+        const int half = threadIdx.x / KG;
+        for (int k = threadIdx.x % KG; k < Kx; k += KG) {
+            const C<T>* zr = tile + SF::off(k);
+            const C<T>* znr = tile + SF::off(k == 0 ? 0 : L - k);
+#pragma unroll
+            for (int r2 = 0; r2 < Q / 2; r2++) {
+                const int r = half * (Q / 2) + r2;
+                if (r >= nr) continue;
+#pragma unroll
+                for (int g = 0; g < NO; g++) {
+                    const int t = r * NO + g;
+                    C<T> A, B;
+                    unpack_pair<T>(zr[t / 2], znr[t / 2], scale, A, B);
+                    stc<T>((V*)wout.p[g] + ob + (int64_t)(row0 + r) * Kx + k, (t & 1) ? B : A);
+                }
+            }
+        }
+    } else {
+        // field-major order: consecutive threads write the block's Q consecutive rows
+        // of one output field, a contiguous range, so a 32-byte sector shared by two
+        // rows (complex64 rows of an odd number of half-sectors) is written whole by
+        // one warp instead of in two halves at different times
+        for (int idx = threadIdx.x; idx < Kx * Q * NO; idx += NT) {
+            const int k = idx % Kx, u = idx / Kx;
+            const int g = u / Q, r = u % Q;
+            if (r >= nr) continue;
+            const int t = r * NO + g;              // its real row in the packed tile
+            C<T> A, B;
+            unpack_pair<T>(tile[SF::off(k) + t / 2], tile[SF::off(k == 0 ? 0 : L - k) + t / 2], scale, A, B);
+            stc<T>((V*)pick_ptr<NO>(wout.p, g) + ob + (int64_t)(row0 + r) * Kx + k, (t & 1) ? B : A);
+        }
     }
 }
 
