@@ -105,6 +105,14 @@ struct ProdCfgT<float, 256, 3, 5> {
     static constexpr int min_blocks = 6;   // 56 registers: 6 blocks per SM (72 and 4 blocks without the bound)
 };
 
+// FP32 MHD in divergence form (6 -> 8) on 256-point rows: the default 16-pencil
+// tiles (12 inverse, 16 forward pencils for 4 rows), point-major phases.
+template <>
+struct ProdCfgT<float, 256, 6, 8> : ProdCfg<256, 6, 8> {
+    static constexpr bool per_point = true;
+    static constexpr int min_blocks = 4;   // 64 registers (90 unbounded: 2 blocks per SM, 565 vs 348 us)
+};
+
 template <typename T, int L, int NI, int NO>
 constexpr size_t prod_smem(size_t csize) {
     using CC = ProdCfgT<T, L, NI, NO>;
