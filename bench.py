@@ -80,6 +80,8 @@ TRAFFIC = {
     ("hydro3d-256-fp64", "x_div_256_f64"): (
         4 * (67.81e6 + 50.79e6),
         "ncu capture of the same kernel on 128x128x256 FP64 (67.81 MB read + 50.79 MB written), x4 rows for 256^3"),
+    ("hydro3d-256-fp32", "x_div_256_f32"): (
+        135.41e6 + 166.06e6, "ncu capture at full size (135.41 MB read + 166.06 MB written)"),
     ("les64-closure", "les_mlp"): (
         9.48e6 + 0.0, "ncu capture at full size (9.48 MB read, stresses still in L2 at kernel end)"),
 }
