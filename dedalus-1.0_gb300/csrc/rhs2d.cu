@@ -6,6 +6,8 @@ namespace dd {
 
 DD_RHS2D_INSTANTIATE(extern, double)
 DD_RHS2D_INSTANTIATE(extern, float)
+DD_RHS2D_INSTANTIATE_LO(extern, PHYS_HYDRO_DIV)
+DD_RHS2D_INSTANTIATE_LO(extern, PHYS_BOUSS_DIV)
 
 // ------------------------------------------------------------------ pass 4
 struct Phys2Params {
@@ -16,6 +18,7 @@ struct Phys2Params {
 struct Stage2Args {
     Geo2 g;
     const double* kx; const double* ky; const double* inv_k2; int intk;
+    const float* kxf; const float* kyf;   // the wavenumber tables rounded to float
     int phys; Phys2Params pp;
     int nrun;
     CPtrs nc; int64_t nc_rs;          // unprojected products (compact)
@@ -94,7 +97,7 @@ __global__ void k_stage2(Stage2Args a) {
         if constexpr (NF == 3) {
             const int64_t ri = a.rin_compact ? run * a.rin_rs + j : run * a.rin_rs + (int64_t)ix * g.Ny + ky_i;
             const double2 T = ((const double2*)a.rin.p[2])[ri];
-            const double2 ud = ((const double2*)a.rin.p[a.pp.dir])[ri];
+            const double2 ud = ((const double2*)(a.pp.dir == 0 ? a.rin.p[0] : a.rin.p[1]))[ri];
             // buoyancy: ((T * g) * alpha_t) added to u_dir (physics.py:691-694)
             const double2 b = make_double2(rmul(rmul(T.x, a.pp.g), a.pp.alpha_t), rmul(rmul(T.y, a.pp.g), a.pp.alpha_t));
             if (a.pp.dir == 0) N[0] = make_double2(radd(N[0].x, b.x), radd(N[0].y, b.y));
@@ -133,6 +136,109 @@ __global__ void k_stage2(Stage2Args a) {
             }
         }
     }
+}
+
+// The RK2mid stages of the low-storage FP32 step (divergence forms): complex64
+// products, stage derivative k1 and stage state; N, the projection and the
+// buoyancy / stratification terms in float from float wavenumbers (k^2 exact
+// for integer wavenumbers); stage 1 forms the float stage state in float;
+// stage 2 updates the FP64 state in FP64 (y = f0 y + h phi1 k1 + 2 h phi2 (k2 - k1)).
+template <int NF, int MODE>
+__global__ void k_stage2_lo(Stage2Args a) {
+    static_assert(MODE == 1 || MODE == 2, "RK2mid stages only");
+    const Geo2& g = a.g;
+    const int per = g.Kx * g.Ky;
+    const int64_t n = (int64_t)per * a.nrun;
+    bool tabs = a.intk && a.inv_k2;
+#pragma unroll
+    for (int c = 0; c < NF; c++) tabs = tabs && a.tab[c];
+    const float hf = (float)a.h;
+    const float pg = (float)a.pp.g, pat = (float)a.pp.alpha_t, pbeta = (float)a.pp.beta;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int run = (int)(i / per);
+        const int j = (int)(i - (int64_t)run * per);
+        const int kyc = j % g.Ky, ix = j / g.Ky;
+        const int ky_i = compact_to_full(kyc, g.Ny, g.Ky);
+        const float kx = a.kxf[ix], ky = a.kyf[ky_i];
+        int q = 0;
+        double k2 = 0.;
+        float s;
+        if (tabs) {
+            q = (int)(kx * kx + ky * ky);
+            s = (float)a.inv_k2[q];
+        } else {
+            const double kxv = a.kx[ix], kyv = a.ky[ky_i];
+            k2 = radd(rmul(kxv, kxv), rmul(kyv, kyv));
+            q = a.intk ? (int)k2 : 0;
+            s = (float)((a.intk && a.inv_k2) ? a.inv_k2[q] : rdiv(1., k2 == 0. ? 1. : k2));
+        }
+        const int64_t ni = run * a.nc_rs + j;
+        // N = -i k_j T_ij with T_xx = u_x^2 - u_y^2, T_xy = u_x u_y; -i s = (s.y, -s.x)
+        const float2 p0 = ((const float2*)a.nc.p[0])[ni], p1 = ((const float2*)a.nc.p[1])[ni];
+        float2 N[NF];
+        N[0] = make_float2(fmaf(ky, p1.y, kx * p0.y), -fmaf(ky, p1.x, kx * p0.x));
+        N[1] = make_float2(kx * p1.y, -(kx * p1.x));
+        if constexpr (NF == 3) {
+            // T and u_dir of the state the RHS was evaluated on: the FP64 state
+            // in stage 1, the complex64 stage state in stage 2
+            float2 T, ud;
+            const void* up = a.pp.dir == 0 ? a.rin.p[0] : a.rin.p[1];
+            if constexpr (MODE == 1) {
+                const int64_t ri = run * a.rin_rs + (int64_t)ix * g.Ny + ky_i;
+                const double2 Td = ((const double2*)a.rin.p[2])[ri], udd = ((const double2*)up)[ri];
+                T = make_float2((float)Td.x, (float)Td.y);
+                ud = make_float2((float)udd.x, (float)udd.y);
+            } else {
+                const int64_t ri = run * a.rin_rs + j;
+                T = ((const float2*)a.rin.p[2])[ri];
+                ud = ((const float2*)up)[ri];
+            }
+            const float2 b = make_float2(T.x * pg * pat, T.y * pg * pat);   // (T g) alpha_t
+            if (a.pp.dir == 0) N[0] = make_float2(N[0].x + b.x, N[0].y + b.y);
+            else N[1] = make_float2(N[1].x + b.x, N[1].y + b.y);
+            // -div(u T) - beta u_dir; i s = (-s.y, s.x)
+            const float2 fx = ((const float2*)a.nc.p[2])[ni], fy = ((const float2*)a.nc.p[3])[ni];
+            const float sr = fmaf(ky, fy.x, kx * fx.x), si = fmaf(ky, fy.y, kx * fx.y);
+            N[2] = make_float2(si - ud.x * pbeta, -sr - ud.y * pbeta);
+        }
+        // projection: N -= k (k . N) / k^2
+        const float cr = fmaf(ky, N[1].x, kx * N[0].x) * s, ci = fmaf(ky, N[1].y, kx * N[0].y) * s;
+        N[0] = make_float2(fmaf(-kx, cr, N[0].x), fmaf(-kx, ci, N[0].y));
+        N[1] = make_float2(fmaf(-ky, cr, N[1].x), fmaf(-ky, ci, N[1].y));
+        const int64_t full = run * a.y_rs + (int64_t)ix * g.Ny + ky_i;
+        const int64_t ci2 = run * a.c_rs + j;
+#pragma unroll
+        for (int c = 0; c < NF; c++) {
+            double f0, f1, f2;
+            if (tabs) {
+                const double* t = reinterpret_cast<const double*>(a.tab[c] + q);
+                f0 = t[1]; f1 = t[2]; f2 = t[3];
+            } else {
+                double Z;
+                phis2(a, c, q, k2, Z, f0, f1, f2);
+            }
+            const double2 y0 = ((const double2*)a.y.p[c])[full];
+            if constexpr (MODE == 1) {
+                ((float2*)a.k1.p[c])[ci2] = N[c];
+                const float f0f = (float)f0, f1hf = (float)f1 * hf;
+                ((float2*)a.ys.p[c])[ci2] = make_float2(fmaf(f1hf, N[c].x, (float)y0.x * f0f),
+                                                        fmaf(f1hf, N[c].y, (float)y0.y * f0f));
+            } else {
+                const float2 d1 = ((const float2*)a.k1.p[c])[ci2];
+                ((double2*)a.y.p[c])[full] =
+                    etd2rk2_fma(y0, make_double2((double)d1.x, (double)d1.y),
+                                make_double2((double)N[c].x, (double)N[c].y), f0, f1 * a.h, 2. * f2 * a.h);
+            }
+        }
+    }
+}
+
+template <int MODE>
+static int launch_stage2_lo(const Stage2Args& a, unsigned nb, cudaStream_t st) {
+    if (a.phys == PHYS_HYDRO_DIV) DD_KT("rk2mid_stage2d_lo", st, k_stage2_lo<2, MODE><<<nb, 256, 0, st>>>(a));
+    else DD_KT("rk2mid_stage2d_lo", st, k_stage2_lo<3, MODE><<<nb, 256, 0, st>>>(a));
+    DD_LAUNCH_CHECK();
+    return DD_OK;
 }
 
 template <int MODE>
@@ -226,6 +332,17 @@ static int nonlinear2_any(const dd_plan* pl, int prec, bool compact, const Work2
     return DD_ERR_UNSUPPORTED;
 }
 
+// the passes of the low-storage FP32 step: complex64 products out and, with
+// compact, complex64 stage states in
+static int nonlinear2_lo(int phys, const dd_plan* pl, bool compact, const Work2& w, const void* const* st,
+                         int64_t st_rs, cudaStream_t s) {
+    if (phys == PHYS_HYDRO_DIV)
+        return compact ? nonlinear2<float, true, PHYS_HYDRO_DIV, float>(pl, w, st, st_rs, s)
+                       : nonlinear2<float, false, PHYS_HYDRO_DIV, float>(pl, w, st, st_rs, s);
+    return compact ? nonlinear2<float, true, PHYS_BOUSS_DIV, float>(pl, w, st, st_rs, s)
+                   : nonlinear2<float, false, PHYS_BOUSS_DIV, float>(pl, w, st, st_rs, s);
+}
+
 static size_t work2_bytes(int prec, const Geo2& g, int nrun) {
     size_t b = 0;
     DD_PREC_DISPATCH(prec, T, b = Work2::bytes<T>(g, nrun));
@@ -243,6 +360,7 @@ static int nonlinear2_phys(int phys, const dd_plan* pl, int prec, bool compact, 
 static void fill_common(Stage2Args& a, const dd_plan* p, int phys, const double* pp, const double* inv_k2,
                         int nrun, const Work2& w, int prec) {
     a.g = p->g2; a.kx = p->kx; a.ky = p->ky; a.inv_k2 = inv_k2; a.intk = inv_k2 != nullptr;
+    a.kxf = p->kxf; a.kyf = p->kyf;
     a.phys = phys; a.nrun = nrun;
     if (pp) { a.pp.g = pp[0]; a.pp.alpha_t = pp[1]; a.pp.beta = pp[2]; a.pp.dir = (int)pp[3]; }
     const int no = phys == PHYS_HYDRO || phys == PHYS_HYDRO_DIV ? 2 : (phys == PHYS_BOUSS ? 3 : 4);
@@ -322,24 +440,34 @@ int dd_rk2mid_step2d(const dd_plan* p, int phys, const double* params, int nrun,
     Stage2Args a{};
     fill_common(a, p, phys, params, inv_k2, nrun, w, precision);
     a.vo = viscosity_order;
+    // FP32 transforms in divergence form: the low-storage step (complex64
+    // products, stage derivative and stage state; FP64 state)
+    const bool lo = p2_div(phys) && precision == DD_FP32;
+    if (lo)
+        for (int f = 0; f < 4; f++) a.nc.p[f] = w.NCf(f);
     for (int c = 0; c < nf; c++) {
         a.y.p[c] = state[c];
         a.nu[c] = nu[c];
-        DD_PREC_DISPATCH(precision, T, a.ys.p[c] = (void*)w.YS<T>(c); a.k1.p[c] = (void*)w.K1<T>(c));
+        if (lo) { a.ys.p[c] = w.YSf(c); a.k1.p[c] = w.K1f(c); }
+        else DD_PREC_DISPATCH(precision, T, a.ys.p[c] = (void*)w.YS<T>(c); a.k1.p[c] = (void*)w.K1<T>(c));
     }
     a.y_rs = state_rs;
     const unsigned nb = ew_grid2((int64_t)p->g2.Kx * p->g2.Ky * nrun);
     // stage 1: k1 = N(y); y2 = etd1(y, k1, dt/2)            (time_step.py:286-294)
-    DD_TRY(nonlinear2_phys(phys, p, precision, false, w, (const void* const*)state, state_rs, st));
+    if (lo) DD_TRY(nonlinear2_lo(phys, p, false, w, (const void* const*)state, state_rs, st));
+    else DD_TRY(nonlinear2_phys(phys, p, precision, false, w, (const void* const*)state, state_rs, st));
     for (int c = 0; c < nf; c++) { a.rin.p[c] = state[c]; a.tab[c] = intk ? (const double4*)tab_half[c] : nullptr; }
     a.rin_rs = state_rs; a.rin_compact = 0; a.h = dt / 2.; a.mode = 1;
-    DD_TRY(launch_stage2<1>(a, nb, "rk2mid_stage2d", st));
+    if (lo) DD_TRY(launch_stage2_lo<1>(a, nb, st));
+    else DD_TRY(launch_stage2<1>(a, nb, "rk2mid_stage2d", st));
     // stage 2: k2 = N(y2); y = etd2rk2(y, k1, k2, dt)       (time_step.py:297-305)
     const void* ysp[3] = {a.ys.p[0], a.ys.p[1], a.ys.p[2]};
-    DD_TRY(nonlinear2_phys(phys, p, precision, true, w, ysp, (int64_t)w.kc, st));
+    if (lo) DD_TRY(nonlinear2_lo(phys, p, true, w, ysp, (int64_t)w.kc, st));
+    else DD_TRY(nonlinear2_phys(phys, p, precision, true, w, ysp, (int64_t)w.kc, st));
     for (int c = 0; c < nf; c++) { a.rin.p[c] = ysp[c]; a.tab[c] = intk ? (const double4*)tab_full[c] : nullptr; }
     a.rin_rs = (int64_t)w.kc; a.rin_compact = 1; a.h = dt; a.mode = 2;
-    DD_TRY(launch_stage2<2>(a, nb, "rk2mid_stage2d", st));
+    if (lo) DD_TRY(launch_stage2_lo<2>(a, nb, st));
+    else DD_TRY(launch_stage2<2>(a, nb, "rk2mid_stage2d", st));
     if (!nonkept_flag || *nonkept_flag) {
         DD_KT("decay_nonkept2", st, k_decay_nonkept2<<<ew_grid2(p->g2.kcount() * nrun), 256, 0, st>>>(
                                         p->g2, a.y, state_rs, nf, nrun, p->kx, p->ky, a));

@@ -3,4 +3,5 @@
 
 namespace dd {
 DD_RHS2D_INSTANTIATE_A(, float)
+DD_RHS2D_INSTANTIATE_LO(, PHYS_HYDRO_DIV)
 }  // namespace dd

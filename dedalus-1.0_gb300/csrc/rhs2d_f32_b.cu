@@ -3,4 +3,5 @@
 
 namespace dd {
 DD_RHS2D_INSTANTIATE_B(, float)
+DD_RHS2D_INSTANTIATE_LO(, PHYS_BOUSS_DIV)
 }  // namespace dd

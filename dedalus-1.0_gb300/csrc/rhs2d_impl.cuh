@@ -42,7 +42,9 @@ template <> struct Phys2<PHYS_BOUSS_DIV> { static constexpr int NF = 3, NI = 3, 
 static_assert(Phys2<PHYS_BOUSS>::NI <= DD_MAXF, "too many transform fields for Ptrs");
 
 // ------------------------------------------------------------------ pass 1
-template <typename T, bool COMPACT, int PHYS>
+// SST: the type of a compact input state (stage states of the low-storage
+// FP32 step are complex64); full-layout inputs are complex128.
+template <typename T, bool COMPACT, int PHYS, typename SST = double>
 struct OpYInvPhys2 {
     using V = typename Vec2<T>::type;
     static constexpr const char* name = PHYS == PHYS_HYDRO ? "y_inv_hydro2d" : PHYS == PHYS_BOUSS ? "y_inv_bouss2d"
@@ -60,6 +62,12 @@ struct OpYInvPhys2 {
     }
     __device__ C<T> load(int fld, int run, int e, int ix) const {
         if (!kept_full(e, g.Ny, g.My)) return zero<T>();
+        if constexpr (COMPACT && std::is_same<SST, float>::value) {
+            static_assert(p2_div(PHYS), "complex64 stage states are for the divergence forms");
+            const float2* S = (const float2*)st.p[fld] + run * st_rs;
+            const float2 v = S[(int64_t)ix * g.Ky + full_to_compact(e, g.Ny, g.Ky)];
+            return mk<T>((T)v.x, (T)v.y);
+        }
         double2 r;
         if (p2_div(PHYS) || fld < 2) r = get(fld, run, ix, e);   // divergence forms: the state itself
         else if (fld == 2) {  // curlX, N == 2: X[1].deriv(x) - X[0].deriv(y)  (physics.py:400)
@@ -117,7 +125,9 @@ struct ProdBoussDiv2 {
 };
 
 // ------------------------------------------------------------------ pass 3
-template <typename T>
+// ST: the type of the compact products (complex128, or complex64 on the
+// low-storage FP32 step).
+template <typename T, typename ST = double>
 struct OpYFwdCompact2 {
     using V = typename Vec2<T>::type;
     static constexpr const char* name = "y_fwd_compact2d";
@@ -132,8 +142,9 @@ struct OpYFwdCompact2 {
     __device__ void store(int fld, int run, int e, int ix, const C<T>* col, int PS) const {
         if (!kept_full(e, g.Ny, g.My)) return;
         const C<T> c = col[e * PS];
-        ((double2*)out.p[fld])[run * nc_rs + (int64_t)ix * g.Ky + full_to_compact(e, g.Ny, g.Ky)] =
-            make_double2((double)c.x, (double)c.y);
+        const int64_t o = run * nc_rs + (int64_t)ix * g.Ky + full_to_compact(e, g.Ny, g.Ky);
+        if constexpr (std::is_same<ST, float>::value) ((float2*)out.p[fld])[o] = make_float2((float)c.x, (float)c.y);
+        else ((double2*)out.p[fld])[o] = make_double2((double)c.x, (double)c.y);
     }
 };
 
@@ -150,12 +161,19 @@ struct Work2 {
     // compact regions: products NC (up to 4), then K1 (3) and YS (3)
     template <typename T> double2* K1(int f) const { return NC<T>(4) + (size_t)f * nrun * kc; }
     template <typename T> double2* YS(int f) const { return NC<T>(7) + (size_t)f * nrun * kc; }
+    // the same ten compact regions as complex64 (low-storage FP32 step), in the
+    // first half of the complex128 space
+    float2* NCf(int f) const { return (float2*)NC<float>(0) + (size_t)f * nrun * kc; }
+    float2* K1f(int f) const { return NCf(4) + (size_t)f * nrun * kc; }
+    float2* YSf(int f) const { return NCf(7) + (size_t)f * nrun * kc; }
     template <typename T> static size_t bytes(const Geo2& g, int nrun) {
         return up256(sizeof(C<T>) * 5 * (size_t)nrun * g.wcount()) + sizeof(double2) * 10 * (size_t)nrun * g.Kx * g.Ky;
     }
 };
 
-template <typename T, bool COMPACT, int PHYS>
+// ST = float (FP32 transforms, divergence forms): complex64 products out of
+// pass 3 and, with COMPACT, complex64 stage states into pass 1.
+template <typename T, bool COMPACT, int PHYS, typename ST = double>
 int nonlinear2(const dd_plan* pl, const Work2& w, const void* const* st, int64_t st_rs, cudaStream_t s) {
     const Geo2& g = pl->g2;
     using PH = Phys2<PHYS>;
@@ -166,13 +184,16 @@ int nonlinear2(const dd_plan* pl, const Work2& w, const void* const* st, int64_t
     constexpr int NW = PH::NI > PH::NO ? PH::NI : PH::NO;
     static_assert(NW <= 5, "Work2 holds 5 transform buffers");
     for (int f = 0; f < NW; f++) { wo.p[f] = w.W<T>(f); wi.p[f] = wo.p[f]; }
-    for (int f = 0; f < PH::NO; f++) nc.p[f] = w.NC<T>(f);
+    for (int f = 0; f < PH::NO; f++) {
+        if constexpr (std::is_same<ST, float>::value) nc.p[f] = w.NCf(f);
+        else nc.p[f] = w.NC<T>(f);
+    }
     // one run of a 64- or 128-point grid: small tiles, so that the y passes
     // have enough blocks (the default 32-pencil tiles give 2 per field)
     // (a tuned tile variant, set on the plan, takes precedence)
     const int yv = pl->sched_y2d;
     const bool small = yv == 0 && w.nrun == 1 && (g.Ny == 64 || g.Ny == 128);
-    OpYInvPhys2<T, COMPACT, PHYS> a{g, sin, st_rs, wo, (int64_t)w.w, TwSel<T>::y(pl), pl->kx, pl->ky};
+    OpYInvPhys2<T, COMPACT, PHYS, ST> a{g, sin, st_rs, wo, (int64_t)w.w, TwSel<T>::y(pl), pl->kx, pl->ky};
     int rc = 1;
     if (yv) rc = launch_pass_variant<T, true, true, false>(g.Ny, yv, a, g.Kx, w.nrun, PH::NI, s);
     if (rc == 1 && small) rc = launch_pass_small<T, true, true, false>(g.Ny, a, g.Kx, w.nrun, PH::NI, s);
@@ -191,7 +212,7 @@ int nonlinear2(const dd_plan* pl, const Work2& w, const void* const* st, int64_t
         DD_TRY((launch_x_prod_len<T>("x_prod_bouss2d", g.Nx, g.Ny, g.Kx, wi, wo, w.nrun, (int64_t)w.w, (int64_t)w.w,
                                      TwSel<T>::x(pl), (T)pl->inv_n, ProdBouss2<T>{}, s)));
     }
-    OpYFwdCompact2<T> c{g, wi, (int64_t)w.w, nc, (int64_t)w.kc, TwSel<T>::y(pl)};
+    OpYFwdCompact2<T, ST> c{g, wi, (int64_t)w.w, nc, (int64_t)w.kc, TwSel<T>::y(pl)};
     rc = 1;
     if (yv) rc = launch_pass_variant<T, false, false, true>(g.Ny, yv, c, g.Kx, w.nrun, PH::NO, s);
     if (rc == 1 && small) rc = launch_pass_small<T, false, false, true>(g.Ny, c, g.Kx, w.nrun, PH::NO, s);
@@ -211,5 +232,11 @@ int nonlinear2(const dd_plan* pl, const Work2& w, const void* const* st, int64_t
 #define DD_RHS2D_INSTANTIATE_B(EXT, T) DD_RHS2D_INSTANTIATE_PH(EXT, T, PHYS_BOUSS) \
     DD_RHS2D_INSTANTIATE_PH(EXT, T, PHYS_BOUSS_DIV)
 #define DD_RHS2D_INSTANTIATE(EXT, T) DD_RHS2D_INSTANTIATE_A(EXT, T) DD_RHS2D_INSTANTIATE_B(EXT, T)
+// the low-storage FP32 step (divergence forms, complex64 products and stage states)
+#define DD_RHS2D_INSTANTIATE_LO(EXT, PH)                                                                \
+    EXT template int nonlinear2<float, false, PH, float>(const dd_plan*, const Work2&, const void* const*,  \
+                                                         int64_t, cudaStream_t);                        \
+    EXT template int nonlinear2<float, true, PH, float>(const dd_plan*, const Work2&, const void* const*,   \
+                                                        int64_t, cudaStream_t);
 
 }  // namespace dd

@@ -34,6 +34,10 @@ from . import init_cond
 PHYS_BOUSS = 1
 PHYS_BOUSS_DIV = 3            # divergence form, for solenoidal velocities
 DIV_TOL2 = 1e-24
+# FP32 transforms keep the increments, and so the state's divergence, at FP32
+# accuracy (the low-storage step projects in float): a relative divergence up
+# to 1e-6, below the FP32 path's own error, still takes the divergence form.
+DIV_TOL2_FP32 = 1e-12
 _TUNE_ENV = "DD_TUNE_CACHE"
 
 
@@ -213,7 +217,8 @@ class BoussinesqEnsemble2D:
             _lib.call("dd_divergence_sums2d", c.plan.handle, c.nrun, dptr(base[0]), dptr(base[1]), 3 * c.fsize,
                       dptr(buf), st)
             num, den = buf.tolist()
-            c.phys = PHYS_BOUSS_DIV if self.nonlinear_form == 'auto' and num <= DIV_TOL2 * den else PHYS_BOUSS
+            tol = DIV_TOL2_FP32 if self.prec == _lib.DD_FP32 else DIV_TOL2
+            c.phys = PHYS_BOUSS_DIV if self.nonlinear_form == 'auto' and num <= tol * den else PHYS_BOUSS
 
     nonlinear_form = 'auto'
 

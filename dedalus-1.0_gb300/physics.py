@@ -406,7 +406,7 @@ class IncompressibleHydro(ReferenceOrderRHS, Physics):
             _lib.call("dd_divergence_sums2d", plan.handle, 1, dptr(data['u'][0].kdata), dptr(data['u'][1].kdata), 0,
                       dptr(buf), current_stream())
             num, den = buf.tolist()
-            if num <= self.DIV_TOL2 * den:
+            if num <= (self.DIV_TOL2_FP32 if prec == _lib.DD_FP32 else self.DIV_TOL2) * den:
                 phys += 2
         self.last_phys2d = phys
         _lib.call("dd_rk2mid_step2d", plan.handle, phys, ppa, 1, sp, 0,

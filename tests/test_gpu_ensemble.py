@@ -98,3 +98,44 @@ def test_ensemble_divergence_form_equals_curl_form(dd, cuda):
         num = sum(np.sum(np.abs(x - y) ** 2) for x, y in zip(a, b))
         den = sum(np.sum(np.abs(y) ** 2) for y in b)
         assert np.sqrt(num / den) < 1e-12
+
+
+@pytest.mark.gpu
+def test_fp32_ensemble_tracks_fp64_and_oracle(dd, cuda):
+    """The FP32 ensemble (float transforms; in divergence form the low-storage
+    step: complex64 products, stage derivative and stage state, N and the
+    projection in float, the FP64 state updated in FP64) against the FP64
+    ensemble and the oracle, all four configured sizes, runs with velocity.
+    Tolerance: the step increments (state after 4 steps minus the initial
+    state) agree with the FP64 ensemble's to 1e-4 relative L2 per run (float
+    arithmetic on the nonlinear term), and the states with the oracle's to
+    1e-6."""
+    sizes = [64, 128, 256, 512, 64]
+    dt, nsteps = 0.01, 4
+    runs = {}
+    init = None
+    for prec in ("fp64", "fp32"):
+        ens = dd.ensemble.BoussinesqEnsemble2D(sizes, nu=2e-3, kappa=2e-3, precision=prec)
+        ens.load_initial_conditions(seed=21)
+        if init is None:
+            for r, n in enumerate(sizes):
+                u = dd.init_cond.turbulence_2d((n, n), seed=200 + r, energy_target=1e-3)
+                st = ens.run_state(r)
+                ens.set_run_state(r, [u[0], u[1], st[2]])
+            init = [ens.run_state(r) for r in range(len(sizes))]
+        else:
+            for r in range(len(sizes)):
+                ens.set_run_state(r, init[r])
+        for _ in range(nsteps):
+            ens.step(dt, graph=True)
+        assert all(c.phys == 3 for c in ens.classes)
+        runs[prec] = [ens.run_state(r) for r in range(len(sizes))]
+    # eager steps re-check the form on the FP32 state: still solenoidal to FP32 accuracy
+    ens.step(dt, graph=False)
+    assert all(c.phys == 3 for c in ens.classes)
+    for r, n in enumerate(sizes):
+        d32 = [a - b for a, b in zip(runs["fp32"][r], init[r])]
+        d64 = [a - b for a, b in zip(runs["fp64"][r], init[r])]
+        assert rel_l2(d32, d64) < 1e-4, (r, n, rel_l2(d32, d64))
+        if n <= 128:
+            assert rel_l2(runs["fp32"][r], oracle_run((n, n), init[r], nsteps, dt)) < 1e-6, (r, n)
