@@ -113,6 +113,20 @@ struct ProdCfgT<float, 256, 6, 8> : ProdCfg<256, 6, 8> {
     static constexpr int min_blocks = 4;   // 64 registers (90 unbounded: 2 blocks per SM, 565 vs 348 us)
 };
 
+// FP32 2D Boussinesq in divergence form (3 -> 4) on 256- and 512-point rows:
+// the default tiles (16 pencils, 8 rows per block; 8 pencils, 4 rows),
+// point-major phases.
+template <>
+struct ProdCfgT<float, 256, 3, 4> : ProdCfg<256, 3, 4> {
+    static constexpr bool per_point = true;
+    static constexpr int min_blocks = 4;   // 64 registers (72 unbounded, 3 blocks per SM)
+};
+template <>
+struct ProdCfgT<float, 512, 3, 4> : ProdCfg<512, 3, 4> {
+    static constexpr bool per_point = true;
+    static constexpr int min_blocks = 1;
+};
+
 template <typename T, int L, int NI, int NO>
 constexpr size_t prod_smem(size_t csize) {
     using CC = ProdCfgT<T, L, NI, NO>;
