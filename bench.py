@@ -113,10 +113,12 @@ def C2(N):
     return 16 * N * (N // 2 + 1)
 
 
-def bytes_2d(label, runs, cs, ni, no, nf):
+def bytes_2d(label, runs, cs, ni, no, nf, lo=False):
     """Algorithmic bytes of one launch of a 2D pass for size classes runs
     {N: number of runs in the launch}: compact intermediates W [y][kxc]
-    (cs bytes per complex), kept-mode arrays Kx x Ky complex128."""
+    (cs bytes per complex), kept-mode arrays Kx x Ky complex128.  lo: the
+    low-storage FP32 step, whose products, stage derivative and stage state
+    are complex64 (the state stays complex128)."""
     m = re.search(r"_(\d+)_f(32|64)$", label)
     sizes = [int(m.group(1))] if m else list(runs)
     tot = 0.0
@@ -125,12 +127,19 @@ def bytes_2d(label, runs, cs, ni, no, nf):
         M = (N - 1) // 3
         Kx, Ky = M + 1, 2 * M + 1
         w, kc = N * Kx * cs, Kx * Ky * 16
+        kp = Kx * Ky * 8 if lo else kc            # a compact product / stage region
         if label.startswith("x_prod") or label.startswith("x_div"):
             b = (ni + no) * w
         elif label.startswith("y_inv"):
-            b = nf * kc + ni * w
+            b = nf * (kc + kp) / 2 + ni * w        # the state (stage 1) or the stage state (stage 2)
         elif label.startswith("y_fwd_compact"):
-            b = no * (w + kc)
+            b = no * (w + kp)
+        elif label.startswith("rk2mid_stage2d_lo"):
+            # stage 1: products, state in, k1 and stage state out; stage 2: products,
+            # T and u_dir of the stage state, state and k1 in, state out (mean of the two)
+            s1 = no * 8 + nf * 16 + 2 * nf * 8
+            s2 = no * 8 + (16 if nf == 3 else 0) + 2 * nf * 16 + nf * 8
+            b = (s1 + s2) / 2 * Kx * Ky
         elif label.startswith("rk2mid_stage2d"):
             b = nf * 5 * kc
         else:
@@ -426,8 +435,9 @@ class EnsembleRunner:
         cs = 16 if self.wl["precision"] == "fp64" else 8
         div = all(c.phys == 3 for c in self.ens.classes)     # divergence form: 3 inverse, 4 forward fields
         ni, no = (3, 4) if div else (5, 3)
-        b = bytes_2d(label, {n: self.sizes.count(n) for n in self.wl["sizes"]}, cs, ni, no, 3)
-        if b is not None and label.startswith("rk2mid_stage2d") and div:
+        lo = div and self.wl["precision"] == "fp32"          # the low-storage FP32 step
+        b = bytes_2d(label, {n: self.sizes.count(n) for n in self.wl["sizes"]}, cs, ni, no, 3, lo)
+        if b is not None and label.startswith("rk2mid_stage2d") and div and not lo:
             b *= 16.0 / 15.0                                  # one more product field read per stage
         return b
 

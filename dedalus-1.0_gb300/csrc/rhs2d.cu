@@ -142,7 +142,8 @@ __global__ void k_stage2(Stage2Args a) {
 // products, stage derivative k1 and stage state; N, the projection and the
 // buoyancy / stratification terms in float from float wavenumbers (k^2 exact
 // for integer wavenumbers); stage 1 forms the float stage state in float;
-// stage 2 updates the FP64 state in FP64 (y = f0 y + h phi1 k1 + 2 h phi2 (k2 - k1)).
+// stage 2 forms the increment h phi1 k1 + 2 h phi2 (k2 - k1) in float and adds
+// it to f0 y in FP64 (the state stays FP64).
 template <int NF, int MODE>
 __global__ void k_stage2_lo(Stage2Args a) {
     static_assert(MODE == 1 || MODE == 2, "RK2mid stages only");
@@ -224,10 +225,13 @@ __global__ void k_stage2_lo(Stage2Args a) {
                 ((float2*)a.ys.p[c])[ci2] = make_float2(fmaf(f1hf, N[c].x, (float)y0.x * f0f),
                                                         fmaf(f1hf, N[c].y, (float)y0.y * f0f));
             } else {
+                // the increment h phi1 k1 + 2 h phi2 (k2 - k1), float like k1 and k2,
+                // added to f0 y in FP64
                 const float2 d1 = ((const float2*)a.k1.p[c])[ci2];
-                ((double2*)a.y.p[c])[full] =
-                    etd2rk2_fma(y0, make_double2((double)d1.x, (double)d1.y),
-                                make_double2((double)N[c].x, (double)N[c].y), f0, f1 * a.h, 2. * f2 * a.h);
+                const float f1hf = (float)f1 * hf, f2hf = 2.f * (float)f2 * hf;
+                const float ir = fmaf(f1hf, d1.x, f2hf * (N[c].x - d1.x));
+                const float ii = fmaf(f1hf, d1.y, f2hf * (N[c].y - d1.y));
+                ((double2*)a.y.p[c])[full] = make_double2(fma(f0, y0.x, (double)ir), fma(f0, y0.y, (double)ii));
             }
         }
     }
