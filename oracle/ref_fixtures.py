@@ -22,14 +22,18 @@ How the reference is made to run under Python 3 (it is Python 2 code):
    the integer divisions that Python 2 performed on integer shapes, indexing
    with a list of slices, and numpy 2's removal of ``asfarray`` (each
    specific one listed with the reference line it touches).
-3. Modules that are absent here or unrelated to the arithmetic are stubbed:
+3. One correction of the reference's own code (``CORRECTIONS`` below): its
+   numpy backend of the shearing box scales the wrong array after the inverse
+   transform (representations.py:740), so that backend is brought to what the
+   FFTW backend computes.
+4. Modules that are absent here or unrelated to the arithmetic are stubbed:
    the FFTW wrapper (``dedalus/utils/fftw``; FFT.method = numpy is selected,
    the reference's own alternative backend, ``representations.py:327-333``),
    ``h5py`` (snapshots only), ``dedalus/funcs.py`` (IPython / Mercurial
    helpers) and ``dedalus/utils/api.py`` (re-exports only the timer and the
    parallel helpers).  mpi4py is absent, so the reference runs serially, as
    its ``CommunicationSystem`` allows (``utils/parallelism.py:28-50``).
-4. The Cython stage and dealias kernels are the reference's own, compiled
+5. The Cython stage and dealias kernels are the reference's own, compiled
    from their ``.pyx`` sources by ``oracle/build_ref.py`` into ``oracle/_ref``
    (the reference imports them by bare module name).
 
@@ -38,7 +42,9 @@ drawn in grid space and transformed with the reference's own forward
 transform): one ``RHS`` call and two or three ``RK2mid`` steps each of 2D
 hydro 32^2, 3D hydro 16^3, 2D Boussinesq 32^2 (direction y), 3D Boussinesq
 16^3 (direction z), 3D MHD 16^3 and 2D MHD 32^2, two ``RK2trap`` steps of 3D
-hydro 16x8x32 and of 2D Boussinesq 32^2, and ``compute_dt`` for each.
+hydro 16x8x32 and of 2D Boussinesq 32^2, in the shearing box
+(``FourierShearRepresentation``) one RHS call and two steps each of 2D and 3D
+hydro, 2D Boussinesq and 2D MHD (RK2trap), and ``compute_dt`` for each.
 Outputs go to ``tests/golden/ref_<case>.npz``.  The reference's RK4 cannot
 run (``RKBase.forward_step`` calls methods defined nowhere,
 ``time_step.py:209-218``), so no fixture exists for it.
@@ -115,6 +121,26 @@ SPECIFIC = [
      "mshape[-1] = mshape[-1] // 2 + 1", 624),
     ("dedalus/data_objects/representations.py", "gmshape[-1] = gmshape[-1] / 2 + 1",
      "gmshape[-1] = gmshape[-1] // 2 + 1", 646),
+    # np.ogrid now returns a tuple (a list in the numpy of the reference's time),
+    # which the next line assigns into; and the slices must be a tuple
+    ("dedalus/data_objects/representations.py",
+     "grid = refgrid[[slice(i) for i in np.asarray(self.local_shape['xspace'], dtype=np.float64)]]",
+     "grid = refgrid[tuple(slice(i) for i in np.asarray(self.local_shape['xspace'], dtype=np.float64))]\n"
+     "        if open:\n            grid = list(grid)", 539),
+]
+
+# (file, exact old text, new text, reference line): corrections of the
+# reference's own code, not Python 2 -> 3 rewrites.  Each makes the numpy
+# backend (the only one that runs here) do what the reference's FFTW backend,
+# the one its runs use, does.
+#  * FourierShearRepresentation.rev_np scales kdata by N after the inverse
+#    transforms where the x-space result needs it (the plain representation's
+#    rev_np scales its x-space result, representations.py:333; the FFTW
+#    backend's rev_fftw is unnormalised and needs no scale): as written the
+#    shearing box's x-space values come out N times too small.
+CORRECTIONS = [
+    ("dedalus/data_objects/representations.py", "        self.kdata *= self.global_shape['xspace'].prod()",
+     "        self.xdata *= self.global_shape['xspace'].prod()", 740),
 ]
 
 STUBS = {
@@ -140,10 +166,10 @@ def convert(text, rel):
             ln = re.sub(pat, rep, ln)
         out.append(ln)
     text = "\n".join(out)
-    for f, old, new, line in SPECIFIC:
+    for f, old, new, line in SPECIFIC + CORRECTIONS:
         if f == rel:
-            if old not in text:
-                raise RuntimeError("%s:%d: expected text not found: %r" % (rel, line, old))
+            if text.count(old) != 1:
+                raise RuntimeError("%s:%d: expected text found %d times: %r" % (rel, line, text.count(old), old))
             text = text.replace(old, new)
     return text
 
@@ -204,9 +230,10 @@ def _state(data, names):
     return {"%s%d" % (f, c): data[f][c]['kspace'].copy() for f, c in names}
 
 
-def run_case(mods, name, cls, shape, params, names, integrator, nsteps, dt, seed):
+def run_case(mods, name, cls, shape, params, names, integrator, nsteps, dt, seed,
+             rep_name="FourierRepresentation"):
     P, T = mods["physics"], mods["time_step"]
-    rep = mods["representations"].FourierRepresentation
+    rep = getattr(mods["representations"], rep_name)
     rng = np.random.Generator(np.random.PCG64(seed))
     RHS = getattr(P, cls)(shape, rep)
     RHS.parameters.update(params)
@@ -215,7 +242,8 @@ def run_case(mods, name, cls, shape, params, names, integrator, nsteps, dt, seed
     import platform
     out = {"numpy_version": np.__version__, "machine": platform.machine(),
            "shape": np.array(shape), "dt": dt, "nsteps": nsteps, "cls": cls, "integrator": integrator,
-           "params": repr(sorted(params.items())), "names": np.array(["%s%d" % n for n in names])}
+           "params": repr(sorted(params.items())), "names": np.array(["%s%d" % n for n in names]),
+           "rep": rep_name}
     for key, v in _state(data, names).items():
         out["in_" + key] = v
     # one RHS call on the input state
@@ -262,6 +290,17 @@ CASES = [
     ("bouss2d_32_trap", "BoussinesqHydro", (32, 32),
      {'nu': 2e-3, 'kappa': 2e-3, 'g': 1., 'alpha_t': 1., 'beta': 1., 'boussinesq_direction': 'y'},
      [('u', 0), ('u', 1), ('T', 0)], "RK2trap", 2, 1e-2, 8),
+    # the shearing box (representations.py:558-740, physics.py shear branches)
+    ("shear_hydro2d_32", "IncompressibleHydro", (32, 32), {'nu': 1e-2, 'shear_rate': 1.0},
+     [('u', 0), ('u', 1)], "RK2mid", 2, 1e-2, 11, "FourierShearRepresentation"),
+    ("shear_hydro3d_16", "IncompressibleHydro", (16, 16, 16), {'nu': 1e-2, 'shear_rate': 1.5},
+     [('u', 0), ('u', 1), ('u', 2)], "RK2mid", 2, 1e-2, 12, "FourierShearRepresentation"),
+    ("shear_bouss2d_32", "BoussinesqHydro", (32, 32),
+     {'nu': 2e-3, 'kappa': 2e-3, 'g': 1., 'alpha_t': 1., 'beta': 1., 'boussinesq_direction': 'y',
+      'shear_rate': 1.0},
+     [('u', 0), ('u', 1), ('T', 0)], "RK2mid", 2, 1e-2, 13, "FourierShearRepresentation"),
+    ("shear_mhd2d_32", "IncompressibleMHD", (32, 32), {'nu': 5e-3, 'eta': 5e-3, 'shear_rate': 0.8},
+     [('u', 0), ('u', 1), ('B', 0), ('B', 1)], "RK2trap", 2, 1e-2, 14, "FourierShearRepresentation"),
 ]
 
 
@@ -271,8 +310,9 @@ def main(ref_root="/root/reference"):
     tmp, mods = import_reference(ref_root)
     try:
         os.makedirs(GOLDEN, exist_ok=True)
-        for name, cls, shape, params, names, integ, nsteps, dt, seed in CASES:
-            out = run_case(mods, name, cls, shape, params, names, integ, nsteps, dt, seed)
+        for case in CASES:
+            name = case[0]
+            out = run_case(mods, *case)
             path = os.path.join(GOLDEN, "ref_%s.npz" % name)
             np.savez_compressed(path, **out)
             print("wrote %s (compute_dt %.6e)" % (os.path.relpath(path, ROOT), out["compute_dt"]))

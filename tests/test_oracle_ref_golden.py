@@ -20,7 +20,7 @@ import numpy as np
 import pytest
 
 from oracle import physics as OP, time_step as OT
-from oracle.representation import FourierRepresentation as OracleRep
+from oracle import representation as OR
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 FILES = sorted(glob.glob(os.path.join(GOLDEN, "ref_*.npz")))
@@ -40,7 +40,10 @@ def load(path):
 
 
 def physics(z, params):
-    rhs = getattr(OP, str(z["cls"]))(tuple(int(v) for v in z["shape"]), OracleRep)
+    # the plain Fourier representation, or the shearing box
+    # (representations.py:558-740) for the shear_* fixtures
+    rep = getattr(OR, str(z["rep"])) if "rep" in z.files else OR.FourierRepresentation
+    rhs = getattr(OP, str(z["cls"]))(tuple(int(v) for v in z["shape"]), rep)
     rhs.parameters.update(params)
     return rhs
 
@@ -53,7 +56,8 @@ def seeded(rhs, z, names):
 
 
 def test_fixtures_present():
-    assert len(FILES) == 8, FILES
+    assert len(FILES) == 12, FILES
+    assert sum(os.path.basename(f).startswith("ref_shear_") for f in FILES) == 4
 
 
 @pytest.mark.parametrize("path", FILES, ids=[os.path.basename(f)[4:-4] for f in FILES])
