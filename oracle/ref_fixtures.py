@@ -44,7 +44,8 @@ hydro 32^2, 3D hydro 16^3, 2D Boussinesq 32^2 (direction y), 3D Boussinesq
 16^3 (direction z), 3D MHD 16^3 and 2D MHD 32^2, two ``RK2trap`` steps of 3D
 hydro 16x8x32 and of 2D Boussinesq 32^2, in the shearing box
 (``FourierShearRepresentation``) one RHS call and two steps each of 2D and 3D
-hydro, 2D Boussinesq and 2D MHD (RK2trap), and ``compute_dt`` for each.
+hydro, 2D Boussinesq and 2D MHD (RK2trap), with rotation 2D and 3D hydro and,
+in the shearing box, 3D hydro and 3D Boussinesq, and ``compute_dt`` for each.
 Outputs go to ``tests/golden/ref_<case>.npz``.  The reference's RK4 cannot
 run (``RKBase.forward_step`` calls methods defined nowhere,
 ``time_step.py:209-218``), so no fixture exists for it.
@@ -301,6 +302,18 @@ CASES = [
      [('u', 0), ('u', 1), ('T', 0)], "RK2mid", 2, 1e-2, 13, "FourierShearRepresentation"),
     ("shear_mhd2d_32", "IncompressibleMHD", (32, 32), {'nu': 5e-3, 'eta': 5e-3, 'shear_rate': 0.8},
      [('u', 0), ('u', 1), ('B', 0), ('B', 1)], "RK2trap", 2, 1e-2, 14, "FourierShearRepresentation"),
+    # rotation (Omega = (Omega_z, Omega_y, Omega_x) in 3D, a scalar in 2D; physics.py:551-565)
+    ("rot_hydro3d_16", "IncompressibleHydro", (16, 16, 16), {'nu': 1e-2, 'Omega': [0.7, -0.2, 0.3]},
+     [('u', 0), ('u', 1), ('u', 2)], "RK2mid", 2, 1e-2, 15),
+    ("rot_hydro2d_32", "IncompressibleHydro", (32, 32), {'nu': 1e-2, 'Omega': 0.8},
+     [('u', 0), ('u', 1)], "RK2mid", 2, 1e-2, 16),
+    ("shear_rot_hydro3d_16", "IncompressibleHydro", (16, 16, 16),
+     {'nu': 1e-2, 'shear_rate': 1.5, 'Omega': [1.0, 0.0, 0.0]},
+     [('u', 0), ('u', 1), ('u', 2)], "RK2mid", 2, 1e-2, 17, "FourierShearRepresentation"),
+    ("shear_rot_bouss3d_16", "BoussinesqHydro", (16, 16, 16),
+     {'nu': 2e-3, 'kappa': 2e-3, 'g': 1., 'alpha_t': 1., 'beta': 1., 'shear_rate': 1.2,
+      'Omega': [1.0, 0.0, 0.0]},
+     [('u', 0), ('u', 1), ('u', 2), ('T', 0)], "RK2mid", 2, 1e-2, 18, "FourierShearRepresentation"),
 ]
 
 

@@ -4,7 +4,8 @@
 (run under Python 3 after mechanical rewrites, with its compiled Cython
 kernels and FFT.method = numpy; ``oracle/ref_fixtures.py``).  Here the
 library's public classes -- the same physics, representation and
-integrators, on the GPU -- start from the stored inputs and must reproduce
+integrators, on the GPU; the shearing box and rotation through the
+reference-ordered path -- start from the stored inputs and must reproduce
 the stored RHS, every stored RK2mid / RK2trap step and the CFL dt:
 relative L2 <= 1e-12 over all fields, dt to 1e-12 relative."""
 import glob
@@ -14,11 +15,7 @@ import numpy as np
 import pytest
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-# the plain-representation fixtures; the shearing-box ones (ref_shear_*) pin the
-# oracle (tests/test_oracle_ref_golden.py), against which tests/test_gpu_shear.py
-# checks the CUDA shearing-box path
-FILES = sorted(f for f in glob.glob(os.path.join(GOLDEN, "ref_*.npz"))
-               if not os.path.basename(f).startswith("ref_shear_"))
+FILES = sorted(glob.glob(os.path.join(GOLDEN, "ref_*.npz")))
 
 
 def rel_l2(got, ref):
@@ -41,8 +38,11 @@ def test_cuda_path_matches_reference_execution(dd, cuda, path):
     M = dd.mods
     shape = tuple(int(v) for v in z["shape"])
 
+    # the plain Fourier representation, or the shearing box for the shear_* fixtures
+    rep = getattr(M, str(z["rep"])) if "rep" in z.files else M.FourierRepresentation
+
     def seeded():
-        rhs = getattr(M, str(z["cls"]))(shape, M.FourierRepresentation)
+        rhs = getattr(M, str(z["cls"]))(shape, rep)
         rhs.parameters.update(params)
         data = rhs.create_fields(0.)
         for f, c in names:

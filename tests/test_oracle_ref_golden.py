@@ -56,8 +56,8 @@ def seeded(rhs, z, names):
 
 
 def test_fixtures_present():
-    assert len(FILES) == 12, FILES
-    assert sum(os.path.basename(f).startswith("ref_shear_") for f in FILES) == 4
+    assert len(FILES) == 16, FILES
+    assert sum(os.path.basename(f).startswith("ref_shear_") for f in FILES) == 6
 
 
 @pytest.mark.parametrize("path", FILES, ids=[os.path.basename(f)[4:-4] for f in FILES])
