@@ -45,7 +45,9 @@ hydro 32^2, 3D hydro 16^3, 2D Boussinesq 32^2 (direction y), 3D Boussinesq
 hydro 16x8x32 and of 2D Boussinesq 32^2, in the shearing box
 (``FourierShearRepresentation``) one RHS call and two steps each of 2D and 3D
 hydro, 2D Boussinesq and 2D MHD (RK2trap), with rotation 2D and 3D hydro and,
-in the shearing box, 3D hydro and 3D Boussinesq, and ``compute_dt`` for each.
+in the shearing box, 3D hydro and 3D Boussinesq, in boxes whose sides are not
+2 pi 3D hydro (anisotropic, hyperviscous), 3D MHD and 2D Boussinesq, and
+``compute_dt`` for each.
 Outputs go to ``tests/golden/ref_<case>.npz``.  The reference's RK4 cannot
 run (``RKBase.forward_step`` calls methods defined nowhere,
 ``time_step.py:209-218``), so no fixture exists for it.
@@ -232,11 +234,11 @@ def _state(data, names):
 
 
 def run_case(mods, name, cls, shape, params, names, integrator, nsteps, dt, seed,
-             rep_name="FourierRepresentation"):
+             rep_name="FourierRepresentation", length=None):
     P, T = mods["physics"], mods["time_step"]
     rep = getattr(mods["representations"], rep_name)
     rng = np.random.Generator(np.random.PCG64(seed))
-    RHS = getattr(P, cls)(shape, rep)
+    RHS = getattr(P, cls)(shape, rep, length=length)
     RHS.parameters.update(params)
     data = RHS.create_fields(0.)
     seed_state(rng, RHS, data, names)
@@ -244,7 +246,7 @@ def run_case(mods, name, cls, shape, params, names, integrator, nsteps, dt, seed
     out = {"numpy_version": np.__version__, "machine": platform.machine(),
            "shape": np.array(shape), "dt": dt, "nsteps": nsteps, "cls": cls, "integrator": integrator,
            "params": repr(sorted(params.items())), "names": np.array(["%s%d" % n for n in names]),
-           "rep": rep_name}
+           "rep": rep_name, "length": np.array(length if length is not None else [2 * np.pi] * len(shape))}
     for key, v in _state(data, names).items():
         out["in_" + key] = v
     # one RHS call on the input state
@@ -255,7 +257,7 @@ def run_case(mods, name, cls, shape, params, names, integrator, nsteps, dt, seed
     # a fresh physics object and state for the integrator: the integrating
     # factors are attached to the derivative fields of the first RHS call
     # (physics.py:573-574), which must be the integrator's own
-    RHS = getattr(P, cls)(shape, rep)
+    RHS = getattr(P, cls)(shape, rep, length=length)
     RHS.parameters.update(params)
     data = RHS.create_fields(0.)
     for (f, c) in names:
@@ -314,6 +316,15 @@ CASES = [
      {'nu': 2e-3, 'kappa': 2e-3, 'g': 1., 'alpha_t': 1., 'beta': 1., 'shear_rate': 1.2,
       'Omega': [1.0, 0.0, 0.0]},
      [('u', 0), ('u', 1), ('u', 2), ('T', 0)], "RK2mid", 2, 1e-2, 18, "FourierShearRepresentation"),
+    # boxes whose sides are not 2 pi (non-integer wavenumbers) and hyperviscosity
+    ("box_hydro3d_16x16x32_vo2", "IncompressibleHydro", (16, 16, 32), {'nu': 2e-4, 'viscosity_order': 2},
+     [('u', 0), ('u', 1), ('u', 2)], "RK2mid", 2, 1e-2, 19, "FourierRepresentation", (3.0, 5.0, 7.0)),
+    ("box_mhd3d_16", "IncompressibleMHD", (16, 16, 16), {'nu': 5e-3, 'eta': 7e-3},
+     [('u', 0), ('u', 1), ('u', 2), ('B', 0), ('B', 1), ('B', 2)], "RK2mid", 2, 1e-2, 20,
+     "FourierRepresentation", (4.0, 4.0, 4.0)),
+    ("box_bouss2d_32", "BoussinesqHydro", (32, 32),
+     {'nu': 2e-3, 'kappa': 2e-3, 'g': 1., 'alpha_t': 1., 'beta': 1., 'boussinesq_direction': 'y'},
+     [('u', 0), ('u', 1), ('T', 0)], "RK2mid", 2, 1e-2, 21, "FourierRepresentation", (2 * np.pi, 4.0)),
 ]
 
 

@@ -40,9 +40,10 @@ def test_cuda_path_matches_reference_execution(dd, cuda, path):
 
     # the plain Fourier representation, or the shearing box for the shear_* fixtures
     rep = getattr(M, str(z["rep"])) if "rep" in z.files else M.FourierRepresentation
+    length = tuple(float(v) for v in z["length"]) if "length" in z.files else None
 
     def seeded():
-        rhs = getattr(M, str(z["cls"]))(shape, rep)
+        rhs = getattr(M, str(z["cls"]))(shape, rep, length=length)
         rhs.parameters.update(params)
         data = rhs.create_fields(0.)
         for f, c in names:

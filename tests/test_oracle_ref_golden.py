@@ -43,7 +43,8 @@ def physics(z, params):
     # the plain Fourier representation, or the shearing box
     # (representations.py:558-740) for the shear_* fixtures
     rep = getattr(OR, str(z["rep"])) if "rep" in z.files else OR.FourierRepresentation
-    rhs = getattr(OP, str(z["cls"]))(tuple(int(v) for v in z["shape"]), rep)
+    length = tuple(float(v) for v in z["length"]) if "length" in z.files else None
+    rhs = getattr(OP, str(z["cls"]))(tuple(int(v) for v in z["shape"]), rep, length=length)
     rhs.parameters.update(params)
     return rhs
 
@@ -56,7 +57,7 @@ def seeded(rhs, z, names):
 
 
 def test_fixtures_present():
-    assert len(FILES) == 16, FILES
+    assert len(FILES) == 19, FILES
     assert sum(os.path.basename(f).startswith("ref_shear_") for f in FILES) == 6
 
 
